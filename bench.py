@@ -1,0 +1,339 @@
+"""Benchmark: accepted Metropolis moves/s of batched water chains on one GB300 (and N GPUs).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the reference's batched configuration): 256 independent rigid 3-site water chains,
+512-8192 molecules each (log-uniform), 0.0334 molecules/A^3, 280-360 K, one seed per chain,
+switched LJ + Coulomb 10-12 A, Verlet skin 2 A, residue translations <= 0.15 A and rotations <=
+15 deg, physical acceptance units.  One step = one sweep: every chain performs as many trial moves
+as it has molecules, in one persistent kernel launch (replayed from a CUDA graph).  Data are
+synthetic (seeded), the working set (2.1 M atoms, 1.5 GB of neighbour lists) exceeds L2, so no
+flush is needed between steps.
+
+Reported: `value` = accepted moves/s over all GPUs (device time, CUDA events on the library's
+stream, max over ranks); `e2e` = the same through the host-buffer API (coordinates copied in and
+out every step, wall clock); `roofline` = FP32 throughput of the sweep kernel (68 flops per pair
+interaction, SURVEY's count) against an FFMA probe measured in the same run; `cpu_baseline` = the
+reference's algorithm (oracle/ port, two full energies per move, OpenMP-free per chain, chains in
+parallel on all host cores) on a bounded stratified sample of the same chains.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_PAIR = 68.0
+WORKLOAD = "256 rigid water chains, 512-8192 molecules (log-uniform), 0.0334 mol/A^3, 280-360 K"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_chains(rank: int, nchains: int):
+    from mc_cpp_gb300 import systems
+    return systems.water_chains(nchains=nchains, seed=3 + 7919 * rank)
+
+
+# ------------------------------------------------------------------ clocks during the timed region
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline (reference algorithm)
+def cpu_sample(chains, budget_s: float, threads: int, seed: int = 17):
+    """Runs the reference's Metropolis algorithm (two full getE per move, oracle/ port) on a
+    stratified sample of the chains, one chain per host thread, and estimates the accepted-moves/s
+    rate of the whole workload on `threads` cores.  Returns (rate, description, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    sizes = np.array([c.natom for c in chains])
+    order = np.argsort(sizes)
+    nsamp = min(threads, len(chains))
+    picks = [int(order[int((k + 0.5) * len(chains) / nsamp)]) for k in range(nsamp)]
+    groups = np.array_split(order, nsamp)          # each sample stands for one size stratum
+    weight = [float(sum(chains[i].natom // 3 for i in g)) for g in groups]
+    res = [None] * nsamp
+
+    def work(k):
+        s = chains[picks[k]]
+        o = orc.Oracle(s)
+        o.set_acceptance_units("physical")
+        t0 = time.perf_counter()
+        o.energy()
+        e_cost = time.perf_counter() - t0
+        nmv = int(max(2, min(400, budget_s / max(1e-6, 2.0 * e_cost))))
+        t0 = time.perf_counter()
+        _, _, acc = o.mc_run(nmv, seed + k, trace=False)
+        res[k] = (nmv, acc, time.perf_counter() - t0)
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(nsamp)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    # stratum s: W_s moves per sweep, acceptance a_s/m_s, time per move t_s/m_s
+    acc_moves = sum(w * r[1] / r[0] for w, r in zip(weight, res))
+    cpu_time = sum(w * r[2] / r[0] for w, r in zip(weight, res))
+    rate = acc_moves / cpu_time * threads
+    desc = ("reference algorithm on %d chains (one per size stratum, %d-%d atoms), %d-%d moves each, "
+            "weighted by molecules per stratum; %d threads" % (nsamp, min(sizes[picks]), max(sizes[picks]),
+                                                              min(r[0] for r in res), max(r[0] for r in res), threads))
+    return rate, desc, threads
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    chains = make_chains(0, args.chains)
+    threads = host_threads()
+    for _ in range(args.warmup):
+        cpu_sample(chains, 0.5, threads)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, desc, cores = cpu_sample(chains, args.ref_budget, threads)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    v = float(np.mean(rates))
+    line = {"impl": "reference", "metric": "accepted MC moves/s", "value": v, "unit": "moves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "chains": args.chains, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "moves/s", "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def traffic_from_profiles():
+    p = os.path.join(ROOT, "profiles", "k_batch_sweep_water256.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(ln.split(":")[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from mc_cpp_gb300 import native
+    from mc_cpp_gb300.engine import BatchChains, FFieldCUDA
+    from mc_cpp_gb300 import systems
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def allmax(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def allsum(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        return float(t.item())
+
+    chains = make_chains(rank, args.chains)
+    B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank)
+    natoms = B.natoms
+    B.sweep(args.warmup)
+    barrier()
+    t0, a0, _ = B.stats()
+    p0 = B.pairs()
+    with ClockSampler(local) as clk:
+        barrier()
+        ms = B.time_sweeps(args.steps)
+        barrier()
+    t1, a1, e1 = B.stats()
+    p1 = B.pairs()
+    acc = float((a1 - a0).sum())
+    trials = float((t1 - t0).sum())
+    pairs = float((p1 - p0).sum())
+    ms_max = allmax(ms)
+    acc_all = allsum(acc)
+    value = acc_all / (ms_max * 1e-3)
+    # roofline of the sweep kernel (the only kernel in the timed region)
+    peak = native.lib()
+    import ctypes as C
+    tf = C.c_double(0)
+    native.check(peak.mcg_probe_fp32_tflops(C.byref(tf)))
+    achieved = pairs * FLOPS_PER_PAIR / (ms * 1e-3 / args.steps) / args.steps / 1e12
+    traffic = traffic_from_profiles()
+    # e2e: host buffers in and out through the public API every step (pinned host memory)
+    hin = torch.empty((3, natoms), dtype=torch.float64, pin_memory=True).numpy()
+    hout = torch.empty((3, natoms), dtype=torch.float64, pin_memory=True).numpy()
+    B.run_host(None, 0, hout)
+    hin[:] = hout
+    barrier()
+    t_e = time.perf_counter()
+    acc_e = 0
+    a_prev = B.stats()[1]
+    for _ in range(args.steps):
+        a_now, _ = B.run_host(hin, 1, hout)
+        acc_e += int((a_now - a_prev).sum())
+        a_prev = a_now
+        hin, hout = hout, hin
+    barrier()
+    e2e_s = allmax(time.perf_counter() - t_e)
+    e2e = allsum(acc_e) / e2e_s
+    # plain single-chain FP64 path (host-driven replay of MC_metropolis on one water box)
+    plain = None
+    if rank == 0 and not args.no_plain:
+        w = systems.water_box()
+        ff = FFieldCUDA(w, "fp64")
+        ff.metropolis(50, 7, acceptance="physical", trace=False)
+        tp = time.perf_counter()
+        _, _, nacc, _ = ff.metropolis(args.plain_steps, 11, acceptance="physical", trace=False)
+        dt = time.perf_counter() - tp
+        plain = {"accepted_moves_per_s": nacc / dt, "moves_per_s": args.plain_steps / dt,
+                 "workload": "one 4096-molecule water box, FP64, MC_metropolis replay through the C ABI",
+                 "steps": args.plain_steps}
+        ff.close()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, desc, cores = cpu_sample(chains, args.cpu_budget, host_threads())
+        cpu = {"value": rate, "unit": "moves/s", "cores": cores, "kind": "port", "sample": desc}
+    rb, nl = B.counters()
+    if rank == 0:
+        line = {
+            "metric": "accepted MC moves/s", "value": value, "unit": "moves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pair terms, f64 sums and acceptance, 64-bit fixed-point coordinates",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "chains": args.chains, "atoms_per_gpu": natoms,
+                       "molecules_per_sweep_per_gpu": int(natoms // 3),
+                       "l2": "no flush: per-sweep working set (1.5 GB lists, 134 MB coordinates) > 129 MB L2",
+                       "acceptance": "physical", "parallelism": "independent chains, weak scaling over GPUs"},
+            "trials_per_s": allsum(trials) / (ms_max * 1e-3),
+            "acceptance_ratio": acc / max(1.0, trials),
+            "pair_interactions_per_s": allsum(pairs) / (ms_max * 1e-3),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": tf.value, "unit": "TFLOP/s",
+                         "frac": achieved / tf.value if tf.value > 0 else None, "traffic": traffic,
+                         "peak_source": "FFMA-chain probe kernel measured in this run (no FP32 figure in MEASURED_PEAKS.json)",
+                         "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
+            "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(3 * natoms * 8),
+                    "d2h_bytes_per_step": int(3 * natoms * 8 + args.chains * 16)},
+            "gpu_launches": args.steps,
+            "list_rebuilds_total": int(rb),
+            "clocks": clk.summary(),
+            "plain_fp64": plain,
+            "batched_vs_plain_accepted": (value / plain["accepted_moves_per_s"]) if plain else None,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    B.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work per sampled chain")
+    ap.add_argument("--ref-budget", type=float, default=3.0, help="seconds per sampled chain per reference step")
+    ap.add_argument("--plain-steps", type=int, default=2000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

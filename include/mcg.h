@@ -1,0 +1,195 @@
+/*
+ * mcg.h — C ABI of the GB300 nonbonded Monte Carlo energy engine (libmcgpu.so).
+ *
+ * This is the drop-in boundary for FHedin/mc_cpp's energy path: every entry point below replaces
+ * one member of the reference's FField / List_nonBonded / MC_metropolis call graph or of its
+ * existing C ABI (src/FORTRAN_interface.cpp).  Plain pointers and sizes only; no C++ or CUDA types
+ * cross this boundary.  All energies are in the reference's internal units
+ * (1 kcal/mol = 418.4 iu, include/Constants.hpp:29) unless a function says otherwise.
+ *
+ * Error convention: every function returns an int status, MCG_OK (0) or a negative MCG_E* code,
+ * and never exits the process.  mcg_last_error() describes the most recent failure of the calling
+ * thread.  (The reference prints to cerr and calls exit(); the C++ adapter FField_CUDA maps a
+ * non-zero status back to that convention.)
+ *
+ * Threading: a handle is single-owner; calls on one handle must not overlap.  Each handle owns one
+ * CUDA stream on the device that was current when it was created.
+ */
+#ifndef MCG_H
+#define MCG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCG_ABI_VERSION 1
+
+enum mcg_status {
+    MCG_OK = 0,
+    MCG_EINVAL = -1,     /* invalid argument or inconsistent system description */
+    MCG_ECUDA = -2,      /* CUDA runtime error (no device, out of memory, launch failure) */
+    MCG_ECAPACITY = -3,  /* a fixed-capacity device structure overflowed and could not grow */
+    MCG_ETIMEOUT = -4,   /* a bounded device-side wait gave up */
+    MCG_ENOTSUP = -5,    /* feature combination not supported */
+    MCG_EIO = -6         /* file could not be read or parsed */
+};
+
+enum mcg_pbc { MCG_PBC_NONE = 0, MCG_PBC_CUBIC = 1, MCG_PBC_ORBIC = 2 };
+enum mcg_cut { MCG_CUT_FULL = 0, MCG_CUT_SWITCH = 1 };
+enum mcg_precision {
+    MCG_PREC_FP64 = 0,   /* plain: every pair term in FP64, reference arithmetic */
+    MCG_PREC_MIXED = 1   /* FP32 pair terms on exact displacements, FP64 accumulation */
+};
+enum mcg_move_type { MCG_MOVE_TRN = 1, MCG_MOVE_ROT = 2 };
+enum mcg_move_mode { MCG_MODE_RESIDUE = 0, MCG_MODE_ALL = 1, MCG_MODE_ATOM = 2 };
+enum mcg_acceptance {
+    MCG_ACCEPT_REFERENCE = 0, /* beta in mol/kcal applied to dE in iu, as MC_metropolis.cpp:188 */
+    MCG_ACCEPT_PHYSICAL = 1   /* beta applied to dE in kcal/mol */
+};
+
+/* One system: what the reference's Parser_XML + IO_MDBAS build (AtomList, PerConditions,
+ * Ens_NVT, FField cut settings and the bonded lists).  Per-atom arrays have natom entries; topology
+ * arrays hold 0-based atom indices; parameters are in forcefield-file units (kcal/mol, Angstrom,
+ * degrees) and are converted exactly as IO_MDBAS::read_ff does (src/IO_MDBAS.cpp:186-467). */
+typedef struct mcg_system_desc {
+    int natom;
+    const double *x, *y, *z;
+    const double *q;
+    const double *eps, *sig;        /* file epsilon (kcal/mol, stored as sqrt(eps*418.4)); MDBAS half-sigma */
+    const double *eps14, *sig14;
+    const double *mass;             /* may be NULL (all 1); used for centre-of-mass rotation pivots */
+    const unsigned char *frozen;    /* may be NULL (none frozen) */
+    const int *resid;               /* global residue ids, 1-based and consecutive; may be NULL */
+    int pbc_type;                   /* enum mcg_pbc */
+    double box[3];                  /* a, b, c (cubic uses a) */
+    int cut_mode;                   /* enum mcg_cut */
+    double cutoff, cuton, dcut;     /* switch: rc, ron, Verlet skin (reference defaults 12, 10, 2) */
+    double temp;                    /* K */
+    int precision;                  /* enum mcg_precision */
+    int nbond;  const int *bond_atoms;  const int *bond_type;  const double *bond_k, *bond_r0, *bond_beta;
+    int nub;    const int *ub_atoms;    const double *ub_k, *ub_r0;
+    int nangle; const int *angle_atoms; const int *angle_type; const double *angle_k, *angle_theta0;
+    int ndihe;  const int *dihe_atoms;  const int *dihe_type, *dihe_order; const double *dihe_k, *dihe_phi0, *dihe_mult;
+    int nimpr;  const int *impr_atoms;  const int *impr_type, *impr_order; const double *impr_k, *impr_phi0, *impr_mult;
+} mcg_system_desc;
+
+typedef struct mcg_system mcg_system;
+
+int mcg_abi_version(void);
+const char* mcg_last_error(void);
+/* Number of CUDA devices visible to the library (0 without a GPU); never fails. */
+int mcg_device_count(void);
+
+/* --- single system: FField_CUDA's engine ------------------------------------------------------
+ * mcg_create replaces `new FField_MDBAS(...)` + `new List_nonBonded(...)` + `setExcl`
+ * (src/Parser.cpp:139-153,210-211): builds exclusion and 1-4 lists on the host
+ * (List_nonBonded::build_exclude_list, src/List_nonBonded.cpp:143-775) and, in switch mode, the
+ * Verlet list on the device (init/update_verlet_list, :777-915). */
+int mcg_create(const mcg_system_desc* desc, mcg_system** out);
+int mcg_destroy(mcg_system* s);
+
+/* AtomList::setCoords for all atoms (src/FORTRAN_interface.cpp:77-82 set_coords_). */
+int mcg_set_coords(mcg_system* s, const double* x, const double* y, const double* z);
+int mcg_get_coords(mcg_system* s, double* x, double* y, double* z);
+
+/* FField::getE(double ener[10]) (src/FField_MDBAS.cpp:77-106): full recompute on the device with
+ * the current list; ener = [tot, pot, kin(=0), elec, vdw, bond, ang, ub, dihe, impr] in iu. */
+int mcg_energy(mcg_system* s, double ener[10]);
+
+/* FField::askListUpdate (src/FField.cpp:222-235): rebuild the Verlet list from the current
+ * coordinates with a device cell list.  No-op in full mode. */
+int mcg_update_lists(mcg_system* s);
+
+/* Energy change of moving atoms[0..n) to (nx,ny,nz), nonbonded (current list, same cutoff, switch,
+ * exclusion and 1-4 rules as mcg_energy) plus the bonded terms that touch them.  Equals
+ * E(after) - E(before) as the reference computes it in MC_metropolis.cpp:94-123 (two getE calls),
+ * without its cancellation error.  The proposal is kept until the next mcg_delta_e / mcg_commit.
+ * 1 <= n <= 1024. */
+int mcg_delta_e(mcg_system* s, int n, const int* atoms, const double* nx, const double* ny,
+                const double* nz, double* de);
+/* Apply the last proposal's coordinates on the device (an accepted move). */
+int mcg_commit(mcg_system* s);
+
+/* Half Verlet list of the current build: for each atom i the partners j > i (List_nonBonded
+ * getNeighPair/getNeighList).  counts[natom] always filled; entries (row-concatenated, each row
+ * sorted ascending) filled when cap is large enough; *total = sum(counts). */
+int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);
+/* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
+ * exclList[i]) and the 1-4 pair list (getNeighList14). */
+int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);
+int mcg_get_pairs14(mcg_system* s, int* pairs, int cap, int* n14);
+/* Host-only (no device needed): validate a description and build its exclusion rows and 1-4
+ * pairs as List_nonBonded::build_exclude_list does (src/List_nonBonded.cpp:143-775). */
+int mcg_build_exclusions(const mcg_system_desc* desc, int* counts, int* entries, int64_t cap, int64_t* total,
+                         int* pairs14, int cap14, int* n14);
+
+/* --- Metropolis driver: MC_metropolis::run on this engine ------------------------------------
+ * Moves are registered like List_Moves::addNewMoveType (src/List_Moves.cpp:257-457);
+ * sele[natom] holds the Selection flags.  mcg_metropolis_run follows MC_metropolis::run's draw
+ * order with libstdc++'s mt19937 + uniform_real_distribution (MC.cpp:110-156), applies moves on
+ * the host exactly as Move.hpp does, and takes dE from mcg_delta_e.  The Verlet list is rebuilt
+ * every 50 steps (MC_metropolis.cpp:151).  trace (may be NULL) receives 12 doubles per step:
+ * st, imvtyp, imvatm, r0, r1, r2, rang, eold, enew, de, alpha (-1 if not drawn), accepted.
+ * With follow != NULL (nsteps*2 ints: imvtyp, accepted per step), accept decisions are taken from
+ * it when they disagree with this engine's (a tie); ties are counted in *n_ties. */
+int mcg_add_move(mcg_system* s, int type, int mode, const int* sele, double dmax, double target, int each);
+int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
+                       const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties);
+
+/* --- batched independent chains ----------------------------------------------------------------
+ * Hundreds of NVT chains of rigid molecules (each chain: identical residues of 1..8 atoms, all
+ * intra-residue pairs excluded, residue moves TRN + ROT as in MC_metropolis) advance in one
+ * persistent kernel per sweep (one sweep = nres(chain) trial moves per chain), mixed precision,
+ * per-chain Philox4x32-10 streams, per-chain Verlet lists rebuilt on the device when any atom
+ * has moved more than half the skin.  Coordinates stay resident on the device. */
+typedef struct mcg_batch mcg_batch;
+
+typedef struct mcg_batch_opts {
+    double dmax_trn;          /* Angstrom */
+    double dmax_rot;          /* degrees */
+    int acceptance_units;     /* enum mcg_acceptance */
+    int threads_per_chain;    /* 0 = autotuned */
+    int list_capacity;        /* 0 = automatic: maximum list entries per residue */
+    uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
+} mcg_batch_opts;
+
+/* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */
+int mcg_batch_create(const mcg_system_desc* chains, int nchains, const mcg_batch_opts* opts, mcg_batch** out);
+int mcg_batch_destroy(mcg_batch* b);
+/* Run nsweeps sweeps (one kernel launch each, replayed from a captured CUDA graph). */
+int mcg_batch_sweep(mcg_batch* b, int nsweeps);
+/* Same, host-synchronous, returning per-chain totals: trials, accepted, running E (iu). */
+int mcg_batch_stats(mcg_batch* b, int64_t* trials, int64_t* accepted, double* etot);
+/* Fresh FP64 recompute of every chain's nonbonded energy (iu) with a freshly built list. */
+int mcg_batch_energy_fp64(mcg_batch* b, double* e);
+int mcg_batch_get_coords(mcg_batch* b, int chain, double* x, double* y, double* z);
+int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double* y, const double* z);
+/* Run nsweeps sweeps and return their device time in milliseconds (CUDA events on the handle's
+ * stream, synchronised on both sides). */
+int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms);
+/* Host-buffer run: when xyz_in != NULL, copy all chains' coordinates in (3*natoms doubles: x for
+ * every atom of every chain, then y, then z), rebuild the lists and recompute the running
+ * energies; run nsweeps sweeps; when xyz_out != NULL copy the coordinates back; fill accepted and
+ * etot (nchains entries each, may be NULL).  Host-synchronous. */
+int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* xyz_out, int64_t* accepted,
+                       double* etot);
+/* Mixed-precision recompute of every chain's energy over its neighbour lists (iu). */
+int mcg_batch_energy_mixed(mcg_batch* b, double* e);
+/* Pair interactions evaluated so far by each chain (pairs inside the cutoff before or after a move). */
+int mcg_batch_pairs(mcg_batch* b, int64_t* pairs);
+/* Total number of atoms over all chains, and a chain's atom count. */
+int64_t mcg_batch_natoms(mcg_batch* b);
+int mcg_batch_chain_natoms(mcg_batch* b, int chain);
+/* Counters of the last sweeps: list rebuilds done, kernel launches issued by this handle. */
+int mcg_batch_counters(mcg_batch* b, int64_t* list_rebuilds, int64_t* kernel_launches);
+
+/* FP32 FMA throughput of the current device in TFLOP/s, measured by an FFMA-chain kernel
+ * (the denominator of the pair kernels' roofline). */
+int mcg_probe_fp32_tflops(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCG_H */

@@ -1,0 +1,991 @@
+// Batched independent NVT chains: one persistent CTA per chain per sweep.
+//
+// Each chain is a box of identical rigid residues (1..8 atoms: argon, 3-site water ...).  A sweep
+// is nres trial moves per chain, performed in order as MC_metropolis::run does
+// (src/MC_metropolis.cpp:80-165): pick TRN or ROT uniformly, a residue uniformly and, for ROT, a
+// pivot atom of it uniformly (the reference lists one move instance per selected atom,
+// List_Moves.cpp:393-440), draw a displacement uniform in the dmax ball or an axis and an angle
+// uniform in [-dmax, dmax] degrees, compute dE against the residue's neighbours, accept with the
+// Metropolis test (MC_metropolis.cpp:175-204).  Differences from the reference, all deliberate:
+// random numbers come from a per-chain Philox4x32-10 stream (counter = move index), rotations use
+// the minimum-image offset from the pivot (the reference rotates raw coordinates of residues
+// straddling the box, Move.hpp:145-183, and can tear them apart), and the neighbour list is
+// rebuilt whenever an atom has moved more than half the skin since the last build (the reference
+// rebuilds every 50 steps whatever the displacement, MC_metropolis.cpp:151), so no pair inside
+// the cutoff is ever missed.
+//
+// HBM layout (pools over all chains, chain c owns a contiguous slice):
+//   M[atoms]      ulonglong4  master coordinates as 64-bit fixed-point box fractions (x, y, z):
+//                 exact, wrap-free integer updates, resolution L/2^64 (finer than FP64 anywhere in
+//                 the box); FP64 views (x = int64 * L/2^64) are formed only for output and checks
+//   F[atoms]      uint4    32-bit mirror = the high words of M (w = residue slot type)
+//   FB[atoms]     uint4    mirror positions at the last list build (displacement check)
+//   LST[res*cap]  uint16   neighbour residues of each residue (any atom pair within rc + skin)
+//   NL[res]       int      list lengths
+//   chains[c]     ChainDev parameters; state[c] ChainState counters and the running energy
+//
+// Precision: 64-bit fixed-point master coordinates (the box wrap is the integer overflow), FP64
+// running energy, dE sum and acceptance threshold -ln(alpha)/beta; FP32 pair terms on exact
+// fixed-point displacements (mixed_pair_delta).  GB300's FP64 rate is a small fraction of its
+// FP32 rate, so no FP64 arithmetic sits on the per-move critical path except one compare: the
+// threshold is computed by a warp that would otherwise wait at the barrier.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+#include "mcg.h"
+#include "pair_math.cuh"
+
+namespace mcg {
+
+#define BK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(MCG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int MAX_APR = 8;
+constexpr int MAX_CELLS = 4096;
+constexpr double TWO64 = 18446744073709551616.0;
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11): 10 rounds of the 4x32 Philox S-box with the published multipliers and Weyl key
+// increments.
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32_10(U4 ctr, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        ctr = U4{hi1 ^ ctr.y ^ k0, lo1, hi0 ^ ctr.w ^ k1, lo0};
+        k0 += W0;
+        k1 += W1;
+    }
+    return ctr;
+}
+
+__device__ __forceinline__ float u01f(uint32_t v) { return (float)(v >> 8) * (1.0f / 16777216.0f); }
+// (0, 1]: never 0, so -ln(alpha) is finite
+__device__ __forceinline__ double u01d_open0(uint32_t hi, uint32_t lo) {
+    return ((double)(((uint64_t)hi << 21) ^ (uint64_t)(lo >> 11)) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+struct ChainDev {
+    int atom0, res0, nres, apr;
+    double L[3], rL[3];
+    double tofix[3];      // 2^64 / L : Angstrom -> master units
+    float Ls[3];          // L / 2^32 : mirror units -> Angstrom
+    double beta;
+    float dmax_trn, dmax_rot;
+    int ntypes_move;      // 1: TRN only, 2: TRN + ROT
+    uint32_t key0, key1;
+    float tab[MAX_APR][MAX_APR][4];   // (qk, e4, ss, 0) per slot pair
+};
+
+struct ChainState {
+    double etot;
+    long long trials, accepted;
+    long long pairs;            // pair interactions evaluated (inside rc before or after a move)
+    unsigned long long moves;   // Philox counter
+    int rebuilds;
+    int err;
+};
+
+struct BatchGeom {
+    float c2f, n2f, sw2f;
+    float rlist2;      // (rc + skin)^2
+    float rcent2;      // (rc + skin + 2 rext)^2, residue-centre prefilter
+    float half_skin2;  // (skin/2)^2
+    float cellmin;     // cell edge for the 5-stencil
+    int cap;
+};
+
+__device__ __forceinline__ float fdelta(uint32_t a, uint32_t b, float Ls) { return __int2float_rn((int)(b - a)) * Ls; }
+
+__device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
+    return (int)((((v + 0x80000000u) >> 8) * (uint64_t)nc) >> 24);
+}
+
+// ---- neighbour list build for one chain by one CTA ------------------------------------------
+// Residues are binned by their first atom into cells of edge >= (rc + skin + 2 rext)/2 and a
+// 5x5x5 stencil is scanned; boxes with fewer than 5 cells per edge scan every residue.  A residue
+// q enters the list of r when any atom pair is within rc + skin (exact fixed-point displacement).
+// s_cell: MAX_CELLS+1 ints of shared memory; g_order, g_cell: nres ints of global scratch.
+template <int APR>
+__device__ void chain_build(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ F, uint4* FB,
+                            uint16_t* LST, int* NL, int* s_cell, int* g_order, int* g_cell, int* err_out) {
+    const int apr = APR ? APR : C.apr;
+    const int nres = C.nres;
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
+    const uint4* Fc = F + C.atom0;
+    for (int i = tid; i < nres * apr; i += T) FB[C.atom0 + i] = Fc[i];
+    int nc[3];
+    bool cells = true;
+    for (int k = 0; k < 3; k++) {
+        nc[k] = (int)floor(C.L[k] / G.cellmin);
+        if (nc[k] < 5) cells = false;
+    }
+    if (cells && nc[0] * nc[1] * nc[2] > MAX_CELLS) cells = false;
+    const int ncell = cells ? nc[0] * nc[1] * nc[2] : 1;
+    __syncthreads();
+    if (cells) {
+        for (int c = tid; c <= ncell; c += T) s_cell[c] = 0;
+        __syncthreads();
+        for (int r = tid; r < nres; r += T) {
+            uint4 p = Fc[r * apr];
+            int c = (cell_coord(p.z, nc[2]) * nc[1] + cell_coord(p.y, nc[1])) * nc[0] + cell_coord(p.x, nc[0]);
+            g_cell[r] = c;
+            atomicAdd(&s_cell[c + 1], 1);
+        }
+        __syncthreads();
+        if (tid == 0)  // inclusive scan of counts shifted by one = start offsets
+            for (int c = 1; c <= ncell; c++) s_cell[c] += s_cell[c - 1];
+        __syncthreads();
+        // s_cell[c] doubles as the fill cursor of cell c: place with atomics, then sort each cell
+        // (warp per cell) so the list order, and with it the dE summation order, is deterministic
+        for (int r = tid; r < nres; r += T) {
+            int c = g_cell[r];
+            int slot = atomicAdd(&s_cell[c], 1);   // s_cell[c] advances to the end of cell c
+            g_order[slot] = r;
+        }
+        __syncthreads();
+        // s_cell[c] now holds end(c) = start(c+1); restore starts by shifting
+        if (tid == 0) {
+            for (int c = ncell; c >= 1; c--) s_cell[c] = s_cell[c - 1];
+            s_cell[0] = 0;
+        }
+        __syncthreads();
+        for (int c = warp; c < ncell; c += nw) {
+            const int b = s_cell[c], e = s_cell[c + 1], m = e - b;
+            if (m <= 1) continue;
+            if (m <= 32) {
+                int v = lane < m ? g_order[b + lane] : 0x7fffffff;
+                for (int k = 2; k <= 32; k <<= 1)
+                    for (int j = k >> 1; j > 0; j >>= 1) {
+                        int o = __shfl_xor_sync(0xffffffffu, v, j);
+                        bool up = (lane & k) == 0, lower = (lane & j) == 0;
+                        v = (lower == up) ? min(v, o) : max(v, o);
+                    }
+                if (lane < m) g_order[b + lane] = v;
+            } else if (lane == 0) {
+                for (int i = b + 1; i < e; i++) {
+                    int v = g_order[i], k = i - 1;
+                    while (k >= b && g_order[k] > v) { g_order[k + 1] = g_order[k]; k--; }
+                    g_order[k + 1] = v;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int r = warp; r < nres; r += nw) {
+        uint4 pa[APR ? APR : MAX_APR];
+        for (int k = 0; k < apr; k++) pa[k] = Fc[r * apr + k];
+        uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
+        int cnt = 0;
+        auto consider = [&](int q, bool valid) {
+            bool ok = false;
+            if (valid && q != r) {
+                uint4 pq = Fc[q * apr];
+                float dx = fdelta(pa[0].x, pq.x, C.Ls[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2]);
+                if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
+                    for (int b = 0; b < apr && !ok; b++) {
+                        uint4 pb = Fc[q * apr + b];
+                        for (int k = 0; k < apr; k++) {
+                            float ex = fdelta(pa[k].x, pb.x, C.Ls[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1]), ez = fdelta(pa[k].z, pb.z, C.Ls[2]);
+                            if (ex * ex + ey * ey + ez * ez <= G.rlist2) { ok = true; break; }
+                        }
+                    }
+                }
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                if (pos < G.cap) row[pos] = (uint16_t)q;
+            }
+            cnt += __popc(bal);
+        };
+        if (cells) {
+            const int cx = cell_coord(pa[0].x, nc[0]), cy = cell_coord(pa[0].y, nc[1]), cz = cell_coord(pa[0].z, nc[2]);
+            for (int dz = -2; dz <= 2; dz++)
+                for (int dy = -2; dy <= 2; dy++)
+                    for (int dx = -2; dx <= 2; dx++) {
+                        int x = (cx + dx + nc[0]) % nc[0], y = (cy + dy + nc[1]) % nc[1], z = (cz + dz + nc[2]) % nc[2];
+                        int cc = (z * nc[1] + y) * nc[0] + x;
+                        int b = s_cell[cc], e = s_cell[cc + 1];
+                        for (int base = b; base < e; base += 32) {
+                            int t = base + lane;
+                            consider(t < e ? g_order[t] : 0, t < e);
+                        }
+                    }
+        } else {
+            for (int base = 0; base < nres; base += 32) {
+                int q = base + lane;
+                consider(q < nres ? q : 0, q < nres);
+            }
+        }
+        if (lane == 0) {
+            NL[C.res0 + r] = min(cnt, G.cap);
+            if (cnt > G.cap) atomicExch(err_out, MCG_ECAPACITY);
+        }
+    }
+    __syncthreads();
+}
+
+template <int APR>
+__global__ void k_batch_build(const ChainDev* __restrict__ chains, BatchGeom G, const uint4* __restrict__ F, uint4* FB,
+                              uint16_t* LST, int* NL, int* g_order, int* g_cell, ChainState* state, int nchains) {
+    __shared__ int s_cell[MAX_CELLS + 1];
+    __shared__ int s_err;
+    const int c = blockIdx.x;
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    if (APR && C.apr != APR) return;
+    if (threadIdx.x == 0) s_err = 0;
+    __syncthreads();
+    chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+    if (threadIdx.x == 0 && s_err) state[c].err = s_err;
+}
+
+// ---- the sweep ------------------------------------------------------------------------------
+struct Proposal {
+    uint4 fo[MAX_APR], fn[MAX_APR];
+    unsigned long long mn[MAX_APR][3];   // new master coordinates
+    float m[MAX_APR][3];                 // fn - fo in Angstrom (exact mirror difference)
+    int res;
+    double thr;                          // -ln(alpha) / beta: accept when dE < thr
+    int rebuild;
+};
+
+template <int APR>
+__global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
+                                                     uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
+                                                     int* g_cell, ChainState* state, const int* __restrict__ order,
+                                                     int nchains) {
+    __shared__ Proposal P;
+    __shared__ double s_red[8];
+    __shared__ int s_cell[MAX_CELLS + 1];
+    __shared__ int s_err;
+    __shared__ float s_tab[MAX_APR][MAX_APR][4];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int c = order[blockIdx.x];
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    if (APR && C.apr != APR) return;
+    const int apr = APR ? APR : C.apr;
+    for (int k = tid; k < MAX_APR * MAX_APR * 4; k += blockDim.x) (&s_tab[0][0][0])[k] = (&C.tab[0][0][0])[k];
+    CutDev cut;
+    cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
+    cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
+    ChainState S = state[c];
+    if (tid == 0) { s_err = 0; P.rebuild = 0; }
+    __syncthreads();
+    const int nmoves = C.nres;
+    long long npairs = 0;
+    uint4* Fc = F + C.atom0;
+    ulonglong4* Mc = M + C.atom0;
+    for (int mv = 0; mv < nmoves; mv++) {
+        const unsigned long long cnt = S.moves + (unsigned long long)mv;
+        if (warp == 0) {
+            // ---- proposal: lanes 0..apr-1 own one atom each
+            __syncwarp();
+            U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
+            U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
+            const bool rot = C.ntypes_move == 2 && (r0.x & 1u);
+            const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
+            const int piv = (int)(((uint64_t)r0.z * (uint64_t)apr) >> 32);
+            const float ct = 2.0f * u01f(r0.w) - 1.0f;   // uniform direction: cos(theta), phi
+            const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+            float sphi, cphi;
+            sincospif(2.0f * u01f(r1.x), &sphi, &cphi);
+            const float ux = st * cphi, uy = st * sphi, uz = ct;
+            if (lane < apr) {
+                const int a = res * apr + lane;
+                const uint4 fo = Fc[a];
+                const ulonglong4 mo = Mc[a];
+                float dx, dy, dz;
+                if (!rot) {
+                    const float rad = C.dmax_trn * cbrtf(u01f(r1.y));
+                    dx = rad * ux; dy = rad * uy; dz = rad * uz;
+                } else {
+                    // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u
+                    float sh, ch;
+                    sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
+                    const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
+                    const uint4 fp = Fc[res * apr + piv];
+                    const float ox = fdelta(fp.x, fo.x, C.Ls[0]), oy = fdelta(fp.y, fo.y, C.Ls[1]), oz = fdelta(fp.z, fo.z, C.Ls[2]);
+                    // rotated offset minus offset: 2 q_w (q_v x o) + 2 q_v x (q_v x o)
+                    const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
+                    dx = qw * tx + (qy * tz - qz * ty);
+                    dy = qw * ty + (qz * tx - qx * tz);
+                    dz = qw * tz + (qx * ty - qy * tx);
+                }
+                const unsigned long long nx = mo.x + (unsigned long long)__double2ll_rn((double)dx * C.tofix[0]);
+                const unsigned long long ny = mo.y + (unsigned long long)__double2ll_rn((double)dy * C.tofix[1]);
+                const unsigned long long nz = mo.z + (unsigned long long)__double2ll_rn((double)dz * C.tofix[2]);
+                const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
+                P.fo[lane] = fo;
+                P.fn[lane] = fn;
+                P.mn[lane][0] = nx; P.mn[lane][1] = ny; P.mn[lane][2] = nz;
+                P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0]);
+                P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1]);
+                P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2]);
+            }
+            if (lane == 0) P.res = res;
+        } else if (warp == 1 && lane == 0) {
+            // acceptance threshold in FP64 while warp 0 builds the proposal
+            U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
+            P.thr = -log(u01d_open0(r1.z, r1.w)) / C.beta;
+        }
+        __syncthreads();
+        if (P.rebuild) {  // requested by the previous accepted move
+            chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+            if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
+            __syncthreads();
+        }
+        // ---- dE over the residue's neighbour list
+        const int res = P.res;
+        uint4 fo[APR ? APR : MAX_APR];
+        float m[APR ? APR : MAX_APR][3];
+#pragma unroll
+        for (int k = 0; k < (APR ? APR : MAX_APR); k++)
+            if (k < apr) { fo[k] = P.fo[k]; m[k][0] = P.m[k][0]; m[k][1] = P.m[k][1]; m[k][2] = P.m[k][2]; }
+        const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
+        const int nl = NL[C.res0 + res];
+        float acc = 0.0f;
+        int np = 0;
+        for (int e = tid; e < nl; e += blockDim.x) {
+            const int q = row[e];
+#pragma unroll
+            for (int b = 0; b < (APR ? APR : MAX_APR); b++) {
+                if (b >= apr) break;
+                const uint4 pb = Fc[q * apr + b];
+#pragma unroll
+                for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
+                    if (k >= apr) break;
+                    const float4 t = *reinterpret_cast<const float4*>(&s_tab[fo[k].w][pb.w][0]);
+                    // d_old = b - a_old, d_new = b - a_new = d_old - m
+                    acc += mixed_pair_delta(fdelta(fo[k].x, pb.x, C.Ls[0]), fdelta(fo[k].y, pb.y, C.Ls[1]),
+                                            fdelta(fo[k].z, pb.z, C.Ls[2]), m[k][0], m[k][1], m[k][2], t.x, t.y, t.z, cut, np);
+                }
+            }
+        }
+        npairs += np;
+        const double v = warp_sum((double)acc);
+        if (lane == 0) s_red[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            double de = 0.0;
+            for (int w = 0; w < nw; w++) de += s_red[w];
+            const bool accept = (de <= 2.220446049250313e-16) || (de < P.thr);
+            bool far = false;
+            if (accept && lane < apr) {
+                const int a = res * apr + lane;
+                Mc[a] = make_ulonglong4(P.mn[lane][0], P.mn[lane][1], P.mn[lane][2], 0ull);
+                Fc[a] = P.fn[lane];
+                const uint4 bpos = FB[C.atom0 + a];
+                const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0]);
+                const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1]);
+                const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2]);
+                far = ex * ex + ey * ey + ez * ez > G.half_skin2;
+            }
+            if (__any_sync(0xffffffffu, far) && lane == 0) P.rebuild = 1;
+            if (lane == 0) {
+                S.trials++;
+                if (accept) { S.accepted++; S.etot += de; }
+            }
+        }
+    }
+    __syncthreads();
+    if (P.rebuild) {
+        chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+        if (tid == 0) S.rebuilds++;
+    }
+    {
+        __shared__ unsigned long long s_pairs;
+        if (tid == 0) s_pairs = 0ull;
+        __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
+        if (lane == 0) atomicAdd(&s_pairs, (unsigned long long)npairs);
+        __syncthreads();
+        if (tid == 0) S.pairs += (long long)s_pairs;
+    }
+    if (tid == 0) {
+        S.moves += (unsigned long long)nmoves;
+        if (s_err) S.err = s_err;
+        state[c] = S;
+    }
+}
+
+// FP64 view of a master coordinate
+__device__ __forceinline__ double master_to_f64(unsigned long long v, double L) {
+    return (double)(long long)v * (L * (1.0 / TWO64));
+}
+
+// ---- fresh FP64 energy of every chain (reference arithmetic, all pairs, cutoff + switch)
+constexpr int ETILE = 128;
+__global__ void k_batch_energy64(const ChainDev* __restrict__ chains, const int* __restrict__ tile_chain,
+                                 const int* __restrict__ tile_first, const ulonglong4* __restrict__ M,
+                                 const double* __restrict__ prm, CutDev cut, double* part) {
+    const int t = blockIdx.x;
+    const int c = tile_chain[t];
+    const ChainDev& C = chains[c];
+    const int n = C.nres * C.apr;
+    const int i = tile_first[t] + threadIdx.x;
+    double s = 0.0;
+    if (i < n) {
+        PbcDev pbc;
+        pbc.type = 2;
+        for (int k = 0; k < 3; k++) { pbc.L[k] = C.L[k]; pbc.rL[k] = C.rL[k]; }
+        const ulonglong4 ma = M[C.atom0 + i];
+        const double ax = master_to_f64(ma.x, C.L[0]), ay = master_to_f64(ma.y, C.L[1]), az = master_to_f64(ma.z, C.L[2]);
+        const int ri = i / C.apr;
+        const double* pa = prm + 3 * (size_t)(C.atom0 + i);
+        for (int j = i + 1; j < n; j++) {
+            if (j / C.apr == ri) continue;  // intra-residue pairs are excluded
+            const ulonglong4 mb = M[C.atom0 + j];
+            const double r2 = ref64_dist2(ax, ay, az, master_to_f64(mb.x, C.L[0]), master_to_f64(mb.y, C.L[1]),
+                                          master_to_f64(mb.z, C.L[2]), pbc);
+            if (r2 > cut.c2) continue;
+            const double* pb = prm + 3 * (size_t)(C.atom0 + j);
+            double el, vd;
+            ref64_pair(r2, pa[0], pb[0], pa[1], pb[1], pa[2], pb[2], true, cut, el, vd);
+            s += CHGCHARMM * KCALTOIU * el + 4.0 * vd;
+        }
+    }
+    s = warp_sum(s);
+    __shared__ double sh[ETILE / 32];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < ETILE / 32; w++) v += sh[w];
+        part[t] = v;
+    }
+}
+
+// ---- mixed-precision energy of every chain over its neighbour lists (each pair once: q > r)
+template <int APR>
+__global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __restrict__ chains, BatchGeom G,
+                                                           const uint4* __restrict__ F, const uint16_t* __restrict__ LST,
+                                                           const int* __restrict__ NL, ChainState* state, int nchains) {
+    __shared__ float s_tab[MAX_APR][MAX_APR][4];
+    __shared__ double s_red[8];
+    const int c = blockIdx.x;
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    if (APR && C.apr != APR) return;
+    const int apr = APR ? APR : C.apr;
+    for (int k = threadIdx.x; k < MAX_APR * MAX_APR * 4; k += blockDim.x) (&s_tab[0][0][0])[k] = (&C.tab[0][0][0])[k];
+    __syncthreads();
+    CutDev cut;
+    cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
+    cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
+    const uint4* Fc = F + C.atom0;
+    F32Acc acc;
+    for (int r = threadIdx.x; r < C.nres; r += blockDim.x) {
+        const uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
+        const int nl = NL[C.res0 + r];
+        for (int e = 0; e < nl; e++) {
+            const int q = row[e];
+            if (q <= r) continue;
+            for (int k = 0; k < apr; k++) {
+                const uint4 pa = Fc[r * apr + k];
+                for (int b = 0; b < apr; b++) {
+                    const uint4 pb = Fc[q * apr + b];
+                    const float dx = fdelta(pa.x, pb.x, C.Ls[0]), dy = fdelta(pa.y, pb.y, C.Ls[1]), dz = fdelta(pa.z, pb.z, C.Ls[2]);
+                    const float u = dx * dx + dy * dy + dz * dz;
+                    if (u > cut.c2f) continue;
+                    const float4 t = *reinterpret_cast<const float4*>(&s_tab[pa.w][pb.w][0]);
+                    float el, vd;
+                    mixed_pair(u, t.x, t.y, t.z, true, cut, el, vd);
+                    acc.add(el + vd);
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double v = warp_sum(acc.value());
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double e = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) e += s_red[w];
+        state[c].etot = e;
+    }
+}
+
+// FP64 coordinates (all chains concatenated) -> 64-bit masters and 32-bit mirrors
+__global__ void k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz, int64_t natoms,
+                               ulonglong4* M, uint4* F, int nchains) {
+    const int c = blockIdx.x;
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    const int n = C.nres * C.apr;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int64_t a = C.atom0 + i;
+        unsigned long long m[3];
+        for (int k = 0; k < 3; k++) {
+            double u = xyz[k * natoms + a] * C.rL[k];
+            u -= rint(u);
+            if (u >= 0.5) u -= 1.0;
+            m[k] = (unsigned long long)__double2ll_rn(u * TWO64);
+        }
+        M[a] = make_ulonglong4(m[0], m[1], m[2], 0ull);
+        F[a] = make_uint4((uint32_t)(m[0] >> 32), (uint32_t)(m[1] >> 32), (uint32_t)(m[2] >> 32), (uint32_t)(i % C.apr));
+    }
+}
+
+__global__ void k_batch_export(const ChainDev* __restrict__ chains, const ulonglong4* __restrict__ M, int64_t natoms,
+                               double* xyz, int nchains) {
+    const int c = blockIdx.x;
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    const int n = C.nres * C.apr;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int64_t a = C.atom0 + i;
+        const ulonglong4 m = M[a];
+        xyz[a] = master_to_f64(m.x, C.L[0]);
+        xyz[natoms + a] = master_to_f64(m.y, C.L[1]);
+        xyz[2 * natoms + a] = master_to_f64(m.z, C.L[2]);
+    }
+}
+
+}  // namespace mcg
+
+// ==============================================================================================
+using namespace mcg;
+
+static uint64_t host_master(double v, double rL) {
+    double u = v * rL;
+    u -= std::nearbyint(u);          // [-0.5, 0.5]
+    if (u >= 0.5) u -= 1.0;
+    return (uint64_t)(int64_t)std::llrint(u * TWO64);
+}
+
+static double host_view(uint64_t v, double L) { return (double)(int64_t)v * (L / TWO64); }
+
+struct mcg_batch {
+    int nchains = 0;
+    int64_t natoms = 0, nres = 0;
+    int apr_all = 0;            // common residue size (0 if mixed)
+    BatchGeom G{};
+    std::vector<ChainDev> chains;
+    std::vector<int> order;
+    cudaStream_t stream = nullptr;
+    ChainDev* d_chains = nullptr;
+    ChainState* d_state = nullptr;
+    int* d_order = nullptr;
+    ulonglong4* d_M = nullptr;
+    uint4 *d_F = nullptr, *d_FB = nullptr;
+    uint16_t* d_LST = nullptr;
+    int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr;
+    double* d_prm = nullptr;
+    int* d_tile_chain = nullptr;
+    int* d_tile_first = nullptr;
+    double* d_part = nullptr;
+    int ntiles = 0;
+    CutDev cut64{};
+    cudaGraphExec_t graph = nullptr;
+    double* d_xyz = nullptr;      // staging for host-buffer runs (3 x natoms)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int threads = 256;
+    int64_t rebuilds_seen = 0, launches = 0;
+    ~mcg_batch() {
+        if (graph) cudaGraphExecDestroy(graph);
+        void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
+                     d_tile_first, d_part, d_xyz};
+        for (void* q : p) if (q) cudaFree(q);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int launch_build() {
+        if (apr_all == 3)
+            k_batch_build<3><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+        else if (apr_all == 1)
+            k_batch_build<1><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+        else
+            k_batch_build<0><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+        BK(cudaGetLastError());
+        launches++;
+        return MCG_OK;
+    }
+    int launch_energy_list() {
+        if (apr_all == 3)
+            k_batch_energy_list<3><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+        else if (apr_all == 1)
+            k_batch_energy_list<1><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+        else
+            k_batch_energy_list<0><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+        BK(cudaGetLastError());
+        launches++;
+        return MCG_OK;
+    }
+    int ensure_graph() {
+        if (graph) return MCG_OK;
+        BK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int r = launch_sweep(stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(stream, &g);
+        if (r) { if (g) cudaGraphDestroy(g); return r; }
+        if (ee != cudaSuccess) return fail(MCG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
+        cudaError_t ie = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return fail(MCG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        return MCG_OK;
+    }
+    int launch_sweep(cudaStream_t st) {
+        if (apr_all == 3)
+            k_batch_sweep<3><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+        else if (apr_all == 1)
+            k_batch_sweep<1><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+        else
+            k_batch_sweep<0><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+        BK(cudaGetLastError());
+        return MCG_OK;
+    }
+};
+
+template <typename T>
+static int balloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(1, n) * sizeof(T));
+    if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return MCG_OK;
+}
+
+extern "C" {
+
+int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_opts* opts, mcg_batch** out) {
+    if (!out) return fail(MCG_EINVAL, "null output handle");
+    *out = nullptr;
+    if (!descs || nchains <= 0 || !opts) return fail(MCG_EINVAL, "need chains and options");
+    if (!(opts->dmax_trn >= 0) || !(opts->dmax_rot >= 0)) return fail(MCG_EINVAL, "dmax values must be >= 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) { cudaGetLastError(); return fail(MCG_ECUDA, "no CUDA device available"); }
+    std::unique_ptr<mcg_batch> B(new mcg_batch);
+    B->nchains = nchains;
+    const mcg_system_desc& d0 = descs[0];
+    const double rc = d0.cutoff, ron = d0.cuton, skin = d0.dcut > 0 ? d0.dcut : 2.0;
+    std::vector<ulonglong4> M;
+    std::vector<uint4> F;
+    std::vector<double> prm;
+    double rext = 0.0;
+    int apr_all = -1;
+    int64_t atom0 = 0, res0 = 0;
+    B->chains.resize(nchains);
+    for (int c = 0; c < nchains; c++) {
+        const mcg_system_desc& d = descs[c];
+        HostSystem hs;
+        int rc2 = build_host_system(&d, hs);
+        if (rc2) return fail(rc2, "chain " + std::to_string(c) + ": " + mcg_last_error());
+        if (hs.cut != MCG_CUT_SWITCH) return fail(MCG_EINVAL, "batched chains need the switch cutoff");
+        if (hs.pbc == MCG_PBC_NONE) return fail(MCG_EINVAL, "batched chains need periodic boxes");
+        if (d.cutoff != rc || d.cuton != ron || d.dcut != d0.dcut) return fail(MCG_EINVAL, "all chains must share cutoff, cuton and skin");
+        if (!hs.pairs14.empty()) return fail(MCG_ENOTSUP, "batched chains hold rigid residues without 1-4 pairs");
+        for (int i = 0; i < hs.n; i++) if (hs.frozen[i]) return fail(MCG_ENOTSUP, "frozen atoms are not supported in batched chains");
+        int apr = 0;
+        while (apr < hs.n && hs.resid[apr] == hs.resid[0]) apr++;
+        if (apr < 1 || apr > MAX_APR || hs.n % apr) return fail(MCG_ENOTSUP, "residues must all have the same size (1..8 atoms)");
+        const int nres = hs.n / apr;
+        if (nres > 65535) return fail(MCG_ENOTSUP, "at most 65535 residues per chain");
+        for (int r = 0; r < nres; r++)
+            for (int k = 0; k < apr; k++) {
+                int a = r * apr + k;
+                if (hs.resid[a] != hs.resid[r * apr] || (r > 0 && hs.resid[a] == hs.resid[a - apr]))
+                    return fail(MCG_ENOTSUP, "residues must all have the same size");
+                if (hs.q[a] != hs.q[k] || hs.eps[a] != hs.eps[k] || hs.sig[a] != hs.sig[k])
+                    return fail(MCG_ENOTSUP, "residues must share one parameter template");
+                for (int k2 = k + 1; k2 < apr; k2++) {
+                    int b = r * apr + k2;
+                    bool ex = false;
+                    for (int t = hs.exclStart[a]; t < hs.exclStart[a + 1]; t++) ex |= hs.exclData[t] == b;
+                    if (!ex) return fail(MCG_ENOTSUP, "every intra-residue pair must be excluded (rigid residues)");
+                }
+            }
+        if (apr_all < 0) apr_all = apr; else if (apr_all != apr) apr_all = 0;
+        ChainDev& C = B->chains[c];
+        memset(&C, 0, sizeof C);
+        C.atom0 = (int)atom0; C.res0 = (int)res0; C.nres = nres; C.apr = apr;
+        for (int k = 0; k < 3; k++) {
+            C.L[k] = hs.L[k]; C.rL[k] = hs.rL[k];
+            C.tofix[k] = TWO64 / hs.L[k];
+            C.Ls[k] = (float)(hs.L[k] / 4294967296.0);
+        }
+        C.beta = 1.0 / ((RBOLTZUI / KCALTOIU) * hs.temp);
+        if (opts->acceptance_units == MCG_ACCEPT_PHYSICAL) C.beta /= KCALTOIU;
+        C.dmax_trn = (float)opts->dmax_trn;
+        C.dmax_rot = (float)opts->dmax_rot;
+        C.ntypes_move = apr > 1 ? 2 : 1;
+        uint64_t key = (opts->seed + 1) * 0x9E3779B97F4A7C15ull ^ ((uint64_t)c * 0xD1B54A32D192ED03ull);
+        C.key0 = (uint32_t)key; C.key1 = (uint32_t)(key >> 32);
+        const double K = CHGCHARMM * KCALTOIU;
+        for (int a = 0; a < apr; a++)
+            for (int b = 0; b < apr; b++) {
+                C.tab[a][b][0] = (float)(K * hs.q[a] * hs.q[b]);
+                C.tab[a][b][1] = (float)(4.0 * hs.eps[a] * hs.eps[b]);
+                double s = hs.sig[a] + hs.sig[b];
+                C.tab[a][b][2] = (float)(s * s);
+            }
+        for (int i = 0; i < hs.n; i++) {
+            ulonglong4 m;
+            m.x = host_master(hs.x[i], hs.rL[0]); m.y = host_master(hs.y[i], hs.rL[1]); m.z = host_master(hs.z[i], hs.rL[2]); m.w = 0;
+            M.push_back(m);
+            F.push_back(make_uint4((uint32_t)(m.x >> 32), (uint32_t)(m.y >> 32), (uint32_t)(m.z >> 32), (uint32_t)(i % apr)));
+            prm.push_back(hs.q[i]); prm.push_back(hs.eps[i]); prm.push_back(hs.sig[i]);
+        }
+        for (int r = 0; r < nres; r++)
+            for (int k = 1; k < apr; k++) {
+                double e[3] = {hs.x[r * apr + k] - hs.x[r * apr], hs.y[r * apr + k] - hs.y[r * apr], hs.z[r * apr + k] - hs.z[r * apr]};
+                for (int t = 0; t < 3; t++) e[t] -= hs.L[t] * std::nearbyint(e[t] * hs.rL[t]);
+                rext = std::max(rext, std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+            }
+        atom0 += hs.n;
+        res0 += nres;
+        if (atom0 > (int64_t)2000000000) return fail(MCG_EINVAL, "too many atoms");
+    }
+    B->natoms = atom0;
+    B->nres = res0;
+    B->apr_all = apr_all;
+    BatchGeom& G = B->G;
+    G.c2f = (float)(rc * rc); G.n2f = (float)(ron * ron);
+    { double dd = rc * rc - ron * ron; G.sw2f = (float)(1.0 / (dd * dd * dd)); }
+    const double rlist = rc + skin;
+    G.rlist2 = (float)(rlist * rlist);
+    rext += 0.01;
+    G.rcent2 = (float)((rlist + 2 * rext) * (rlist + 2 * rext));
+    G.half_skin2 = (float)(0.25 * skin * skin);
+    G.cellmin = (float)(0.5 * (rlist + 2 * rext) + 1e-3);
+    for (auto& C : B->chains)
+        for (int k = 0; k < 3; k++)
+            if (rc > 0.5 * C.L[k]) return fail(MCG_EINVAL, "cutoff exceeds half a chain's box");
+    if (opts->list_capacity > 0) G.cap = opts->list_capacity;
+    else {
+        double dens = 0;
+        int maxres = 0;
+        for (auto& C : B->chains) { dens = std::max(dens, C.nres / (C.L[0] * C.L[1] * C.L[2])); maxres = std::max(maxres, C.nres); }
+        double r = rlist + 2 * rext;
+        G.cap = (int)(4.0 / 3.0 * PI * r * r * r * dens * 1.6) + 64;
+        G.cap = std::min((G.cap + 31) & ~31, ((maxres + 31) & ~31) + 32);
+    }
+    if (G.cap > 65535) G.cap = 65535;
+    B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 256;
+    if (B->threads % 32 || B->threads > 256 || B->threads < 64) return fail(MCG_EINVAL, "threads_per_chain must be a multiple of 32 in [64, 256]");
+    // chain order: largest first, so the longest sweeps start first
+    B->order.resize(nchains);
+    std::iota(B->order.begin(), B->order.end(), 0);
+    std::stable_sort(B->order.begin(), B->order.end(), [&](int a, int b) { return B->chains[a].nres > B->chains[b].nres; });
+    BK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+    int r;
+    if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) || (r = balloc(&B->d_order, nchains)) ||
+        (r = balloc(&B->d_M, atom0)) || (r = balloc(&B->d_F, atom0)) || (r = balloc(&B->d_FB, atom0)) ||
+        (r = balloc(&B->d_LST, (size_t)res0 * G.cap)) || (r = balloc(&B->d_NL, res0)) || (r = balloc(&B->d_gorder, res0)) ||
+        (r = balloc(&B->d_gcell, res0)) || (r = balloc(&B->d_prm, prm.size())))
+        return r;
+    BK(cudaMemcpyAsync(B->d_chains, B->chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_order, B->order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4) * atom0, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_F, F.data(), sizeof(uint4) * atom0, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemsetAsync(B->d_state, 0, sizeof(ChainState) * nchains, B->stream));
+    std::vector<int> tc, tf;
+    for (int c = 0; c < nchains; c++) {
+        int n = B->chains[c].nres * B->chains[c].apr;
+        for (int f = 0; f < n; f += ETILE) { tc.push_back(c); tf.push_back(f); }
+    }
+    B->ntiles = (int)tc.size();
+    if ((r = balloc(&B->d_tile_chain, tc.size())) || (r = balloc(&B->d_tile_first, tf.size())) || (r = balloc(&B->d_part, tc.size())))
+        return r;
+    BK(cudaMemcpyAsync(B->d_tile_chain, tc.data(), sizeof(int) * tc.size(), cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_tile_first, tf.data(), sizeof(int) * tf.size(), cudaMemcpyHostToDevice, B->stream));
+    B->cut64.mode = 1;
+    B->cut64.c2 = rc * rc; B->cut64.n2 = ron * ron;
+    { double dd = B->cut64.c2 - B->cut64.n2; B->cut64.sw2 = 1. / (dd * dd * dd); }
+    if ((r = B->launch_build())) return r;
+    std::vector<double> e(nchains);
+    r = mcg_batch_energy_fp64(B.get(), e.data());
+    if (r) return r;
+    std::vector<ChainState> st(nchains);
+    BK(cudaMemcpyAsync(st.data(), B->d_state, sizeof(ChainState) * nchains, cudaMemcpyDeviceToHost, B->stream));
+    BK(cudaStreamSynchronize(B->stream));
+    for (int c = 0; c < nchains; c++) {
+        if (st[c].err) return fail(st[c].err, "neighbour list capacity exceeded (chain " + std::to_string(c) + ")");
+        st[c].etot = e[c];
+    }
+    BK(cudaMemcpyAsync(B->d_state, st.data(), sizeof(ChainState) * nchains, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaStreamSynchronize(B->stream));
+    *out = B.release();
+    return MCG_OK;
+}
+
+int mcg_batch_destroy(mcg_batch* b) {
+    delete b;
+    return MCG_OK;
+}
+
+int mcg_batch_sweep(mcg_batch* b, int nsweeps) {
+    if (!b || nsweeps < 0) return fail(MCG_EINVAL, "bad arguments");
+    int r = b->ensure_graph();
+    if (r) return r;
+    for (int s = 0; s < nsweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
+    b->launches += nsweeps;
+    return MCG_OK;
+}
+
+int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms) {
+    if (!b || nsweeps < 0 || !ms) return fail(MCG_EINVAL, "bad arguments");
+    int r = b->ensure_graph();
+    if (r) return r;
+    if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
+    BK(cudaStreamSynchronize(b->stream));
+    BK(cudaEventRecord(b->ev0, b->stream));
+    for (int s = 0; s < nsweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
+    BK(cudaEventRecord(b->ev1, b->stream));
+    BK(cudaEventSynchronize(b->ev1));
+    BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    b->launches += nsweeps;
+    return MCG_OK;
+}
+
+int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* xyz_out, int64_t* accepted, double* etot) {
+    if (!b || nsweeps < 0) return fail(MCG_EINVAL, "bad arguments");
+    const size_t bytes = sizeof(double) * 3 * (size_t)b->natoms;
+    int r;
+    if ((xyz_in || xyz_out) && !b->d_xyz) { if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r; }
+    if (xyz_in) {
+        BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
+        k_batch_import<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M, b->d_F, b->nchains);
+        BK(cudaGetLastError());
+        b->launches++;
+        if ((r = b->launch_build()) || (r = b->launch_energy_list())) return r;
+    }
+    if ((r = mcg_batch_sweep(b, nsweeps))) return r;
+    if (xyz_out) {
+        k_batch_export<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_M, b->natoms, b->d_xyz, b->nchains);
+        BK(cudaGetLastError());
+        b->launches++;
+        BK(cudaMemcpyAsync(xyz_out, b->d_xyz, bytes, cudaMemcpyDeviceToHost, b->stream));
+    }
+    return mcg_batch_stats(b, nullptr, accepted, etot);
+}
+
+int mcg_batch_energy_mixed(mcg_batch* b, double* e) {
+    if (!b || !e) return fail(MCG_EINVAL, "null argument");
+    std::vector<ChainState> keep(b->nchains);
+    BK(cudaMemcpyAsync(keep.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    int r = b->launch_energy_list();
+    if (r) return r;
+    std::vector<ChainState> st(b->nchains);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < b->nchains; c++) e[c] = st[c].etot;
+    BK(cudaMemcpyAsync(b->d_state, keep.data(), sizeof(ChainState) * b->nchains, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    return MCG_OK;
+}
+
+int mcg_batch_pairs(mcg_batch* b, int64_t* pairs) {
+    if (!b || !pairs) return fail(MCG_EINVAL, "null argument");
+    std::vector<ChainState> st(b->nchains);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < b->nchains; c++) pairs[c] = st[c].pairs;
+    return MCG_OK;
+}
+
+int mcg_batch_stats(mcg_batch* b, int64_t* trials, int64_t* accepted, double* etot) {
+    if (!b) return fail(MCG_EINVAL, "null handle");
+    std::vector<ChainState> st(b->nchains);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    int64_t rb = 0;
+    for (int c = 0; c < b->nchains; c++) {
+        if (st[c].err) return fail(st[c].err, "chain " + std::to_string(c) + " reported status " + std::to_string(st[c].err));
+        if (trials) trials[c] = st[c].trials;
+        if (accepted) accepted[c] = st[c].accepted;
+        if (etot) etot[c] = st[c].etot;
+        rb += st[c].rebuilds;
+    }
+    b->rebuilds_seen = rb;
+    return MCG_OK;
+}
+
+int mcg_batch_energy_fp64(mcg_batch* b, double* e) {
+    if (!b || !e) return fail(MCG_EINVAL, "null argument");
+    k_batch_energy64<<<b->ntiles, ETILE, 0, b->stream>>>(b->d_chains, b->d_tile_chain, b->d_tile_first, b->d_M, b->d_prm,
+                                                         b->cut64, b->d_part);
+    BK(cudaGetLastError());
+    std::vector<double> part(b->ntiles);
+    std::vector<int> tc(b->ntiles);
+    BK(cudaMemcpyAsync(part.data(), b->d_part, sizeof(double) * b->ntiles, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaMemcpyAsync(tc.data(), b->d_tile_chain, sizeof(int) * b->ntiles, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < b->nchains; c++) e[c] = 0.0;
+    for (int t = 0; t < b->ntiles; t++) e[tc[t]] += part[t];
+    b->launches += 1;
+    return MCG_OK;
+}
+
+int mcg_batch_get_coords(mcg_batch* b, int chain, double* x, double* y, double* z) {
+    if (!b || chain < 0 || chain >= b->nchains || !x || !y || !z) return fail(MCG_EINVAL, "bad arguments");
+    const ChainDev& C = b->chains[chain];
+    int n = C.nres * C.apr;
+    std::vector<ulonglong4> M(n);
+    BK(cudaMemcpyAsync(M.data(), b->d_M + C.atom0, sizeof(ulonglong4) * n, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < n; i++) { x[i] = host_view(M[i].x, C.L[0]); y[i] = host_view(M[i].y, C.L[1]); z[i] = host_view(M[i].z, C.L[2]); }
+    return MCG_OK;
+}
+
+int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double* y, const double* z) {
+    if (!b || chain < 0 || chain >= b->nchains || !x || !y || !z) return fail(MCG_EINVAL, "bad arguments");
+    const ChainDev& C = b->chains[chain];
+    int n = C.nres * C.apr;
+    std::vector<ulonglong4> M(n);
+    std::vector<uint4> F(n);
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i])) return fail(MCG_EINVAL, "non-finite coordinate");
+        M[i].x = host_master(x[i], C.rL[0]); M[i].y = host_master(y[i], C.rL[1]); M[i].z = host_master(z[i], C.rL[2]); M[i].w = 0;
+        F[i] = make_uint4((uint32_t)(M[i].x >> 32), (uint32_t)(M[i].y >> 32), (uint32_t)(M[i].z >> 32), (uint32_t)(i % C.apr));
+    }
+    BK(cudaMemcpyAsync(b->d_M + C.atom0, M.data(), sizeof(ulonglong4) * n, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_F + C.atom0, F.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice, b->stream));
+    int r = b->launch_build();
+    if (r) return r;
+    std::vector<double> e(b->nchains);
+    r = mcg_batch_energy_fp64(b, e.data());
+    if (r) return r;
+    std::vector<ChainState> st(b->nchains);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    st[chain].etot = e[chain];
+    BK(cudaMemcpyAsync(b->d_state + chain, &st[chain], sizeof(ChainState), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    return MCG_OK;
+}
+
+int64_t mcg_batch_natoms(mcg_batch* b) { return b ? b->natoms : 0; }
+
+int mcg_batch_chain_natoms(mcg_batch* b, int chain) {
+    if (!b || chain < 0 || chain >= b->nchains) return fail(MCG_EINVAL, "bad chain");
+    return b->chains[chain].nres * b->chains[chain].apr;
+}
+
+int mcg_batch_counters(mcg_batch* b, int64_t* list_rebuilds, int64_t* kernel_launches) {
+    if (!b) return fail(MCG_EINVAL, "null handle");
+    int r = mcg_batch_stats(b, nullptr, nullptr, nullptr);
+    if (r) return r;
+    if (list_rebuilds) *list_rebuilds = b->rebuilds_seen;
+    if (kernel_launches) *kernel_launches = b->launches;
+    return MCG_OK;
+}
+
+}  // extern "C"

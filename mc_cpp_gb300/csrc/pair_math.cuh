@@ -1,0 +1,169 @@
+// Pair arithmetic shared by the single-system and batched kernels.
+//
+// * ref64_*: the reference's FP64 arithmetic, operation for operation, with explicit
+//   round-to-nearest intrinsics so the compiler cannot contract a multiply-add into an FMA
+//   (the reference is built in ISO C++ mode without contraction).  A pair evaluated here gives
+//   bitwise the value FField_MDBAS computes for it (FField_MDBAS.cpp:366-414, Tools.hpp:151-224,
+//   PerConditions.cpp:244-285).
+// * mixed_*: FP32 pair terms on an exact minimum-image displacement taken from 32-bit
+//   fixed-point coordinates (coordinate / box * 2^32): unsigned subtraction wraps modulo the box,
+//   which is the minimum image, and the integer difference is exact.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dev_types.hpp"
+
+namespace mcg {
+
+// Tools::rint (Tools.hpp:221-224): half away from zero through an int cast.
+__device__ __forceinline__ double ref64_rint(double x) {
+    double t = (x >= 0.0) ? __dadd_rn(x, 0.5) : __dsub_rn(x, 0.5);
+    return (double)__double2int_rz(t);
+}
+
+// d -= L * rint(rL * d)
+__device__ __forceinline__ double ref64_mic(double d, double L, double rL) {
+    return __dsub_rn(d, __dmul_rn(L, ref64_rint(__dmul_rn(rL, d))));
+}
+
+// Tools::distance2(a1, a2): delta = a2 - a1, MIC, r^2 = (dx^2 + dy^2) + dz^2.
+__device__ __forceinline__ double ref64_dist2(double ax, double ay, double az, double bx, double by, double bz,
+                                              const PbcDev& p, double* d = nullptr) {
+    double dx = __dsub_rn(bx, ax), dy = __dsub_rn(by, ay), dz = __dsub_rn(bz, az);
+    if (p.type != 0) {
+        dx = ref64_mic(dx, p.L[0], p.rL[0]);
+        dy = ref64_mic(dy, p.L[1], p.rL[1]);
+        dz = ref64_mic(dz, p.L[2], p.rL[2]);
+    }
+    if (d) { d[0] = dx; d[1] = dy; d[2] = dz; }
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// computeEelec / computeEvdw and the switch of computeNonBonded_switch, unscaled:
+// el = qi qj / r * S, vd = eps_i eps_j (x^12 - x^6) * S with x = (sig_i + sig_j) / r.
+__device__ __forceinline__ void ref64_pair(double r2, double qi, double qj, double ei, double ej, double si,
+                                           double sj, bool do_switch, const CutDev& c, double& el, double& vd) {
+    double r = __dsqrt_rn(r2);
+    double rt = __ddiv_rn(1.0, r);
+    double pe = __dmul_rn(__dmul_rn(qi, qj), rt);
+    double x = __dmul_rn(__dadd_rn(si, sj), rt);
+    double x12 = x;
+#pragma unroll
+    for (int k = 0; k < 11; k++) x12 = __dmul_rn(x12, x);
+    double x6 = x;
+#pragma unroll
+    for (int k = 0; k < 5; k++) x6 = __dmul_rn(x6, x);
+    double pv = __dmul_rn(__dmul_rn(ei, ej), __dsub_rn(x12, x6));
+    if (do_switch && r2 > c.n2) {
+        double s1 = __dsub_rn(c.c2, r2);
+        double f = __dmul_rn(__dmul_rn(__dmul_rn(s1, s1), __dsub_rn(__dadd_rn(c.c2, __dmul_rn(2.0, r2)),
+                                                                      __dmul_rn(3.0, c.n2))), c.sw2);
+        pe = __dmul_rn(pe, f);
+        pv = __dmul_rn(pv, f);
+    }
+    el = pe;
+    vd = pv;
+}
+
+// ---- fixed-point coordinates --------------------------------------------------------------
+// u = wrapped(x) / L in [-1/2, 1/2) scaled by 2^32 and stored modulo 2^32.
+__device__ __forceinline__ uint32_t to_fixed(double x, double rL) {
+    double u = x * rL;
+    u -= rint(u);                               // [-0.5, 0.5]
+    long long v = __double2ll_rn(u * 4294967296.0);
+    return (uint32_t)(unsigned long long)v;
+}
+
+// exact minimum-image displacement b - a in box units of 2^-32, converted to Angstrom (FP32)
+__device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float Lscale) {
+    int d = (int)(b - a);
+    return __int2float_rn(d) * Lscale;
+}
+
+// FP32 switched LJ + Coulomb on r^2 (unscaled el, vd as in ref64_pair).  qq = qi qj,
+// ee = eps_i eps_j, ss = (sig_i + sig_j)^2.
+__device__ __forceinline__ void mixed_pair(float r2, float qq, float ee, float ss, bool do_switch, const CutDev& c,
+                                           float& el, float& vd) {
+    float rinv = rsqrtf(r2);
+    float x2 = ss * (rinv * rinv);
+    float x6 = x2 * x2 * x2;
+    float f = 1.0f;
+    if (do_switch && r2 > c.n2f) {
+        float s1 = c.c2f - r2;
+        f = s1 * s1 * (c.c2f + 2.0f * r2 - 3.0f * c.n2f) * c.sw2f;
+    }
+    el = qq * rinv * f;
+    vd = ee * (x6 * x6 - x6) * f;
+}
+
+// Error-free FP32 accumulation (Kahan-Babuska / Neumaier): sum + comp carries ~48 bits.
+struct F32Acc {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        float t = s + v;
+        c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace mcg
+
+namespace mcg {
+
+// Energy change of one pair when one side moves by m (d_new = d_old - m), FP32, in iu.
+// qk = 332.0716*418.4*qi*qj, e4 = 4*eps_i*eps_j, ss = (sig_i+sig_j)^2.
+// Coulomb (the large term) is differenced analytically so its error is relative to the change,
+// not to the pair energy: with u = r^2 and du = u_new - u_old = -m.(d_old + d_new),
+//   1/r_new - 1/r_old = -du (rn ro)^2 / (rn + ro)        (rn, ro = rsqrt(u_new), rsqrt(u_old))
+//   S_b - S_a = sw2 du' [2 A_a^2 - (A_a + A_b) B_b],  A = c2 - u, B = c2 + 2u - 3 n2
+// on the switch polynomial (u clamped to [n2, c2]).  LJ is small at these distances and is
+// differenced directly.  Pairs crossing the cutoff fall back to the direct difference.
+// npair counts pair interactions (inside the cutoff before or after the move).
+__device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float doz, float mx, float my, float mz,
+                                                  float qk, float e4, float ss, const CutDev& c, int& npair) {
+    const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
+    const float uo = dox * dox + doy * doy + doz * doz;
+    const float un = dnx * dnx + dny * dny + dnz * dnz;
+    const bool io = uo <= c.c2f, in = un <= c.c2f;
+    if (!io && !in) return 0.0f;
+    npair++;
+    const float ro = rsqrtf(uo), rn = rsqrtf(un);
+    auto sw = [&](float u) {
+        if (u <= c.n2f) return 1.0f;
+        float a = c.c2f - u;
+        return a * a * (c.c2f + 2.0f * u - 3.0f * c.n2f) * c.sw2f;
+    };
+    auto lj = [&](float u, float r) {
+        float x2 = ss * r * r;
+        float x6 = x2 * x2 * x2;
+        return e4 * (x6 * x6 - x6);
+    };
+    const float so = io ? sw(uo) : 0.0f, sn = in ? sw(un) : 0.0f;
+    float d = (in ? lj(un, rn) * sn : 0.0f) - (io ? lj(uo, ro) * so : 0.0f);
+    if (io && in) {
+        const float du = -(mx * (dox + dnx) + my * (doy + dny) + mz * (doz + dnz));
+        const float p = ro * rn;
+        const float dinv = -du * p * p / (ro + rn);
+        float ds = 0.0f;
+        const float ua = fmaxf(uo, c.n2f), ub = fmaxf(un, c.n2f);
+        if (ua != ub) {
+            const float dd = (uo > c.n2f && un > c.n2f) ? du : (ub - ua);
+            const float Aa = c.c2f - ua, Ab = c.c2f - ub, Bb = c.c2f + 2.0f * ub - 3.0f * c.n2f;
+            ds = c.sw2f * dd * (2.0f * Aa * Aa - (Aa + Ab) * Bb);
+        }
+        d += qk * (dinv * sn + ro * ds);
+    } else {
+        d += (in ? qk * rn * sn : 0.0f) - (io ? qk * ro * so : 0.0f);
+    }
+    return d;
+}
+
+}  // namespace mcg

@@ -1,0 +1,1105 @@
+// Single-system engine: the device side of FField_CUDA.
+//
+// Data layout in HBM (one system, n atoms):
+//   pq[n]        double4 (x, y, z, q)      FP64 master coordinates + charge (32 B, aligned loads)
+//   es[n]        double2 (eps, sig)        sqrt(eps*418.4) and MDBAS half-sigma
+//   es14[n]      double2 (eps14, sig14)
+//   fx[n]        uint4 (fx, fy, fz, q as float bits)  fixed-point mirror for the mixed kernels
+//   esf[n]       float2 (eps, sig)
+//   nbr[n*cap]   int   Verlet rows: partners j > i from the front, j < i from the back
+//   nup[n], nlo[n]
+//   cell_*       cell list of the last build
+//   exclusion CSR (stored rows, and the full-mode effective rows), 1-4 pairs and per-atom 1-4 CSR
+//   part[]       FP64 per-block partial sums (scratch), reduced in a fixed order by one block
+//
+// Kernels (all launched on the handle's stream):
+//   k_cell_assign / k_cell_scan / k_cell_scatter / k_cell_sort / k_build_rows   Verlet build
+//   k_energy_list<P>   switch energy over the half list (warp per row)        FField_MDBAS.cpp:336-424
+//   k_energy_all<P>    full energy over all pairs (triangular tile grid)      FField_MDBAS.cpp:194-265
+//   k_energy_14<P>     1-4 pairs                                               FField_MDBAS.cpp:267-318,426-488
+//   k_bonded           bonds, Urey-Bradley, angles, dihedrals, impropers       FField_MDBAS.cpp:490-786
+//   k_finalize         fixed-order reduction of the partials into ener[10]
+//   k_delta_e<P>       energy change of a moved atom set, one launch
+//   k_commit           write accepted coordinates
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+#include "pair_math.cuh"
+#include "single.hpp"
+
+namespace mcg {
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(MCG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int NB_BLOCKS = 152 * 4;   // grid of the list-driven kernels: 4 CTAs per SM
+constexpr int NB_THREADS = 256;
+constexpr int MAX_MOVED = 1024;
+constexpr int SORT_MAX = 2048;       // cells larger than this are sorted by one thread
+
+enum { PREC_F64 = 0, PREC_MIX = 1 };
+
+// ------------------------------------------------------------------------------------------
+// Verlet list build with a cell grid (replaces the O(N^2) List_nonBonded::update_verlet_list,
+// List_nonBonded.cpp:836-915; same acceptance rule: r^2 <= (rc + skin)^2 in the reference's FP64
+// arithmetic, not both frozen, not in the stored exclusion row of the lower index).
+struct Grid {
+    int nc[3];
+    double lo[3], inv[3];   // PBC none: bounding-box origin and 1/cell size
+    int periodic;
+};
+
+__global__ void k_cell_assign(const double4* __restrict__ pq, int n, PbcDev pbc, Grid g, int* cell_of,
+                              int* cell_count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 p = pq[i];
+    double c[3] = {p.x, p.y, p.z};
+    int idx[3];
+    for (int k = 0; k < 3; k++) {
+        double u;
+        if (g.periodic) { u = c[k] * pbc.rL[k]; u -= floor(u); }
+        else u = (c[k] - g.lo[k]) * g.inv[k];
+        int v = (int)(u * g.nc[k]);
+        idx[k] = min(max(v, 0), g.nc[k] - 1);
+    }
+    int cell = (idx[2] * g.nc[1] + idx[1]) * g.nc[0] + idx[0];
+    cell_of[i] = cell;
+    atomicAdd(&cell_count[cell], 1);
+}
+
+// Exclusive scan of cell counts by one block (cells are few: one per (rc+skin)^3 of volume).
+__global__ void k_cell_scan(const int* __restrict__ cell_count, int ncell, int* cell_start, int* cell_fill) {
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ncell; base += 1024) {
+        int i = base + threadIdx.x;
+        int v = i < ncell ? cell_count[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            int t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < ncell) { cell_start[i] = carry + sh[threadIdx.x] - v; cell_fill[i] = 0; }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cell_start[ncell] = carry;
+}
+
+__global__ void k_cell_scatter(const int* __restrict__ cell_of, int n, const int* __restrict__ cell_start,
+                               int* cell_fill, int* cell_atoms) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = cell_of[i];
+    int slot = atomicAdd(&cell_fill[c], 1);
+    cell_atoms[cell_start[c] + slot] = i;
+}
+
+// Sort each cell's atoms ascending so rows come out in a deterministic order.
+__global__ void k_cell_sort(const int* __restrict__ cell_start, int ncell, int* cell_atoms) {
+    __shared__ int sh[SORT_MAX];
+    int c = blockIdx.x;
+    if (c >= ncell) return;
+    int b = cell_start[c], e = cell_start[c + 1], m = e - b;
+    if (m <= 1) return;
+    if (m > SORT_MAX) {
+        if (threadIdx.x == 0)
+            for (int i = b + 1; i < e; i++) {
+                int v = cell_atoms[i], k = i - 1;
+                while (k >= b && cell_atoms[k] > v) { cell_atoms[k + 1] = cell_atoms[k]; k--; }
+                cell_atoms[k + 1] = v;
+            }
+        return;
+    }
+    int m2 = 1;
+    while (m2 < m) m2 <<= 1;
+    for (int i = threadIdx.x; i < m2; i += blockDim.x) sh[i] = i < m ? cell_atoms[b + i] : 0x7fffffff;
+    __syncthreads();
+    for (int k = 2; k <= m2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m2; i += blockDim.x) {
+                int l = i ^ j;
+                if (l > i) {
+                    bool up = (i & k) == 0;
+                    int a = sh[i], bb = sh[l];
+                    if ((a > bb) == up) { sh[i] = bb; sh[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) cell_atoms[b + i] = sh[i];
+}
+
+struct ListParams {
+    double cutnb2;
+    int cap;
+    int maxspan;
+};
+
+__device__ __forceinline__ bool stored_excluded(int lo, int hi, const int* __restrict__ xs,
+                                                const int* __restrict__ xd, int maxspan) {
+    if (hi - lo > maxspan) return false;
+    int b = xs[lo], e = xs[lo + 1];
+    for (int k = b; k < e; k++) if (xd[k] == hi) return true;
+    return false;
+}
+
+// One warp per atom i; lanes walk the candidates of the stencil cells 32 at a time.
+__global__ void __launch_bounds__(256) k_build_rows(const double4* __restrict__ pq, const uint8_t* __restrict__ frozen,
+                                                    int n, PbcDev pbc, Grid g, ListParams lp,
+                                                    const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+                                                    const int* __restrict__ cell_atoms, const int* __restrict__ xs,
+                                                    const int* __restrict__ xd, int* nbr, int* nup, int* nlo,
+                                                    int* max_row) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = warp; i < n; i += nwarps) {
+        double4 pi = pq[i];
+        bool fi = frozen[i] != 0;
+        int c = cell_of[i];
+        int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+        int rng[3][2], ctr[3] = {cx, cy, cz};
+        for (int k = 0; k < 3; k++) {
+            if (g.nc[k] >= 3) { rng[k][0] = -1; rng[k][1] = 1; }
+            else { rng[k][0] = -ctr[k]; rng[k][1] = g.nc[k] - 1 - ctr[k]; }
+            if (!g.periodic && g.nc[k] >= 3) {
+                rng[k][0] = max(-1, -ctr[k]);
+                rng[k][1] = min(1, g.nc[k] - 1 - ctr[k]);
+            }
+        }
+        int up = 0, lo = 0;
+        int* row = nbr + (size_t)i * lp.cap;
+        for (int dz = rng[2][0]; dz <= rng[2][1]; dz++)
+            for (int dy = rng[1][0]; dy <= rng[1][1]; dy++)
+                for (int dx = rng[0][0]; dx <= rng[0][1]; dx++) {
+                    int x = cx + dx, y = cy + dy, z = cz + dz;
+                    if (g.periodic) {
+                        x = (x + g.nc[0]) % g.nc[0]; y = (y + g.nc[1]) % g.nc[1]; z = (z + g.nc[2]) % g.nc[2];
+                    }
+                    int cc = (z * g.nc[1] + y) * g.nc[0] + x;
+                    int b = cell_start[cc], e = cell_start[cc + 1];
+                    for (int base = b; base < e; base += 32) {
+                        int t = base + lane;
+                        bool ok_up = false, ok_lo = false;
+                        int j = -1;
+                        if (t < e) {
+                            j = cell_atoms[t];
+                            if (j != i) {
+                                double4 pj = pq[j];
+                                double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
+                                if (r2 <= lp.cutnb2 && !(fi && frozen[j])) {
+                                    int a = min(i, j), bb = max(i, j);
+                                    if (!stored_excluded(a, bb, xs, xd, lp.maxspan)) {
+                                        ok_up = j > i;
+                                        ok_lo = j < i;
+                                    }
+                                }
+                            }
+                        }
+                        unsigned bu = __ballot_sync(0xffffffffu, ok_up);
+                        unsigned bl = __ballot_sync(0xffffffffu, ok_lo);
+                        unsigned lt = (1u << lane) - 1u;
+                        if (ok_up) {
+                            int pos = up + __popc(bu & lt);
+                            if (pos + lo < lp.cap) row[pos] = j;
+                        }
+                        if (ok_lo) {
+                            int pos = lo + __popc(bl & lt);
+                            if (up + pos < lp.cap) row[lp.cap - 1 - pos] = j;
+                        }
+                        up += __popc(bu);
+                        lo += __popc(bl);
+                    }
+                }
+        if (lane == 0) {
+            nup[i] = up;
+            nlo[i] = lo;
+            atomicMax(max_row, up + lo);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Energies.
+struct AtomsDev {
+    const double4* pq;
+    const double2* es;
+    const double2* es14;
+    const uint4* fx;
+    const float2* esf;
+    const float2* esf14;
+    float Ls[3];          // box / 2^32 (mixed displacement scale)
+};
+
+template <int P>
+__device__ __forceinline__ void pair_energy(const AtomsDev& A, const PbcDev& pbc, const CutDev& cut, bool fourteen,
+                                            double4 pi, uint4 fi, int i, double4 pj, uint4 fj, int j,
+                                            bool apply_cut, double& el, double& vd) {
+    if (P == PREC_F64) {
+        double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
+        el = 0.0; vd = 0.0;
+        if (apply_cut && r2 > cut.c2) return;
+        double2 a = fourteen ? A.es14[i] : A.es[i];
+        double2 b = fourteen ? A.es14[j] : A.es[j];
+        ref64_pair(r2, pi.w, pj.w, a.x, b.x, a.y, b.y, apply_cut, cut, el, vd);
+    } else {
+        float dx, dy, dz;
+        if (pbc.type != 0) {
+            dx = fixed_delta(fi.x, fj.x, A.Ls[0]);
+            dy = fixed_delta(fi.y, fj.y, A.Ls[1]);
+            dz = fixed_delta(fi.z, fj.z, A.Ls[2]);
+        } else {
+            dx = (float)(pj.x - pi.x); dy = (float)(pj.y - pi.y); dz = (float)(pj.z - pi.z);
+        }
+        float r2 = dx * dx + dy * dy + dz * dz;
+        el = 0.0; vd = 0.0;
+        if (apply_cut && r2 > cut.c2f) return;
+        float2 a = fourteen ? A.esf14[i] : A.esf[i];
+        float2 b = fourteen ? A.esf14[j] : A.esf[j];
+        float s = a.y + b.y;
+        float e1, v1;
+        mixed_pair(r2, __int_as_float(fi.w) * __int_as_float(fj.w), a.x * b.x, s * s, apply_cut, cut, e1, v1);
+        el = e1; vd = v1;
+    }
+}
+
+__device__ __forceinline__ void block_reduce2(double a, double b, double* out) {
+    __shared__ double sa[32], sb[32];
+    a = warp_sum(a); b = warp_sum(b);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { sa[w] = a; sb[w] = b; }
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        a = l < nw ? sa[l] : 0.0; b = l < nw ? sb[l] : 0.0;
+        a = warp_sum(a); b = warp_sum(b);
+        if (l == 0) { out[0] = a; out[1] = b; }
+    }
+    __syncthreads();
+}
+
+// Switch energy over the half list: a warp per row i, lanes over its j > i entries.
+template <int P>
+__global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, PbcDev pbc, CutDev cut,
+                                                            const int* __restrict__ nbr, const int* __restrict__ nup,
+                                                            int cap, double* part) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double sel = 0.0, svd = 0.0;
+    for (int i = warp; i < n; i += nwarps) {
+        double4 pi = A.pq[i];
+        uint4 fi = P == PREC_MIX ? A.fx[i] : make_uint4(0, 0, 0, 0);
+        const int* row = nbr + (size_t)i * cap;
+        int m = nup[i];
+        F32Acc fe, fv;
+        for (int k = lane; k < m; k += 32) {
+            int j = row[k];
+            double4 pj = P == PREC_F64 ? A.pq[j] : make_double4(0, 0, 0, 0);
+            uint4 fj = P == PREC_MIX ? A.fx[j] : make_uint4(0, 0, 0, 0);
+            if (P == PREC_MIX && pbc.type == 0) pj = A.pq[j];
+            double el, vd;
+            pair_energy<P>(A, pbc, cut, false, pi, fi, i, pj, fj, j, true, el, vd);
+            if (P == PREC_F64) { sel += el; svd += vd; }
+            else { fe.add((float)el); fv.add((float)vd); }
+        }
+        if (P == PREC_MIX) { sel += fe.value(); svd += fv.value(); }
+    }
+    block_reduce2(sel, svd, part + 2 * blockIdx.x);
+}
+
+// Full energy: all pairs j > i not in the full-mode exclusion row of i, no cutoff.  Triangular
+// grid of TILE x TILE blocks; each thread owns one i and walks a shared-memory j tile with the
+// reference's sorted-row cursor (FField_MDBAS.cpp:227-234).
+constexpr int TILE = 128;
+
+template <int P>
+__global__ void __launch_bounds__(TILE) k_energy_all(AtomsDev A, int n, PbcDev pbc, CutDev cut,
+                                                     const int* __restrict__ fxs, const int* __restrict__ fxd,
+                                                     int ntile, double* part) {
+    __shared__ double4 spq[TILE];
+    __shared__ uint4 sfx[TILE];
+    // block -> (I, J) with I <= J, row-major over the upper triangle
+    int b = blockIdx.x;
+    int I = 0;
+    while (b >= ntile - I) { b -= ntile - I; I++; }
+    int J = I + b;
+    int i = I * TILE + threadIdx.x;
+    int jt = J * TILE + threadIdx.x;
+    if (jt < n) {
+        spq[threadIdx.x] = A.pq[jt];
+        if (P == PREC_MIX) sfx[threadIdx.x] = A.fx[jt];
+    }
+    __syncthreads();
+    double sel = 0.0, svd = 0.0;
+    if (i < n) {
+        double4 pi = A.pq[i];
+        uint4 fi = P == PREC_MIX ? A.fx[i] : make_uint4(0, 0, 0, 0);
+        int xb = fxs[i], xe = fxs[i + 1];
+        int cur = xb;
+        int j0 = max(J * TILE, i + 1);
+        while (cur < xe && fxd[cur] < j0) cur++;
+        int jend = min(n, J * TILE + TILE);
+        F32Acc fe, fv;
+        for (int j = j0; j < jend; j++) {
+            if (cur < xe && fxd[cur] == j) { cur++; continue; }
+            int t = j - J * TILE;
+            double el, vd;
+            pair_energy<P>(A, pbc, cut, false, pi, fi, i, spq[t], P == PREC_MIX ? sfx[t] : make_uint4(0, 0, 0, 0), j,
+                           false, el, vd);
+            if (P == PREC_F64) { sel += el; svd += vd; }
+            else { fe.add((float)el); fv.add((float)vd); }
+        }
+        if (P == PREC_MIX) { sel = fe.value(); svd = fv.value(); }
+    }
+    block_reduce2(sel, svd, part + 2 * blockIdx.x);
+}
+
+template <int P>
+__global__ void k_energy_14(AtomsDev A, PbcDev pbc, CutDev cut, const int2* __restrict__ p14, int n14, double* part) {
+    double sel = 0.0, svd = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n14; k += gridDim.x * blockDim.x) {
+        int2 p = p14[k];
+        double el, vd;
+        uint4 fi = P == PREC_MIX ? A.fx[p.x] : make_uint4(0, 0, 0, 0);
+        uint4 fj = P == PREC_MIX ? A.fx[p.y] : make_uint4(0, 0, 0, 0);
+        pair_energy<P>(A, pbc, cut, true, A.pq[p.x], fi, p.x, A.pq[p.y], fj, p.y, cut.mode == 1, el, vd);
+        sel += el; svd += vd;
+    }
+    block_reduce2(sel, svd, part + 2 * blockIdx.x);
+}
+
+// ---- bonded terms (FP64, device math library) ---------------------------------------------
+struct BondedDev {
+    const BondT* bonds; int nb;
+    const BondT* ubs; int nu;
+    const AngleT* angles; int na;
+    const TorsT* dihes; int nd;
+    const TorsT* imprs; int ni;
+};
+
+__device__ __forceinline__ void crd(const double4* pq, int i, double c[3]) {
+    double4 p = pq[i]; c[0] = p.x; c[1] = p.y; c[2] = p.z;
+}
+__device__ __forceinline__ void apply_pbc(double d[3], const PbcDev& p) {
+    if (p.type != 0) for (int k = 0; k < 3; k++) d[k] = ref64_mic(d[k], p.L[k], p.rL[k]);
+}
+
+// crd_of: coordinates of atom i, with moved atoms taken from the proposal.
+struct CrdSrc {
+    const double4* pq;
+    const int* mv_idx; const double* mv_xyz; int m;   // sorted moved atoms (may be m = 0)
+    __device__ __forceinline__ void get(int i, double c[3]) const {
+        int lo = 0, hi = m - 1;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1, v = mv_idx[mid];
+            if (v == i) { c[0] = mv_xyz[3 * mid]; c[1] = mv_xyz[3 * mid + 1]; c[2] = mv_xyz[3 * mid + 2]; return; }
+            if (v < i) lo = mid + 1; else hi = mid - 1;
+        }
+        crd(pq, i, c);
+    }
+};
+
+__device__ double bond_e(const BondT& b, const CrdSrc& S, const PbcDev& pbc, bool morse_ok) {
+    double di[3], dj[3];
+    S.get(b.a, di); S.get(b.b, dj);
+    double d = sqrt(ref64_dist2(di[0], di[1], di[2], dj[0], dj[1], dj[2], pbc));
+    if (morse_ok && b.type == 1) {
+        double ma = exp(-b.beta * (d - b.r0));
+        return b.k * (ma * ma - 2. * ma) + b.k;
+    }
+    return 0.5 * b.k * (d - b.r0) * (d - b.r0);
+}
+
+__device__ double angle_e(const AngleT& a, const CrdSrc& S, const PbcDev& pbc) {
+    double di[3], dj[3], dk[3], dab[3], dbc[3];
+    S.get(a.a, di); S.get(a.b, dj); S.get(a.c, dk);
+    double rab = sqrt(ref64_dist2(di[0], di[1], di[2], dj[0], dj[1], dj[2], pbc, dab));
+    double rbc = sqrt(ref64_dist2(dk[0], dk[1], dk[2], dj[0], dj[1], dj[2], pbc, dbc));
+    double cost = (dab[0] * dbc[0] + dab[1] * dbc[1] + dab[2] * dbc[2]) / (rab * rbc);
+    double th = acos(cost) - a.theta0;
+    return 0.5 * a.k * th * th;
+}
+
+__device__ double tors_e(const TorsT& t, const CrdSrc& S, const PbcDev& pbc) {
+    double di[3], dj[3], dk[3], dl[3], dab[3], dbc[3], dcd[3], pb[3], pc[3];
+    S.get(t.a, di); S.get(t.b, dj); S.get(t.c, dk); S.get(t.d, dl);
+    for (int k = 0; k < 3; k++) { dab[k] = di[k] - dj[k]; dcd[k] = dk[k] - dl[k]; }
+    apply_pbc(dab, pbc); apply_pbc(dcd, pbc);
+    double rbc = sqrt(ref64_dist2(dk[0], dk[1], dk[2], dj[0], dj[1], dj[2], pbc, dbc));
+    pb[0] = dab[1] * dbc[2] - dab[2] * dbc[1];
+    pb[1] = dab[2] * dbc[0] - dab[0] * dbc[2];
+    pb[2] = dab[0] * dbc[1] - dab[1] * dbc[0];
+    double rpb = sqrt(pb[0] * pb[0] + pb[1] * pb[1] + pb[2] * pb[2]);
+    pc[0] = dbc[1] * dcd[2] - dbc[2] * dcd[1];
+    pc[1] = dbc[2] * dcd[0] - dbc[0] * dcd[2];
+    pc[2] = dbc[0] * dcd[1] - dbc[1] * dcd[0];
+    double rpc = sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+    double cosp = (pb[0] * pc[0] + pb[1] * pc[1] + pb[2] * pc[2]) / (rpb * rpc);
+    double sinp = (dbc[0] * (pc[1] * pb[2] - pc[2] * pb[1]) + dbc[1] * (pb[0] * pc[2] - pb[2] * pc[0]) +
+                   dbc[2] * (pc[0] * pb[1] - pc[1] * pb[0])) / (rpb * rpc * rbc);
+    double phi = atan2(sinp, cosp);
+    if (t.type == 2) {
+        phi = phi - t.phi0;
+        phi = phi - ref64_rint(phi / TWOPI) * TWOPI;
+        return 0.5 * t.k * phi * phi;
+    }
+    return t.k * (1. + cos(t.mult * phi - t.phi0));
+}
+
+// part layout: 5 doubles per block (bond, ang, ub, dihe, impr)
+__global__ void k_bonded(BondedDev B, PbcDev pbc, const double4* __restrict__ pq, double* part) {
+    double e[5] = {0, 0, 0, 0, 0};
+    CrdSrc S{pq, nullptr, nullptr, 0};
+    int total = B.nb + B.na + B.nu + B.nd + B.ni;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        int t = k;
+        if (t < B.nb) { e[0] += bond_e(B.bonds[t], S, pbc, true); continue; }
+        t -= B.nb;
+        if (t < B.na) { e[1] += angle_e(B.angles[t], S, pbc); continue; }
+        t -= B.na;
+        if (t < B.nu) { e[2] += bond_e(B.ubs[t], S, pbc, false); continue; }
+        t -= B.nu;
+        if (t < B.nd) { e[3] += tors_e(B.dihes[t], S, pbc); continue; }
+        t -= B.nd;
+        e[4] += tors_e(B.imprs[t], S, pbc);
+    }
+    __shared__ double sh[5][32];
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int c = 0; c < 5; c++) {
+        double v = warp_sum(e[c]);
+        if (l == 0) sh[c][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[threadIdx.x][k];
+        part[5 * blockIdx.x + threadIdx.x] = s;
+    }
+}
+
+// Fixed-order reduction: one block.  nbp/n14p pairs of (el, vd) partials, bdp blocks of 5.
+__global__ void k_finalize(const double* __restrict__ nb, int nnb, const double* __restrict__ p14, int n14,
+                           const double* __restrict__ bd, int nbd, double* out) {
+    __shared__ double sh[9][256];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = threadIdx.x; k < nnb; k += blockDim.x) { acc[0] += nb[2 * k]; acc[1] += nb[2 * k + 1]; }
+    for (int k = threadIdx.x; k < n14; k += blockDim.x) { acc[2] += p14[2 * k]; acc[3] += p14[2 * k + 1]; }
+    for (int k = threadIdx.x; k < nbd; k += blockDim.x)
+        for (int c = 0; c < 5; c++) acc[4 + c] += bd[5 * k + c];
+    for (int c = 0; c < 9; c++) sh[c][threadIdx.x] = acc[c];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) for (int c = 0; c < 9; c++) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double K = CHGCHARMM * KCALTOIU;
+        double elec = K * sh[0][0];
+        double vdw = 4.0 * sh[1][0];
+        elec += K * sh[2][0];
+        vdw += 4.0 * sh[3][0];
+        double bond = sh[4][0], ang = sh[5][0], ub = sh[6][0], dihe = sh[7][0], impr = sh[8][0];
+        double pot = elec + vdw + bond + ang + ub + dihe + impr;
+        out[0] = pot + 0.0; out[1] = pot; out[2] = 0.0; out[3] = elec; out[4] = vdw;
+        out[5] = bond; out[6] = ang; out[7] = ub; out[8] = dihe; out[9] = impr;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Energy change of a moved set.  Block b < m handles moved atom mv[b] against its partners
+// (Verlet row in switch mode, every atom in full mode) and its 1-4 partners; block m evaluates
+// the listed bonded terms.  Pairs with both atoms moved are counted once, by the lower index.
+// The last block to finish sums the partials in block order and writes de (iu).
+struct MoveDev {
+    int m;
+    const int* idx;        // sorted moved atoms
+    const double* xyz;     // their proposed coordinates (3 per atom)
+    const int* terms;      // bonded terms touching them: (kind, index) pairs
+    int nterms;
+};
+
+template <int P>
+__global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, CutDev cut, MoveDev mv,
+                                                 const int* __restrict__ nbr, const int* __restrict__ nup,
+                                                 const int* __restrict__ nlo, int cap,
+                                                 const int* __restrict__ fxs, const int* __restrict__ fxd,
+                                                 const int* __restrict__ c14s, const int* __restrict__ c14d,
+                                                 BondedDev B, double* part, unsigned* ticket, double* out) {
+    __shared__ int s_idx[MAX_MOVED];
+    __shared__ double s_xyz[3 * MAX_MOVED];
+    __shared__ uint4 s_fx[MAX_MOVED];
+    __shared__ bool s_last;
+    const int m = mv.m;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        s_idx[k] = mv.idx[k];
+        double x = mv.xyz[3 * k], y = mv.xyz[3 * k + 1], z = mv.xyz[3 * k + 2];
+        s_xyz[3 * k] = x; s_xyz[3 * k + 1] = y; s_xyz[3 * k + 2] = z;
+        if (P == PREC_MIX) {
+            uint4 f = A.fx[mv.idx[k]];
+            if (pbc.type != 0) { f.x = to_fixed(x, pbc.rL[0]); f.y = to_fixed(y, pbc.rL[1]); f.z = to_fixed(z, pbc.rL[2]); }
+            s_fx[k] = f;
+        }
+    }
+    __syncthreads();
+    auto slot = [&](int j) -> int {
+        int lo = 0, hi = m - 1;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1, v = s_idx[mid];
+            if (v == j) return mid;
+            if (v < j) lo = mid + 1; else hi = mid - 1;
+        }
+        return -1;
+    };
+    double del = 0.0, dvd = 0.0, dbd = 0.0;
+    const bool sw = cut.mode == 1;
+    if ((int)blockIdx.x < m) {
+        const int ka = blockIdx.x;
+        const int a = s_idx[ka];
+        const double4 ao = A.pq[a];
+        const double4 an = make_double4(s_xyz[3 * ka], s_xyz[3 * ka + 1], s_xyz[3 * ka + 2], ao.w);
+        const uint4 fo = P == PREC_MIX ? A.fx[a] : make_uint4(0, 0, 0, 0);
+        const uint4 fn = P == PREC_MIX ? s_fx[ka] : make_uint4(0, 0, 0, 0);
+        // mixed: displacement of the moved atom as the fixed-point mirror sees it (exact)
+        float ma[3] = {0.f, 0.f, 0.f};
+        CutDev cutx = cut;   // full mode: no cutoff and no switch
+        if (!sw) { cutx.c2f = 3.0e38f; cutx.n2f = 3.0e38f; }
+        if (P == PREC_MIX) {
+            if (pbc.type != 0) {
+                ma[0] = fixed_delta(fo.x, fn.x, A.Ls[0]); ma[1] = fixed_delta(fo.y, fn.y, A.Ls[1]); ma[2] = fixed_delta(fo.z, fn.z, A.Ls[2]);
+            } else {
+                ma[0] = (float)(an.x - ao.x); ma[1] = (float)(an.y - ao.y); ma[2] = (float)(an.z - ao.z);
+            }
+        }
+        auto visit = [&](int j, bool fourteen, bool apply_cut) {
+            int sj = slot(j);
+            if (sj >= 0 && j < a) return;       // counted by the lower index's block
+            double4 jo = A.pq[j];
+            uint4 gjo = P == PREC_MIX ? A.fx[j] : make_uint4(0, 0, 0, 0);
+            double4 jn = jo;
+            uint4 gjn = gjo;
+            if (sj >= 0) { jn.x = s_xyz[3 * sj]; jn.y = s_xyz[3 * sj + 1]; jn.z = s_xyz[3 * sj + 2]; if (P == PREC_MIX) gjn = s_fx[sj]; }
+            if (P == PREC_F64) {
+                double e0, v0, e1, v1;
+                pair_energy<P>(A, pbc, cut, fourteen, ao, fo, a, jo, gjo, j, apply_cut, e0, v0);
+                pair_energy<P>(A, pbc, cut, fourteen, an, fn, a, jn, gjn, j, apply_cut, e1, v1);
+                del += e1 - e0;
+                dvd += v1 - v0;
+            } else {
+                // d_old = j_old - a_old, d_new = j_new - a_new = d_old - m
+                float d[3], m[3];
+                if (pbc.type != 0) {
+                    d[0] = fixed_delta(fo.x, gjo.x, A.Ls[0]); d[1] = fixed_delta(fo.y, gjo.y, A.Ls[1]); d[2] = fixed_delta(fo.z, gjo.z, A.Ls[2]);
+                } else {
+                    d[0] = (float)(jo.x - ao.x); d[1] = (float)(jo.y - ao.y); d[2] = (float)(jo.z - ao.z);
+                }
+                if (sj >= 0) {   // both atoms moved: m = d_old - d_new
+                    float dn[3];
+                    if (pbc.type != 0) {
+                        dn[0] = fixed_delta(fn.x, gjn.x, A.Ls[0]); dn[1] = fixed_delta(fn.y, gjn.y, A.Ls[1]); dn[2] = fixed_delta(fn.z, gjn.z, A.Ls[2]);
+                    } else {
+                        dn[0] = (float)(jn.x - an.x); dn[1] = (float)(jn.y - an.y); dn[2] = (float)(jn.z - an.z);
+                    }
+                    m[0] = d[0] - dn[0]; m[1] = d[1] - dn[1]; m[2] = d[2] - dn[2];
+                } else { m[0] = ma[0]; m[1] = ma[1]; m[2] = ma[2]; }
+                float2 pa = fourteen ? A.esf14[a] : A.esf[a];
+                float2 pb = fourteen ? A.esf14[j] : A.esf[j];
+                float s = pa.y + pb.y;
+                float qk = (float)(CHGCHARMM * KCALTOIU) * __int_as_float(fo.w) * __int_as_float(gjo.w);
+                int np_ = 0;
+                dbd += (double)mixed_pair_delta(d[0], d[1], d[2], m[0], m[1], m[2], qk, 4.0f * pa.x * pb.x, s * s,
+                                                apply_cut ? cut : cutx, np_);
+            }
+        };
+        if (sw) {
+            const int* row = nbr + (size_t)a * cap;
+            int u = nup[a], l = nlo[a];
+            for (int k = threadIdx.x; k < u + l; k += blockDim.x) {
+                int j = k < u ? row[k] : row[cap - 1 - (k - u)];
+                visit(j, false, true);
+            }
+        } else {
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                if (j == a) continue;
+                int lo_ = min(a, j), hi_ = max(a, j);
+                bool ex = false;
+                for (int k = fxs[lo_]; k < fxs[lo_ + 1]; k++) if (fxd[k] == hi_) { ex = true; break; }
+                if (!ex) visit(j, false, false);
+            }
+        }
+        for (int k = c14s[a] + threadIdx.x; k < c14s[a + 1]; k += blockDim.x) visit(c14d[k], true, sw);
+    } else {
+        CrdSrc S_old{A.pq, nullptr, nullptr, 0};
+        CrdSrc S_new{A.pq, s_idx, s_xyz, m};
+        for (int k = threadIdx.x; k < mv.nterms; k += blockDim.x) {
+            int kind = mv.terms[2 * k], t = mv.terms[2 * k + 1];
+            double e0 = 0, e1 = 0;
+            if (kind == 0) { e0 = bond_e(B.bonds[t], S_old, pbc, true); e1 = bond_e(B.bonds[t], S_new, pbc, true); }
+            else if (kind == 1) { e0 = angle_e(B.angles[t], S_old, pbc); e1 = angle_e(B.angles[t], S_new, pbc); }
+            else if (kind == 2) { e0 = bond_e(B.ubs[t], S_old, pbc, false); e1 = bond_e(B.ubs[t], S_new, pbc, false); }
+            else if (kind == 3) { e0 = tors_e(B.dihes[t], S_old, pbc); e1 = tors_e(B.dihes[t], S_new, pbc); }
+            else { e0 = tors_e(B.imprs[t], S_old, pbc); e1 = tors_e(B.imprs[t], S_new, pbc); }
+            dbd += e1 - e0;
+        }
+    }
+    __shared__ double red[3];
+    block_reduce2(del, dvd, red);
+    {
+        double v = warp_sum(dbd);
+        __shared__ double sb[32];
+        if ((threadIdx.x & 31) == 0) sb[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sb[k];
+            red[2] = s;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = red[0];
+        part[3 * blockIdx.x + 1] = red[1];
+        part[3 * blockIdx.x + 2] = red[2];
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        double se = 0.0, sv = 0.0, sb = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) {
+            se += ((volatile double*)part)[3 * b];
+            sv += ((volatile double*)part)[3 * b + 1];
+            sb += ((volatile double*)part)[3 * b + 2];
+        }
+        out[0] = CHGCHARMM * KCALTOIU * se + 4.0 * sv + sb;
+        out[1] = se; out[2] = sv; out[3] = sb;
+        *ticket = 0u;
+    }
+}
+
+template <int P>
+__global__ void k_commit(int m, const int* __restrict__ idx, const double* __restrict__ xyz, double4* pq, uint4* fx,
+                         PbcDev pbc) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    int a = idx[k];
+    double4 p = pq[a];
+    p.x = xyz[3 * k]; p.y = xyz[3 * k + 1]; p.z = xyz[3 * k + 2];
+    pq[a] = p;
+    if (pbc.type != 0) {
+        uint4 f = fx[a];
+        f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]);
+        fx[a] = f;
+    }
+}
+
+__global__ void k_fix_all(int n, const double4* __restrict__ pq, uint4* fx, PbcDev pbc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 p = pq[i];
+    uint4 f;
+    if (pbc.type != 0) { f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]); }
+    else { f.x = f.y = f.z = 0; }
+    f.w = __float_as_uint((float)p.w);
+    fx[i] = f;
+}
+
+// ==========================================================================================
+// Host side of the engine.
+template <typename T>
+static int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return MCG_OK;
+}
+
+template <typename T>
+static int dupload(T** p, const std::vector<T>& v, cudaStream_t st) {
+    int rc = dalloc(p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) CK(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return MCG_OK;
+}
+
+SingleEngine::~SingleEngine() { release(); }
+
+void SingleEngine::release() {
+    void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
+                    d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
+                    d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_out, d_maxrow,
+                    d_stage};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    if (h_stage) cudaFreeHost(h_stage);
+    if (stream) cudaStreamDestroy(stream);
+    d_pq = nullptr; stream = nullptr; h_stage = nullptr;
+}
+
+int SingleEngine::init(const HostSystem& h) {
+    hs = h;
+    n = hs.n;
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    pbc.type = hs.pbc;
+    for (int k = 0; k < 3; k++) { pbc.L[k] = hs.L[k]; pbc.rL[k] = hs.rL[k]; }
+    cut.mode = hs.cut;
+    cut.c2 = hs.rc * hs.rc;
+    cut.n2 = hs.ron * hs.ron;
+    {
+        double d = cut.c2 - cut.n2;
+        cut.sw2 = 1. / (d * d * d);
+    }
+    cut.c2f = (float)cut.c2; cut.n2f = (float)cut.n2; cut.sw2f = (float)cut.sw2;
+    std::vector<double4> pq(n);
+    std::vector<double2> es(n), es14(n);
+    std::vector<float2> esf(n), esf14(n);
+    for (int i = 0; i < n; i++) {
+        pq[i] = make_double4(hs.x[i], hs.y[i], hs.z[i], hs.q[i]);
+        es[i] = make_double2(hs.eps[i], hs.sig[i]);
+        es14[i] = make_double2(hs.eps14[i], hs.sig14[i]);
+        esf[i] = make_float2((float)hs.eps[i], (float)hs.sig[i]);
+        esf14[i] = make_float2((float)hs.eps14[i], (float)hs.sig14[i]);
+    }
+    int rc;
+    if ((rc = dupload(&d_pq, pq, stream)) || (rc = dupload(&d_es, es, stream)) || (rc = dupload(&d_es14, es14, stream)) ||
+        (rc = dupload(&d_esf, esf, stream)) || (rc = dupload(&d_esf14, esf14, stream)) ||
+        (rc = dupload(&d_frozen, hs.frozen, stream)) || (rc = dupload(&d_xs, hs.exclStart, stream)) ||
+        (rc = dupload(&d_xd, hs.exclData, stream)) || (rc = dupload(&d_fxs, hs.fexclStart, stream)) ||
+        (rc = dupload(&d_fxd, hs.fexclData, stream)))
+        return rc;
+    if ((rc = dalloc(&d_fx, n))) return rc;
+    // 1-4 pairs and their per-atom CSR (both directions) for the ΔE kernel
+    n14 = (int)hs.pairs14.size() / 2;
+    std::vector<int2> p14(n14);
+    std::vector<std::vector<int>> adj(n);
+    for (int k = 0; k < n14; k++) {
+        p14[k] = make_int2(hs.pairs14[2 * k], hs.pairs14[2 * k + 1]);
+        adj[p14[k].x].push_back(p14[k].y);
+        adj[p14[k].y].push_back(p14[k].x);
+    }
+    std::vector<int> c14s(n + 1, 0), c14d;
+    for (int i = 0; i < n; i++) { c14s[i] = (int)c14d.size(); c14d.insert(c14d.end(), adj[i].begin(), adj[i].end()); }
+    c14s[n] = (int)c14d.size();
+    if ((rc = dupload(&d_p14, p14, stream)) || (rc = dupload(&d_c14s, c14s, stream)) || (rc = dupload(&d_c14d, c14d, stream)))
+        return rc;
+    if ((rc = dupload(&d_bonds, hs.bonds, stream)) || (rc = dupload(&d_ubs, hs.ubs, stream)) ||
+        (rc = dupload(&d_angles, hs.angles, stream)) || (rc = dupload(&d_dihes, hs.dihes, stream)) ||
+        (rc = dupload(&d_imprs, hs.imprs, stream)))
+        return rc;
+    // per-atom bonded-term index for ΔE (kind, index)
+    term_start.assign(n + 1, 0);
+    std::vector<std::vector<int>> tl(n);
+    auto addt = [&](int atom, int kind, int idx) { tl[atom].push_back(kind); tl[atom].push_back(idx); };
+    for (int k = 0; k < (int)hs.bonds.size(); k++) { addt(hs.bonds[k].a, 0, k); addt(hs.bonds[k].b, 0, k); }
+    for (int k = 0; k < (int)hs.angles.size(); k++) { const AngleT& a = hs.angles[k]; addt(a.a, 1, k); addt(a.b, 1, k); addt(a.c, 1, k); }
+    for (int k = 0; k < (int)hs.ubs.size(); k++) { addt(hs.ubs[k].a, 2, k); addt(hs.ubs[k].b, 2, k); }
+    for (int k = 0; k < (int)hs.dihes.size(); k++) { const TorsT& t = hs.dihes[k]; addt(t.a, 3, k); addt(t.b, 3, k); addt(t.c, 3, k); addt(t.d, 3, k); }
+    for (int k = 0; k < (int)hs.imprs.size(); k++) { const TorsT& t = hs.imprs[k]; addt(t.a, 4, k); addt(t.b, 4, k); addt(t.c, 4, k); addt(t.d, 4, k); }
+    term_data.clear();
+    for (int i = 0; i < n; i++) { term_start[i] = (int)term_data.size() / 2; term_data.insert(term_data.end(), tl[i].begin(), tl[i].end()); }
+    term_start[n] = (int)term_data.size() / 2;
+    // scratch: partial sums and the ΔE ticket
+    ntile = (n + TILE - 1) / TILE;
+    size_t nparts = std::max<size_t>({(size_t)NB_BLOCKS, (size_t)ntile * (ntile + 1) / 2, (size_t)MAX_MOVED + 1});
+    part_cap = nparts * 3 + 2 * 64 + 5 * 64 + 16;
+    if ((rc = dalloc(&d_part, part_cap)) || (rc = dalloc(&d_ticket, 1)) || (rc = dalloc(&d_out, 16)) ||
+        (rc = dalloc(&d_maxrow, 1)))
+        return rc;
+    CK(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned), stream));
+    // staging for moves: idx (sorted), xyz, terms
+    stage_bytes = (size_t)MAX_MOVED * (4 + 24) + 64 * 1024 * 8;
+    CK(cudaMallocHost(&h_stage, stage_bytes));
+    if ((rc = dalloc((char**)&d_stage, stage_bytes))) return rc;
+    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
+    CK(cudaGetLastError());
+    host_x = hs.x; host_y = hs.y; host_z = hs.z;
+    if (hs.cut == MCG_CUT_SWITCH) {
+        if ((rc = build_list())) return rc;
+    }
+    CK(cudaStreamSynchronize(stream));
+    return MCG_OK;
+}
+
+AtomsDev SingleEngine::atoms() const {
+    AtomsDev A;
+    A.pq = d_pq; A.es = d_es; A.es14 = d_es14; A.fx = d_fx; A.esf = d_esf; A.esf14 = d_esf14;
+    for (int k = 0; k < 3; k++) A.Ls[k] = (float)(hs.L[k] / 4294967296.0);
+    return A;
+}
+
+BondedDev SingleEngine::bonded() const {
+    return BondedDev{d_bonds, (int)hs.bonds.size(), d_ubs, (int)hs.ubs.size(), d_angles, (int)hs.angles.size(),
+                     d_dihes, (int)hs.dihes.size(), d_imprs, (int)hs.imprs.size()};
+}
+
+int SingleEngine::build_list() {
+    const double rl = hs.rc + hs.dcut;
+    Grid g;
+    g.periodic = hs.pbc != MCG_PBC_NONE;
+    if (g.periodic) {
+        for (int k = 0; k < 3; k++) { g.nc[k] = std::max(1, (int)std::floor(hs.L[k] / rl)); g.lo[k] = 0; g.inv[k] = 0; }
+    } else {
+        for (int k = 0; k < 3; k++) {
+            const std::vector<double>& c = k == 0 ? host_x : (k == 1 ? host_y : host_z);
+            double lo = *std::min_element(c.begin(), c.end()), hi = *std::max_element(c.begin(), c.end());
+            double ext = std::max(hi - lo, 1e-6);
+            g.nc[k] = std::max(1, (int)std::floor(ext / rl));
+            g.lo[k] = lo;
+            g.inv[k] = 1.0 / ext * (1.0 - 1e-12);
+        }
+    }
+    while ((long long)g.nc[0] * g.nc[1] * g.nc[2] > (1 << 20))
+        for (int k = 0; k < 3; k++) g.nc[k] = std::max(1, g.nc[k] / 2);
+    int ncell = g.nc[0] * g.nc[1] * g.nc[2];
+    int rc;
+    if (ncell > ncell_cap) {
+        if (d_cell_count) { cudaFree(d_cell_count); cudaFree(d_cell_start); cudaFree(d_cell_fill); }
+        if ((rc = dalloc(&d_cell_count, ncell)) || (rc = dalloc(&d_cell_start, ncell + 1)) || (rc = dalloc(&d_cell_fill, ncell)))
+            return rc;
+        ncell_cap = ncell;
+    }
+    if (!d_cell_of) {
+        if ((rc = dalloc(&d_cell_of, n)) || (rc = dalloc(&d_cell_atoms, n)) || (rc = dalloc(&d_nup, n)) || (rc = dalloc(&d_nlo, n)))
+            return rc;
+    }
+    if (cap == 0) {
+        // initial capacity from the density of the list sphere, grown on overflow below
+        double vol = g.periodic ? hs.L[0] * hs.L[1] * hs.L[2] : 0.0;
+        double est = g.periodic ? (4.0 / 3.0 * PI * rl * rl * rl) * n / vol : n;
+        cap = (int)std::min<double>(n, est * 1.3 + 64);
+        cap = (cap + 31) & ~31;
+        if ((rc = dalloc(&d_nbr, (size_t)n * cap))) return rc;
+    }
+    ListParams lp{rl * rl, cap, hs.maxExclSpan};
+    {
+        double t = hs.rc + hs.dcut;  // (cutoff + deltacut)^2 as List_nonBonded.cpp:842-843
+        lp.cutnb2 = t * t;
+    }
+    for (int attempt = 0; attempt < 3; attempt++) {
+        CK(cudaMemsetAsync(d_cell_count, 0, sizeof(int) * ncell, stream));
+        CK(cudaMemsetAsync(d_maxrow, 0, sizeof(int), stream));
+        k_cell_assign<<<(n + 255) / 256, 256, 0, stream>>>(d_pq, n, pbc, g, d_cell_of, d_cell_count);
+        k_cell_scan<<<1, 1024, 0, stream>>>(d_cell_count, ncell, d_cell_start, d_cell_fill);
+        k_cell_scatter<<<(n + 255) / 256, 256, 0, stream>>>(d_cell_of, n, d_cell_start, d_cell_fill, d_cell_atoms);
+        k_cell_sort<<<ncell, 256, 0, stream>>>(d_cell_start, ncell, d_cell_atoms);
+        int blocks = std::min((n + 7) / 8, NB_BLOCKS * 2);
+        k_build_rows<<<blocks, 256, 0, stream>>>(d_pq, d_frozen, n, pbc, g, lp, d_cell_of, d_cell_start, d_cell_atoms,
+                                                 d_xs, d_xd, d_nbr, d_nup, d_nlo, d_maxrow);
+        CK(cudaGetLastError());
+        int maxrow = 0;
+        CK(cudaMemcpyAsync(&maxrow, d_maxrow, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        last_max_row = maxrow;
+        if (maxrow <= cap) return MCG_OK;
+        cudaFree(d_nbr);
+        d_nbr = nullptr;
+        cap = ((int)(maxrow * 1.1) + 32 + 31) & ~31;
+        lp.cap = cap;
+        if ((rc = dalloc(&d_nbr, (size_t)n * cap))) return rc;
+    }
+    return fail(MCG_ECAPACITY, "Verlet row capacity could not be grown");
+}
+
+int SingleEngine::energy(double ener[10]) {
+    AtomsDev A = atoms();
+    double* nbp = d_part;
+    int nnb = 0;
+    if (hs.cut == MCG_CUT_SWITCH) {
+        nnb = NB_BLOCKS;
+        if (hs.prec == MCG_PREC_FP64)
+            k_energy_list<PREC_F64><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
+        else
+            k_energy_list<PREC_MIX><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
+    } else {
+        nnb = ntile * (ntile + 1) / 2;
+        if (hs.prec == MCG_PREC_FP64)
+            k_energy_all<PREC_F64><<<nnb, TILE, 0, stream>>>(A, n, pbc, cut, d_fxs, d_fxd, ntile, nbp);
+        else
+            k_energy_all<PREC_MIX><<<nnb, TILE, 0, stream>>>(A, n, pbc, cut, d_fxs, d_fxd, ntile, nbp);
+    }
+    double* p14 = nbp + 2 * (size_t)nnb;
+    int n14b = 0;
+    if (n14 > 0) {
+        n14b = std::min(64, (n14 + 255) / 256);
+        if (hs.prec == MCG_PREC_FP64) k_energy_14<PREC_F64><<<n14b, 256, 0, stream>>>(A, pbc, cut, d_p14, n14, p14);
+        else k_energy_14<PREC_MIX><<<n14b, 256, 0, stream>>>(A, pbc, cut, d_p14, n14, p14);
+    }
+    double* bd = p14 + 2 * (size_t)n14b;
+    BondedDev B = bonded();
+    int nterm = B.nb + B.na + B.nu + B.nd + B.ni;
+    int nbd = 0;
+    if (nterm > 0) {
+        nbd = std::min(64, (nterm + 255) / 256);
+        k_bonded<<<nbd, 256, 0, stream>>>(B, pbc, d_pq, bd);
+    }
+    k_finalize<<<1, 256, 0, stream>>>(nbp, nnb, p14, n14b, bd, nbd, d_out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h_stage, d_out, 10 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    memcpy(ener, h_stage, 10 * sizeof(double));
+    launches += 1 + (n14b > 0) + (nbd > 0) + 1;
+    return MCG_OK;
+}
+
+int SingleEngine::set_coords(const double* x, const double* y, const double* z) {
+    std::vector<double4> pq(n);
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i]))
+            return fail(MCG_EINVAL, "non-finite coordinate at atom " + std::to_string(i));
+        pq[i] = make_double4(x[i], y[i], z[i], hs.q[i]);
+        host_x[i] = x[i]; host_y[i] = y[i]; host_z[i] = z[i];
+    }
+    CK(cudaMemcpyAsync(d_pq, pq.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, stream));
+    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    return MCG_OK;
+}
+
+int SingleEngine::get_coords(double* x, double* y, double* z) {
+    std::vector<double4> pq(n);
+    CK(cudaMemcpyAsync(pq.data(), d_pq, sizeof(double4) * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < n; i++) { x[i] = pq[i].x; y[i] = pq[i].y; z[i] = pq[i].z; }
+    return MCG_OK;
+}
+
+int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const double* ny, const double* nz, double* de) {
+    if (m <= 0 || m > MAX_MOVED) return fail(MCG_EINVAL, "moved-set size must be in [1, 1024]");
+    // sort the moved set (keeps proposal coordinates paired), reject duplicates
+    std::vector<int> ord(m);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return atoms_in[a] < atoms_in[b]; });
+    char* st = (char*)h_stage;
+    int* idx = (int*)st;
+    double* xyz = (double*)(st + 4 * (size_t)MAX_MOVED);
+    int* terms = (int*)(st + 28 * (size_t)MAX_MOVED);
+    for (int k = 0; k < m; k++) {
+        int a = atoms_in[ord[k]];
+        if (a < 0 || a >= n) return fail(MCG_EINVAL, "moved atom index out of range");
+        if (k > 0 && a == idx[k - 1]) return fail(MCG_EINVAL, "duplicate moved atom");
+        double px = nx[ord[k]], py = ny[ord[k]], pz = nz[ord[k]];
+        if (!std::isfinite(px) || !std::isfinite(py) || !std::isfinite(pz)) return fail(MCG_EINVAL, "non-finite proposal");
+        idx[k] = a;
+        xyz[3 * k] = px; xyz[3 * k + 1] = py; xyz[3 * k + 2] = pz;
+    }
+    // bonded terms touching the moved set, each once
+    stamp++;
+    int nt = 0;
+    const size_t tcap = (stage_bytes - 28 * (size_t)MAX_MOVED) / 8;
+    for (int k = 0; k < m; k++) {
+        int a = idx[k];
+        for (int t = term_start[a]; t < term_start[a + 1]; t++) {
+            int kind = term_data[2 * t], ti = term_data[2 * t + 1];
+            size_t gk = (size_t)ti * 5 + kind;
+            if (gk >= term_seen.size()) term_seen.resize(gk + 1, 0);
+            if (term_seen[gk] == stamp) continue;
+            term_seen[gk] = stamp;
+            if ((size_t)nt >= tcap) return fail(MCG_ECAPACITY, "too many bonded terms in one move");
+            terms[2 * nt] = kind; terms[2 * nt + 1] = ti;
+            nt++;
+        }
+    }
+    size_t bytes = 28 * (size_t)MAX_MOVED + (size_t)nt * 8;
+    CK(cudaMemcpyAsync(d_stage, h_stage, bytes, cudaMemcpyHostToDevice, stream));
+    MoveDev mv;
+    mv.m = m;
+    mv.idx = (const int*)d_stage;
+    mv.xyz = (const double*)((char*)d_stage + 4 * (size_t)MAX_MOVED);
+    mv.terms = (const int*)((char*)d_stage + 28 * (size_t)MAX_MOVED);
+    mv.nterms = nt;
+    AtomsDev A = atoms();
+    BondedDev B = bonded();
+    if (hs.prec == MCG_PREC_FP64)
+        k_delta_e<PREC_F64><<<m + 1, 256, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs, d_fxd,
+                                                        d_c14s, d_c14d, B, d_part, d_ticket, d_out);
+    else
+        k_delta_e<PREC_MIX><<<m + 1, 256, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs, d_fxd,
+                                                        d_c14s, d_c14d, B, d_part, d_ticket, d_out);
+    CK(cudaGetLastError());
+    double* hout = (double*)(st + stage_bytes - 64);
+    CK(cudaMemcpyAsync(hout, d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    *de = hout[0];
+    pending_m = m;
+    pending_idx.assign(idx, idx + m);
+    pending_xyz.assign(xyz, xyz + 3 * m);
+    launches += 1;
+    return MCG_OK;
+}
+
+int SingleEngine::commit() {
+    if (pending_m <= 0) return fail(MCG_EINVAL, "no pending proposal to commit");
+    // the staged proposal is still on the device (d_stage) unless a later call overwrote it;
+    // re-upload from the host copy to be safe against interleaved calls
+    char* st = (char*)h_stage;
+    memcpy(st, pending_idx.data(), 4 * pending_m);
+    memcpy(st + 4 * (size_t)MAX_MOVED, pending_xyz.data(), 24 * pending_m);
+    CK(cudaMemcpyAsync(d_stage, h_stage, 28 * (size_t)MAX_MOVED, cudaMemcpyHostToDevice, stream));
+    const int* didx = (const int*)d_stage;
+    const double* dxyz = (const double*)((char*)d_stage + 4 * (size_t)MAX_MOVED);
+    k_commit<0><<<(pending_m + 127) / 128, 128, 0, stream>>>(pending_m, didx, dxyz, d_pq, d_fx, pbc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    for (int k = 0; k < pending_m; k++) {
+        int a = pending_idx[k];
+        host_x[a] = pending_xyz[3 * k]; host_y[a] = pending_xyz[3 * k + 1]; host_z[a] = pending_xyz[3 * k + 2];
+    }
+    pending_m = 0;
+    launches += 1;
+    return MCG_OK;
+}
+
+int SingleEngine::update_lists() {
+    if (hs.cut != MCG_CUT_SWITCH) return MCG_OK;
+    int rc = build_list();
+    launches += 5;
+    return rc;
+}
+
+int SingleEngine::get_pairlist(int* counts, int* entries, int64_t cap_entries, int64_t* total) {
+    if (hs.cut != MCG_CUT_SWITCH) {
+        for (int i = 0; i < n; i++) counts[i] = 0;
+        if (total) *total = 0;
+        return MCG_OK;
+    }
+    std::vector<int> up(n);
+    CK(cudaMemcpyAsync(up.data(), d_nup, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    std::vector<int> rows((size_t)n * cap);
+    CK(cudaMemcpyAsync(rows.data(), d_nbr, sizeof(int) * (size_t)n * cap, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    int64_t t = 0;
+    for (int i = 0; i < n; i++) { counts[i] = up[i]; t += up[i]; }
+    if (total) *total = t;
+    if (entries && cap_entries >= t) {
+        int64_t p = 0;
+        for (int i = 0; i < n; i++) {
+            int* r = rows.data() + (size_t)i * cap;
+            std::sort(r, r + up[i]);
+            memcpy(entries + p, r, sizeof(int) * up[i]);
+            p += up[i];
+        }
+    }
+    return MCG_OK;
+}
+
+}  // namespace mcg

@@ -1,0 +1,76 @@
+// Single-system engine (host object owning the device state of one FField_CUDA).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "dev_types.hpp"
+#include "engine.hpp"
+
+namespace mcg {
+
+struct AtomsDev;
+struct BondedDev;
+
+class SingleEngine {
+public:
+    ~SingleEngine();
+    int init(const HostSystem& hs);
+    int energy(double ener[10]);
+    int update_lists();
+    int set_coords(const double* x, const double* y, const double* z);
+    int get_coords(double* x, double* y, double* z);
+    int delta_e(int m, const int* atoms, const double* nx, const double* ny, const double* nz, double* de);
+    int commit();
+    int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
+
+    HostSystem hs;
+    int n = 0;
+    // host mirror of the coordinates (the device copy is the master once moves are committed)
+    std::vector<double> host_x, host_y, host_z;
+    int64_t launches = 0;
+    int last_max_row = 0;
+    int cap = 0;
+
+private:
+    int build_list();
+    void release();
+    AtomsDev atoms() const;
+    BondedDev bonded() const;
+
+    cudaStream_t stream = nullptr;
+    PbcDev pbc{};
+    CutDev cut{};
+    int n14 = 0, ntile = 0;
+    double4* d_pq = nullptr;
+    double2 *d_es = nullptr, *d_es14 = nullptr;
+    uint4* d_fx = nullptr;
+    float2 *d_esf = nullptr, *d_esf14 = nullptr;
+    uint8_t* d_frozen = nullptr;
+    int *d_xs = nullptr, *d_xd = nullptr, *d_fxs = nullptr, *d_fxd = nullptr;
+    int2* d_p14 = nullptr;
+    int *d_c14s = nullptr, *d_c14d = nullptr;
+    BondT *d_bonds = nullptr, *d_ubs = nullptr;
+    AngleT* d_angles = nullptr;
+    TorsT *d_dihes = nullptr, *d_imprs = nullptr;
+    int *d_nbr = nullptr, *d_nup = nullptr, *d_nlo = nullptr;
+    int *d_cell_of = nullptr, *d_cell_count = nullptr, *d_cell_start = nullptr, *d_cell_fill = nullptr, *d_cell_atoms = nullptr;
+    int ncell_cap = 0;
+    double* d_part = nullptr;
+    size_t part_cap = 0;
+    unsigned* d_ticket = nullptr;
+    double* d_out = nullptr;
+    int* d_maxrow = nullptr;
+    void* h_stage = nullptr;
+    void* d_stage = nullptr;
+    size_t stage_bytes = 0;
+    std::vector<int> term_start, term_data;
+    std::vector<unsigned> term_seen;
+    unsigned stamp = 0;
+    int pending_m = 0;
+    std::vector<int> pending_idx;
+    std::vector<double> pending_xyz;
+};
+
+}  // namespace mcg

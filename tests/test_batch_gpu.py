@@ -1,0 +1,151 @@
+"""Batched chains (the persistent sweep kernel) against the FP64 oracle, through the C ABI.
+
+Tolerances: the FP64 recompute of the device equals the oracle's energy of the same coordinates
+within 1e-10 relative; the running energy (initial FP64 energy plus the accepted mixed-precision
+dE) stays within 1e-6 relative of the FP64 recompute; rigid geometry is kept to 1e-5 A.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from mc_cpp_gb300 import build, native, systems
+from mc_cpp_gb300.engine import BatchChains
+
+pytestmark = pytest.mark.gpu
+KCAL = 418.4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+    orc.build()
+    if native.lib().mcg_device_count() < 1:
+        pytest.fail("no CUDA device visible to libmcgpu.so")
+
+
+def _waters(sizes=(512, 700, 1100, 2300), seed=21, temp=300.0):
+    return [systems.water_box(n, seed=seed + k, temp=temp + 10 * k) for k, n in enumerate(sizes)]
+
+
+def _oracle_nonbonded(s, xyz):
+    t = s.copy()
+    t.set_coords(xyz)
+    o = orc.Oracle(t, moves=False)
+    e = o.energy()
+    return e[3] + e[4]
+
+
+def test_initial_energies_match_oracle():
+    ch = _waters()
+    B = BatchChains(ch, seed=5)
+    e = B.energy_fp64()
+    for k, s in enumerate(ch):
+        want = _oracle_nonbonded(s, s.coords())
+        assert abs(e[k] - want) <= 1e-10 * abs(want), (k, e[k], want)
+    _, _, etot = B.stats()
+    assert np.allclose(etot, e, rtol=0, atol=0)
+    em = B.energy_mixed()
+    assert np.all(np.abs(em - e) <= 1e-6 * np.abs(e))
+
+
+def test_sweeps_keep_running_energy_and_geometry():
+    ch = _waters()
+    B = BatchChains(ch, seed=6)
+    B.sweep(4)
+    t, a, etot = B.stats()
+    assert np.all(t == 4 * (B.sizes // 3))
+    assert np.all(a > 0) and np.all(a < t)
+    e = B.energy_fp64()
+    rel = np.abs(etot - e) / np.abs(e)
+    assert rel.max() <= 1e-6, rel
+    for k, s in enumerate(ch):
+        xyz = B.coords(k)
+        want = _oracle_nonbonded(s, xyz)
+        assert abs(e[k] - want) <= 1e-10 * abs(want)
+        L = s.box[0]
+        o, h1, h2 = xyz[0::3], xyz[1::3], xyz[2::3]
+        for h in (h1, h2):
+            d = h - o
+            d -= L * np.round(d / L)
+            assert np.abs(np.linalg.norm(d, axis=1) - 0.9572).max() < 1e-5
+        d = h1 - h2
+        d -= L * np.round(d / L)
+        hh = 2 * 0.9572 * np.sin(np.radians(104.52 / 2))
+        assert np.abs(np.linalg.norm(d, axis=1) - hh).max() < 1e-5
+
+
+def test_deterministic_for_a_seed():
+    ch = _waters((512, 900))
+    B1 = BatchChains(ch, seed=9)
+    B2 = BatchChains(ch, seed=9)
+    B1.sweep(2)
+    B2.sweep(2)
+    for k in range(2):
+        assert np.array_equal(B1.coords(k), B2.coords(k))
+    assert np.array_equal(B1.stats()[2], B2.stats()[2])
+    B3 = BatchChains(ch, seed=10)
+    B3.sweep(2)
+    assert not np.array_equal(B1.coords(0), B3.coords(0))
+
+
+def test_list_rebuilds_keep_energy_exact():
+    ch = _waters((600, 1500))
+    for s in ch:
+        s.dcut = 0.4          # small skin: the half-skin trigger fires every few moves
+    B = BatchChains(ch, seed=12)
+    B.sweep(3)
+    rb, _ = B.counters()
+    assert rb > 0
+    _, _, etot = B.stats()
+    e = B.energy_fp64()
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+
+
+def test_argon_chains_and_mixed_residue_sizes():
+    ar = [systems.argon_random(n, rho, seed, temp=t) for n, rho, seed, t in ((500, 0.02, 1, 100.0), (900, 0.018, 2, 130.0))]
+    B = BatchChains(ar, seed=3)
+    B.sweep(3)
+    _, a, etot = B.stats()
+    e = B.energy_fp64()
+    assert np.all(a > 0)
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+    for k, s in enumerate(ar):
+        assert abs(e[k] - _oracle_nonbonded(s, B.coords(k))) <= 1e-10 * abs(e[k])
+    # argon and water in one batch take the generic residue-size kernel
+    mix = [ar[0], _waters((512,))[0]]
+    M = BatchChains(mix, seed=4)
+    M.sweep(2)
+    _, _, etot = M.stats()
+    e = M.energy_fp64()
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+
+
+def test_host_buffer_run_roundtrip():
+    ch = _waters((512, 800))
+    B = BatchChains(ch, seed=14)
+    n = B.natoms
+    out = np.zeros((3, n))
+    B.run_host(None, 0, out)
+    xyz0 = np.concatenate([s.coords() for s in ch]).T
+    assert np.abs(out - xyz0).max() < 1e-9
+    a, e = B.run_host(out.copy(), 2, out)
+    ef = B.energy_fp64()
+    assert (np.abs(e - ef) / np.abs(ef)).max() <= 1e-6
+    got = np.concatenate([B.coords(k) for k in range(2)]).T
+    assert np.array_equal(got, out)
+
+
+def test_invalid_batches_rejected():
+    w = systems.water_box(512, seed=3)
+    flexible = w.copy()
+    flexible.angles = flexible.angles[:0]     # H-H no longer excluded: not a rigid residue
+    flexible.angle_type = flexible.angle_type[:0]
+    flexible.angle_k = flexible.angle_k[:0]
+    flexible.angle_theta0 = flexible.angle_theta0[:0]
+    with pytest.raises(native.McgError) as ei:
+        BatchChains([w, flexible])
+    assert ei.value.code == native.MCG_ENOTSUP
+    small = systems.water_box(100, seed=1)    # box < 2 * cutoff
+    with pytest.raises(native.McgError) as ei:
+        BatchChains([small])
+    assert ei.value.code == native.MCG_EINVAL
