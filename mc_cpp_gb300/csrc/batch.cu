@@ -82,13 +82,15 @@ __device__ __forceinline__ double u01d_open0(uint32_t hi, uint32_t lo) {
 struct ChainDev {
     int atom0, res0, nres, apr;
     double L[3], rL[3];
-    double tofix[3];      // 2^64 / L : Angstrom -> master units
+    float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
+    int nc[3];            // cell grid for list builds
+    int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
     float Ls[3];          // L / 2^32 : mirror units -> Angstrom
     double beta;
     float dmax_trn, dmax_rot;
     int ntypes_move;      // 1: TRN only, 2: TRN + ROT
     uint32_t key0, key1;
-    float tab[MAX_APR][MAX_APR][4];   // (qk, e4, ss, 0) per slot pair
+    float tab[MAX_APR][MAX_APR][4];   // (qk, e4, ss, qk_lo) per slot pair; qk + qk_lo = K q_a q_b
 };
 
 struct ChainState {
@@ -115,144 +117,161 @@ __device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
     return (int)((((v + 0x80000000u) >> 8) * (uint64_t)nc) >> 24);
 }
 
-// ---- neighbour list build for one chain by one CTA ------------------------------------------
+// ---- neighbour lists ----------------------------------------------------------------------
 // Residues are binned by their first atom into cells of edge >= (rc + skin + 2 rext)/2 and a
 // 5x5x5 stencil is scanned; boxes with fewer than 5 cells per edge scan every residue.  A residue
 // q enters the list of r when any atom pair is within rc + skin (exact fixed-point displacement).
-// s_cell: MAX_CELLS+1 ints of shared memory; g_order, g_cell: nres ints of global scratch.
-template <int APR>
-__device__ void chain_build(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ F, uint4* FB,
-                            uint16_t* LST, int* NL, int* s_cell, int* g_order, int* g_cell, int* err_out) {
-    const int apr = APR ? APR : C.apr;
-    const int nres = C.nres;
+// Lists are rebuilt for every chain before every sweep by a grid-wide kernel (k_batch_bin +
+// k_batch_lists); inside a sweep, a chain whose atom has moved more than half the skin since the
+// build rebuilds its own lists with its CTA (chain_rebuild) before the next move.
+
+// Block-level binning of chain C: copies the build positions and, when the chain uses cells,
+// fills starts[0..ncell] (shared or global) and g_order (residues sorted by cell, then index).
+__device__ void chain_bin(const ChainDev& C, const uint4* __restrict__ F, uint4* FB, int* starts, int* g_order,
+                          int* g_cell) {
+    const int apr = C.apr, nres = C.nres;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     const uint4* Fc = F + C.atom0;
     for (int i = tid; i < nres * apr; i += T) FB[C.atom0 + i] = Fc[i];
-    int nc[3];
-    bool cells = true;
-    for (int k = 0; k < 3; k++) {
-        nc[k] = (int)floor(C.L[k] / G.cellmin);
-        if (nc[k] < 5) cells = false;
-    }
-    if (cells && nc[0] * nc[1] * nc[2] > MAX_CELLS) cells = false;
-    const int ncell = cells ? nc[0] * nc[1] * nc[2] : 1;
+    if (!C.use_cells) { __syncthreads(); return; }
+    const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
+    for (int c = tid; c <= ncell; c += T) starts[c] = 0;
     __syncthreads();
-    if (cells) {
-        for (int c = tid; c <= ncell; c += T) s_cell[c] = 0;
-        __syncthreads();
-        for (int r = tid; r < nres; r += T) {
-            uint4 p = Fc[r * apr];
-            int c = (cell_coord(p.z, nc[2]) * nc[1] + cell_coord(p.y, nc[1])) * nc[0] + cell_coord(p.x, nc[0]);
-            g_cell[r] = c;
-            atomicAdd(&s_cell[c + 1], 1);
-        }
-        __syncthreads();
-        if (tid == 0)  // inclusive scan of counts shifted by one = start offsets
-            for (int c = 1; c <= ncell; c++) s_cell[c] += s_cell[c - 1];
-        __syncthreads();
-        // s_cell[c] doubles as the fill cursor of cell c: place with atomics, then sort each cell
-        // (warp per cell) so the list order, and with it the dE summation order, is deterministic
-        for (int r = tid; r < nres; r += T) {
-            int c = g_cell[r];
-            int slot = atomicAdd(&s_cell[c], 1);   // s_cell[c] advances to the end of cell c
-            g_order[slot] = r;
-        }
-        __syncthreads();
-        // s_cell[c] now holds end(c) = start(c+1); restore starts by shifting
-        if (tid == 0) {
-            for (int c = ncell; c >= 1; c--) s_cell[c] = s_cell[c - 1];
-            s_cell[0] = 0;
-        }
-        __syncthreads();
-        for (int c = warp; c < ncell; c += nw) {
-            const int b = s_cell[c], e = s_cell[c + 1], m = e - b;
-            if (m <= 1) continue;
-            if (m <= 32) {
-                int v = lane < m ? g_order[b + lane] : 0x7fffffff;
-                for (int k = 2; k <= 32; k <<= 1)
-                    for (int j = k >> 1; j > 0; j >>= 1) {
-                        int o = __shfl_xor_sync(0xffffffffu, v, j);
-                        bool up = (lane & k) == 0, lower = (lane & j) == 0;
-                        v = (lower == up) ? min(v, o) : max(v, o);
-                    }
-                if (lane < m) g_order[b + lane] = v;
-            } else if (lane == 0) {
-                for (int i = b + 1; i < e; i++) {
-                    int v = g_order[i], k = i - 1;
-                    while (k >= b && g_order[k] > v) { g_order[k + 1] = g_order[k]; k--; }
-                    g_order[k + 1] = v;
-                }
-            }
-        }
-        __syncthreads();
+    for (int r = tid; r < nres; r += T) {
+        const uint4 p = Fc[r * apr];
+        const int c = (cell_coord(p.z, C.nc[2]) * C.nc[1] + cell_coord(p.y, C.nc[1])) * C.nc[0] + cell_coord(p.x, C.nc[0]);
+        g_cell[r] = c;
+        atomicAdd(&starts[c + 1], 1);
     }
-    for (int r = warp; r < nres; r += nw) {
-        uint4 pa[APR ? APR : MAX_APR];
-        for (int k = 0; k < apr; k++) pa[k] = Fc[r * apr + k];
-        uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
-        int cnt = 0;
-        auto consider = [&](int q, bool valid) {
-            bool ok = false;
-            if (valid && q != r) {
-                uint4 pq = Fc[q * apr];
-                float dx = fdelta(pa[0].x, pq.x, C.Ls[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2]);
-                if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
-                    for (int b = 0; b < apr && !ok; b++) {
-                        uint4 pb = Fc[q * apr + b];
-                        for (int k = 0; k < apr; k++) {
-                            float ex = fdelta(pa[k].x, pb.x, C.Ls[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1]), ez = fdelta(pa[k].z, pb.z, C.Ls[2]);
-                            if (ex * ex + ey * ey + ez * ez <= G.rlist2) { ok = true; break; }
-                        }
-                    }
+    __syncthreads();
+    if (tid == 0)
+        for (int c = 1; c <= ncell; c++) starts[c] += starts[c - 1];
+    __syncthreads();
+    // starts[c] doubles as the fill cursor of cell c; restored afterwards
+    for (int r = tid; r < nres; r += T) g_order[atomicAdd(&starts[g_cell[r]], 1)] = r;
+    __syncthreads();
+    if (tid == 0) {
+        for (int c = ncell; c >= 1; c--) starts[c] = starts[c - 1];
+        starts[0] = 0;
+    }
+    __syncthreads();
+    // sort each cell so the list order (and the dE summation order) is deterministic
+    for (int c = warp; c < ncell; c += nw) {
+        const int b = starts[c], e = starts[c + 1], m = e - b;
+        if (m <= 1) continue;
+        if (m <= 32) {
+            int v = lane < m ? g_order[b + lane] : 0x7fffffff;
+            for (int k = 2; k <= 32; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const int o = __shfl_xor_sync(0xffffffffu, v, j);
+                    const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+                    v = (lower == up) ? min(v, o) : max(v, o);
                 }
+            if (lane < m) g_order[b + lane] = v;
+        } else if (lane == 0) {
+            for (int i = b + 1; i < e; i++) {
+                int v = g_order[i], k = i - 1;
+                while (k >= b && g_order[k] > v) { g_order[k + 1] = g_order[k]; k--; }
+                g_order[k + 1] = v;
             }
-            unsigned bal = __ballot_sync(0xffffffffu, ok);
-            if (ok) {
-                int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-                if (pos < G.cap) row[pos] = (uint16_t)q;
-            }
-            cnt += __popc(bal);
-        };
-        if (cells) {
-            const int cx = cell_coord(pa[0].x, nc[0]), cy = cell_coord(pa[0].y, nc[1]), cz = cell_coord(pa[0].z, nc[2]);
-            for (int dz = -2; dz <= 2; dz++)
-                for (int dy = -2; dy <= 2; dy++)
-                    for (int dx = -2; dx <= 2; dx++) {
-                        int x = (cx + dx + nc[0]) % nc[0], y = (cy + dy + nc[1]) % nc[1], z = (cz + dz + nc[2]) % nc[2];
-                        int cc = (z * nc[1] + y) * nc[0] + x;
-                        int b = s_cell[cc], e = s_cell[cc + 1];
-                        for (int base = b; base < e; base += 32) {
-                            int t = base + lane;
-                            consider(t < e ? g_order[t] : 0, t < e);
-                        }
-                    }
-        } else {
-            for (int base = 0; base < nres; base += 32) {
-                int q = base + lane;
-                consider(q < nres ? q : 0, q < nres);
-            }
-        }
-        if (lane == 0) {
-            NL[C.res0 + r] = min(cnt, G.cap);
-            if (cnt > G.cap) atomicExch(err_out, MCG_ECAPACITY);
         }
     }
     __syncthreads();
 }
 
+// Warp-level list of residue r (all 32 lanes of the calling warp).
 template <int APR>
-__global__ void k_batch_build(const ChainDev* __restrict__ chains, BatchGeom G, const uint4* __restrict__ F, uint4* FB,
-                              uint16_t* LST, int* NL, int* g_order, int* g_cell, ChainState* state, int nchains) {
-    __shared__ int s_cell[MAX_CELLS + 1];
-    __shared__ int s_err;
+__device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int r,
+                             const int* __restrict__ starts, const int* __restrict__ g_order, uint16_t* LST, int* NL,
+                             int* err_out) {
+    const int apr = APR ? APR : C.apr;
+    const int lane = threadIdx.x & 31;
+    uint4 pa[APR ? APR : MAX_APR];
+    for (int k = 0; k < apr; k++) pa[k] = Fc[r * apr + k];
+    uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
+    int cnt = 0;
+    auto consider = [&](int q, bool valid) {
+        bool ok = false;
+        if (valid && q != r) {
+            const uint4 pq = Fc[q * apr];
+            const float dx = fdelta(pa[0].x, pq.x, C.Ls[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2]);
+            if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
+                for (int b = 0; b < apr && !ok; b++) {
+                    const uint4 pb = Fc[q * apr + b];
+                    for (int k = 0; k < apr; k++) {
+                        const float ex = fdelta(pa[k].x, pb.x, C.Ls[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1]),
+                                    ez = fdelta(pa[k].z, pb.z, C.Ls[2]);
+                        if (ex * ex + ey * ey + ez * ez <= G.rlist2) { ok = true; break; }
+                    }
+                }
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+            if (pos < G.cap) row[pos] = (uint16_t)q;
+        }
+        cnt += __popc(bal);
+    };
+    if (C.use_cells) {
+        const int cx = cell_coord(pa[0].x, C.nc[0]), cy = cell_coord(pa[0].y, C.nc[1]), cz = cell_coord(pa[0].z, C.nc[2]);
+        for (int dz = -2; dz <= 2; dz++)
+            for (int dy = -2; dy <= 2; dy++)
+                for (int dx = -2; dx <= 2; dx++) {
+                    const int x = (cx + dx + C.nc[0]) % C.nc[0], y = (cy + dy + C.nc[1]) % C.nc[1], z = (cz + dz + C.nc[2]) % C.nc[2];
+                    const int cc = (z * C.nc[1] + y) * C.nc[0] + x;
+                    const int b = starts[cc], e = starts[cc + 1];
+                    for (int base = b; base < e; base += 32) {
+                        const int t = base + lane;
+                        consider(t < e ? g_order[t] : 0, t < e);
+                    }
+                }
+    } else {
+        for (int base = 0; base < C.nres; base += 32) {
+            const int q = base + lane;
+            consider(q < C.nres ? q : 0, q < C.nres);
+        }
+    }
+    if (lane == 0) {
+        NL[C.res0 + r] = min(cnt, G.cap);
+        if (cnt > G.cap) atomicExch(err_out, MCG_ECAPACITY);
+    }
+}
+
+// Per-chain binning before a sweep: one CTA per chain, cell starts to global memory.
+__global__ void k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __restrict__ F, uint4* FB, int* g_starts,
+                            int* g_order, int* g_cell, int nchains) {
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
-    if (APR && C.apr != APR) return;
-    if (threadIdx.x == 0) s_err = 0;
+    chain_bin(C, F, FB, g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0, g_cell + C.res0);
+}
+
+// Lists of every residue of every chain: one warp per residue over the whole GPU.
+template <int APR>
+__global__ void __launch_bounds__(256) k_batch_lists(const ChainDev* __restrict__ chains, BatchGeom G,
+                                                     const uint4* __restrict__ F, const int* __restrict__ res_chain,
+                                                     const int* __restrict__ g_starts, const int* __restrict__ g_order,
+                                                     uint16_t* LST, int* NL, ChainState* state, int64_t nres_total) {
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
+        const int c = res_chain[gr];
+        const ChainDev& C = chains[c];
+        if (APR && C.apr != APR) continue;
+        residue_list<APR>(C, G, F + C.atom0, (int)(gr - C.res0), g_starts + (size_t)c * (MAX_CELLS + 1),
+                          g_order + C.res0, LST, NL, &state[c].err);
+    }
+}
+
+// In-sweep rebuild of one chain by its own CTA (shared-memory cell starts).
+template <int APR>
+__device__ void chain_rebuild(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ F, uint4* FB,
+                              uint16_t* LST, int* NL, int* s_starts, int* g_order, int* g_cell, int* err_out) {
+    chain_bin(C, F, FB, s_starts, g_order, g_cell);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    (void)lane;
+    for (int r = warp; r < C.nres; r += nw) residue_list<APR>(C, G, F + C.atom0, r, s_starts, g_order, LST, NL, err_out);
     __syncthreads();
-    chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
-    if (threadIdx.x == 0 && s_err) state[c].err = s_err;
 }
 
 // ---- the sweep ------------------------------------------------------------------------------
@@ -261,9 +280,20 @@ struct Proposal {
     unsigned long long mn[MAX_APR][3];   // new master coordinates
     float m[MAX_APR][3];                 // fn - fo in Angstrom (exact mirror difference)
     int res;
-    double thr;                          // -ln(alpha) / beta: accept when dE < thr
+    float lna;                           // -ln(alpha), FP32 estimate
+    double alpha;                        // alpha in (0, 1]
     int rebuild;
 };
+
+// Master-unit increment for a displacement d (Angstrom): d * 2^64 / L as a 64-bit integer, formed
+// in FP32 + integer arithmetic (v = d * 2^32 / L; integer part -> high word, fraction -> low word).
+__device__ __forceinline__ unsigned long long master_step(float d, float tofix32) {
+    const float v = d * tofix32;
+    const float fl = floorf(v);
+    const int hi = __float2int_rn(fl);
+    const uint32_t lo = __float2uint_rn((v - fl) * 4294967296.0f);   // (v - fl) < 1 exactly
+    return ((unsigned long long)(long long)hi << 32) + lo;
+}
 
 template <int APR>
 __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
@@ -271,17 +301,19 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                                                      int* g_cell, ChainState* state, const int* __restrict__ order,
                                                      int nchains) {
     __shared__ Proposal P;
-    __shared__ double s_red[8];
+    __shared__ float2 s_red[8];
     __shared__ int s_cell[MAX_CELLS + 1];
     __shared__ int s_err;
-    __shared__ float s_tab[MAX_APR][MAX_APR][4];
+    __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const int c = order[blockIdx.x];
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     if (APR && C.apr != APR) return;
     const int apr = APR ? APR : C.apr;
-    for (int k = tid; k < MAX_APR * MAX_APR * 4; k += blockDim.x) (&s_tab[0][0][0])[k] = (&C.tab[0][0][0])[k];
+    for (int k = tid; k < MAX_APR * MAX_APR; k += blockDim.x)
+        s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
+                                                      C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
     cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
@@ -295,10 +327,10 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
     for (int mv = 0; mv < nmoves; mv++) {
         const unsigned long long cnt = S.moves + (unsigned long long)mv;
         if (warp == 0) {
-            // ---- proposal: lanes 0..apr-1 own one atom each
+            // ---- proposal: lanes 0..apr-1 own one atom each; FP32 and integer work only
             __syncwarp();
-            U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
-            U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
+            const U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
+            const U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
             const bool rot = C.ntypes_move == 2 && (r0.x & 1u);
             const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
             const int piv = (int)(((uint64_t)r0.z * (uint64_t)apr) >> 32);
@@ -316,21 +348,21 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                     const float rad = C.dmax_trn * cbrtf(u01f(r1.y));
                     dx = rad * ux; dy = rad * uy; dz = rad * uz;
                 } else {
-                    // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u
+                    // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
+                    // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
                     float sh, ch;
                     sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
                     const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
                     const uint4 fp = Fc[res * apr + piv];
                     const float ox = fdelta(fp.x, fo.x, C.Ls[0]), oy = fdelta(fp.y, fo.y, C.Ls[1]), oz = fdelta(fp.z, fo.z, C.Ls[2]);
-                    // rotated offset minus offset: 2 q_w (q_v x o) + 2 q_v x (q_v x o)
                     const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
                     dx = qw * tx + (qy * tz - qz * ty);
                     dy = qw * ty + (qz * tx - qx * tz);
                     dz = qw * tz + (qx * ty - qy * tx);
                 }
-                const unsigned long long nx = mo.x + (unsigned long long)__double2ll_rn((double)dx * C.tofix[0]);
-                const unsigned long long ny = mo.y + (unsigned long long)__double2ll_rn((double)dy * C.tofix[1]);
-                const unsigned long long nz = mo.z + (unsigned long long)__double2ll_rn((double)dz * C.tofix[2]);
+                const unsigned long long nx = mo.x + master_step(dx, C.tofix32[0]);
+                const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
+                const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
                 const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
                 P.fo[lane] = fo;
                 P.fn[lane] = fn;
@@ -339,15 +371,16 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                 P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1]);
                 P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2]);
             }
-            if (lane == 0) P.res = res;
-        } else if (warp == 1 && lane == 0) {
-            // acceptance threshold in FP64 while warp 0 builds the proposal
-            U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
-            P.thr = -log(u01d_open0(r1.z, r1.w)) / C.beta;
+            if (lane == 0) {
+                P.res = res;
+                const double alpha = u01d_open0(r1.z, r1.w);
+                P.alpha = alpha;
+                P.lna = -__logf((float)alpha);
+            }
         }
         __syncthreads();
         if (P.rebuild) {  // requested by the previous accepted move
-            chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
             if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
             __syncthreads();
         }
@@ -371,7 +404,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
 #pragma unroll
                 for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
                     if (k >= apr) break;
-                    const float4 t = *reinterpret_cast<const float4*>(&s_tab[fo[k].w][pb.w][0]);
+                    const float4 t = s_tab[fo[k].w][pb.w];
                     // d_old = b - a_old, d_new = b - a_new = d_old - m
                     acc += mixed_pair_delta(fdelta(fo[k].x, pb.x, C.Ls[0]), fdelta(fo[k].y, pb.y, C.Ls[1]),
                                             fdelta(fo[k].z, pb.z, C.Ls[2]), m[k][0], m[k][1], m[k][2], t.x, t.y, t.z, cut, np);
@@ -379,13 +412,45 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
             }
         }
         npairs += np;
-        const double v = warp_sum((double)acc);
-        if (lane == 0) s_red[warp] = v;
+        // float-float warp reduction (TwoSum), then across warps by warp 0
+        float hi = acc, lo = 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            float s, e;
+            two_sum(hi, oh, s, e);
+            hi = s;
+            lo = lo + ol + e;
+        }
+        if (lane == 0) s_red[warp] = make_float2(hi, lo);
         __syncthreads();
         if (warp == 0) {
+            float2 v = lane < nw ? s_red[lane] : make_float2(0.f, 0.f);
+            hi = v.x; lo = v.y;
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+                float s, e;
+                two_sum(hi, oh, s, e);
+                hi = s;
+                lo = lo + ol + e;
+            }
+            // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in FP32
+            // when the margin is clear and in FP64 otherwise
+            bool accept;
             double de = 0.0;
-            for (int w = 0; w < nw; w++) de += s_red[w];
-            const bool accept = (de <= 2.220446049250313e-16) || (de < P.thr);
+            if (lane == 0) {
+                de = (double)hi + (double)lo;
+                if (de <= 2.220446049250313e-16) accept = true;
+                else {
+                    const double t = C.beta * de;
+                    const float tf = (float)t;
+                    if (tf < P.lna - 1e-4f * fmaxf(1.0f, P.lna)) accept = true;
+                    else if (tf > P.lna + 1e-4f * fmaxf(1.0f, P.lna)) accept = false;
+                    else accept = P.alpha < exp(-t);
+                }
+            }
+            accept = __shfl_sync(0xffffffffu, accept, 0);
             bool far = false;
             if (accept && lane < apr) {
                 const int a = res * apr + lane;
@@ -406,7 +471,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
     }
     __syncthreads();
     if (P.rebuild) {
-        chain_build<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+        chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
         if (tid == 0) S.rebuilds++;
     }
     {
@@ -477,14 +542,14 @@ template <int APR>
 __global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __restrict__ chains, BatchGeom G,
                                                            const uint4* __restrict__ F, const uint16_t* __restrict__ LST,
                                                            const int* __restrict__ NL, ChainState* state, int nchains) {
-    __shared__ float s_tab[MAX_APR][MAX_APR][4];
+    __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
     __shared__ double s_red[8];
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     if (APR && C.apr != APR) return;
     const int apr = APR ? APR : C.apr;
-    for (int k = threadIdx.x; k < MAX_APR * MAX_APR * 4; k += blockDim.x) (&s_tab[0][0][0])[k] = (&C.tab[0][0][0])[k];
+    for (int k = threadIdx.x; k < MAX_APR * MAX_APR; k += blockDim.x) s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1], C.tab[k / MAX_APR][k % MAX_APR][2], 0.f);
     __syncthreads();
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
@@ -504,9 +569,9 @@ __global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __res
                     const float dx = fdelta(pa.x, pb.x, C.Ls[0]), dy = fdelta(pa.y, pb.y, C.Ls[1]), dz = fdelta(pa.z, pb.z, C.Ls[2]);
                     const float u = dx * dx + dy * dy + dz * dz;
                     if (u > cut.c2f) continue;
-                    const float4 t = *reinterpret_cast<const float4*>(&s_tab[pa.w][pb.w][0]);
+                    const float4 t = s_tab[pa.w][pb.w];
                     float el, vd;
-                    mixed_pair(u, t.x, t.y, t.z, true, cut, el, vd);
+                    mixed_pair(u, t.x, t.w, t.y, t.z, true, cut, el, vd);
                     acc.add(el + vd);
                 }
             }
@@ -587,7 +652,7 @@ struct mcg_batch {
     ulonglong4* d_M = nullptr;
     uint4 *d_F = nullptr, *d_FB = nullptr;
     uint16_t* d_LST = nullptr;
-    int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr;
+    int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr, *d_gstarts = nullptr, *d_res_chain = nullptr;
     double* d_prm = nullptr;
     int* d_tile_chain = nullptr;
     int* d_tile_first = nullptr;
@@ -602,23 +667,27 @@ struct mcg_batch {
     ~mcg_batch() {
         if (graph) cudaGraphExecDestroy(graph);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
-                     d_tile_first, d_part, d_xyz};
+                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
     }
-    int launch_build() {
+    // list rebuild of every chain: per-chain binning, then one warp per residue over the GPU
+    int launch_build(cudaStream_t st) {
+        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, nchains);
+        const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_build<3><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+            k_batch_lists<3><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
         else if (apr_all == 1)
-            k_batch_build<1><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+            k_batch_lists<1><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
         else
-            k_batch_build<0><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, nchains);
+            k_batch_lists<0><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
         BK(cudaGetLastError());
-        launches++;
+        launches += 2;
         return MCG_OK;
     }
+    int launch_build() { return launch_build(stream); }
     int launch_energy_list() {
         if (apr_all == 3)
             k_batch_energy_list<3><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
@@ -633,7 +702,8 @@ struct mcg_batch {
     int ensure_graph() {
         if (graph) return MCG_OK;
         BK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        int r = launch_sweep(stream);
+        int r = launch_build(stream);
+        if (!r) r = launch_sweep(stream);
         cudaGraph_t g = nullptr;
         cudaError_t ee = cudaStreamEndCapture(stream, &g);
         if (r) { if (g) cudaGraphDestroy(g); return r; }
@@ -678,7 +748,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     std::vector<ulonglong4> M;
     std::vector<uint4> F;
     std::vector<double> prm;
-    double rext = 0.0;
+    double rext = 0.0;       // largest distance from a residue's first atom to its other atoms
+    double span_max = 0.0;   // largest intra-residue distance
     int apr_all = -1;
     int64_t atom0 = 0, res0 = 0;
     B->chains.resize(nchains);
@@ -717,7 +788,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         C.atom0 = (int)atom0; C.res0 = (int)res0; C.nres = nres; C.apr = apr;
         for (int k = 0; k < 3; k++) {
             C.L[k] = hs.L[k]; C.rL[k] = hs.rL[k];
-            C.tofix[k] = TWO64 / hs.L[k];
+            C.tofix32[k] = (float)(4294967296.0 / hs.L[k]);
             C.Ls[k] = (float)(hs.L[k] / 4294967296.0);
         }
         C.beta = 1.0 / ((RBOLTZUI / KCALTOIU) * hs.temp);
@@ -730,7 +801,9 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         const double K = CHGCHARMM * KCALTOIU;
         for (int a = 0; a < apr; a++)
             for (int b = 0; b < apr; b++) {
-                C.tab[a][b][0] = (float)(K * hs.q[a] * hs.q[b]);
+                const double qk = K * hs.q[a] * hs.q[b];
+                C.tab[a][b][0] = (float)qk;
+                C.tab[a][b][3] = (float)(qk - (double)(float)qk);
                 C.tab[a][b][1] = (float)(4.0 * hs.eps[a] * hs.eps[b]);
                 double s = hs.sig[a] + hs.sig[b];
                 C.tab[a][b][2] = (float)(s * s);
@@ -743,11 +816,15 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             prm.push_back(hs.q[i]); prm.push_back(hs.eps[i]); prm.push_back(hs.sig[i]);
         }
         for (int r = 0; r < nres; r++)
-            for (int k = 1; k < apr; k++) {
-                double e[3] = {hs.x[r * apr + k] - hs.x[r * apr], hs.y[r * apr + k] - hs.y[r * apr], hs.z[r * apr + k] - hs.z[r * apr]};
-                for (int t = 0; t < 3; t++) e[t] -= hs.L[t] * std::nearbyint(e[t] * hs.rL[t]);
-                rext = std::max(rext, std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
-            }
+            for (int k = 0; k < apr; k++)
+                for (int k2 = k + 1; k2 < apr; k2++) {
+                    const int i = r * apr + k, j = r * apr + k2;
+                    double e[3] = {hs.x[j] - hs.x[i], hs.y[j] - hs.y[i], hs.z[j] - hs.z[i]};
+                    for (int t = 0; t < 3; t++) e[t] -= hs.L[t] * std::nearbyint(e[t] * hs.rL[t]);
+                    const double d = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+                    span_max = std::max(span_max, d);
+                    if (k == 0) rext = std::max(rext, d);
+                }
         atom0 += hs.n;
         res0 += nres;
         if (atom0 > (int64_t)2000000000) return fail(MCG_EINVAL, "too many atoms");
@@ -764,9 +841,19 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     G.rcent2 = (float)((rlist + 2 * rext) * (rlist + 2 * rext));
     G.half_skin2 = (float)(0.25 * skin * skin);
     G.cellmin = (float)(0.5 * (rlist + 2 * rext) + 1e-3);
-    for (auto& C : B->chains)
-        for (int k = 0; k < 3; k++)
-            if (rc > 0.5 * C.L[k]) return fail(MCG_EINVAL, "cutoff exceeds half a chain's box");
+    // dE forms the new displacement as d_old - m; that is the minimum image for every pair inside
+    // the cutoff only while rc + |m| <= L/2 (m: the largest move of one atom)
+    const double span = span_max + 0.01;   // rigid residues keep their intra-residue distances
+    const double mmax = std::max((double)opts->dmax_trn, 2.0 * span * std::sin(0.5 * opts->dmax_rot * PI / 180.0)) + 1e-6;
+    for (auto& C : B->chains) {
+        for (int k = 0; k < 3; k++) {
+            if (rc + mmax > 0.5 * C.L[k])
+                return fail(MCG_EINVAL, "cutoff plus the largest move exceeds half a chain's box");
+            C.nc[k] = (int)std::floor(C.L[k] / G.cellmin);
+        }
+        C.use_cells = (C.nc[0] >= 5 && C.nc[1] >= 5 && C.nc[2] >= 5 && C.nc[0] * C.nc[1] * C.nc[2] <= MAX_CELLS) ? 1 : 0;
+        if (!C.use_cells) C.nc[0] = C.nc[1] = C.nc[2] = 1;
+    }
     if (opts->list_capacity > 0) G.cap = opts->list_capacity;
     else {
         double dens = 0;
@@ -788,8 +875,15 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) || (r = balloc(&B->d_order, nchains)) ||
         (r = balloc(&B->d_M, atom0)) || (r = balloc(&B->d_F, atom0)) || (r = balloc(&B->d_FB, atom0)) ||
         (r = balloc(&B->d_LST, (size_t)res0 * G.cap)) || (r = balloc(&B->d_NL, res0)) || (r = balloc(&B->d_gorder, res0)) ||
-        (r = balloc(&B->d_gcell, res0)) || (r = balloc(&B->d_prm, prm.size())))
+        (r = balloc(&B->d_gcell, res0)) || (r = balloc(&B->d_prm, prm.size())) ||
+        (r = balloc(&B->d_gstarts, (size_t)nchains * (MAX_CELLS + 1))) || (r = balloc(&B->d_res_chain, res0)))
         return r;
+    {
+        std::vector<int> rcn(res0);
+        for (int c = 0; c < nchains; c++)
+            for (int k = 0; k < B->chains[c].nres; k++) rcn[B->chains[c].res0 + k] = c;
+        BK(cudaMemcpy(B->d_res_chain, rcn.data(), sizeof(int) * res0, cudaMemcpyHostToDevice));
+    }
     BK(cudaMemcpyAsync(B->d_chains, B->chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_order, B->order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4) * atom0, cudaMemcpyHostToDevice, B->stream));
@@ -836,7 +930,7 @@ int mcg_batch_sweep(mcg_batch* b, int nsweeps) {
     int r = b->ensure_graph();
     if (r) return r;
     for (int s = 0; s < nsweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
-    b->launches += nsweeps;
+    b->launches += 3 * (int64_t)nsweeps;
     return MCG_OK;
 }
 
@@ -851,7 +945,7 @@ int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms) {
     BK(cudaEventRecord(b->ev1, b->stream));
     BK(cudaEventSynchronize(b->ev1));
     BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
-    b->launches += nsweeps;
+    b->launches += 3 * (int64_t)nsweeps;
     return MCG_OK;
 }
 

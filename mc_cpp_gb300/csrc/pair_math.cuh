@@ -81,11 +81,14 @@ __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float Lscal
     return __int2float_rn(d) * Lscale;
 }
 
-// FP32 switched LJ + Coulomb on r^2 (unscaled el, vd as in ref64_pair).  qq = qi qj,
-// ee = eps_i eps_j, ss = (sig_i + sig_j)^2.
-__device__ __forceinline__ void mixed_pair(float r2, float qq, float ee, float ss, bool do_switch, const CutDev& c,
-                                           float& el, float& vd) {
+// FP32 switched LJ + Coulomb on r^2 (unscaled el, vd as in ref64_pair).  The charge product is
+// a float-float pair (qq + qq_lo): per-type products rounded to float are systematic biases that
+// the cancellation between positive and negative Coulomb terms would amplify to ~1e-6 of the
+// total.  ee = eps_i eps_j, ss = (sig_i + sig_j)^2.
+__device__ __forceinline__ void mixed_pair(float r2, float qq, float qq_lo, float ee, float ss, bool do_switch,
+                                           const CutDev& c, float& el, float& vd) {
     float rinv = rsqrtf(r2);
+    rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step on the hardware estimate
     float x2 = ss * (rinv * rinv);
     float x6 = x2 * x2 * x2;
     float f = 1.0f;
@@ -93,8 +96,21 @@ __device__ __forceinline__ void mixed_pair(float r2, float qq, float ee, float s
         float s1 = c.c2f - r2;
         f = s1 * s1 * (c.c2f + 2.0f * r2 - 3.0f * c.n2f) * c.sw2f;
     }
-    el = qq * rinv * f;
+    el = fmaf(qq, rinv, qq_lo * rinv) * f;
     vd = ee * (x6 * x6 - x6) * f;
+}
+
+// float-float product of two float-float values (hi parts exact by FMA, cross terms rounded)
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+    ph = ah * bh;
+    pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
+}
+
+// TwoSum: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
 }
 
 // Error-free FP32 accumulation (Kahan-Babuska / Neumaier): sum + comp carries ~48 bits.

@@ -245,6 +245,7 @@ struct AtomsDev {
     const uint4* fx;
     const float2* esf;
     const float2* esf14;
+    const float2* qf;     // charge as float-float (hi, lo)
     float Ls[3];          // box / 2^32 (mixed displacement scale)
 };
 
@@ -274,8 +275,11 @@ __device__ __forceinline__ void pair_energy(const AtomsDev& A, const PbcDev& pbc
         float2 a = fourteen ? A.esf14[i] : A.esf[i];
         float2 b = fourteen ? A.esf14[j] : A.esf[j];
         float s = a.y + b.y;
+        float2 qa = A.qf[i], qb = A.qf[j];
+        float qh, ql;
+        ff_mul(qa.x, qa.y, qb.x, qb.y, qh, ql);
         float e1, v1;
-        mixed_pair(r2, __int_as_float(fi.w) * __int_as_float(fj.w), a.x * b.x, s * s, apply_cut, cut, e1, v1);
+        mixed_pair(r2, qh, ql, a.x * b.x, s * s, apply_cut, cut, e1, v1);
         el = e1; vd = v1;
     }
 }
@@ -577,17 +581,8 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         const double4 an = make_double4(s_xyz[3 * ka], s_xyz[3 * ka + 1], s_xyz[3 * ka + 2], ao.w);
         const uint4 fo = P == PREC_MIX ? A.fx[a] : make_uint4(0, 0, 0, 0);
         const uint4 fn = P == PREC_MIX ? s_fx[ka] : make_uint4(0, 0, 0, 0);
-        // mixed: displacement of the moved atom as the fixed-point mirror sees it (exact)
-        float ma[3] = {0.f, 0.f, 0.f};
         CutDev cutx = cut;   // full mode: no cutoff and no switch
         if (!sw) { cutx.c2f = 3.0e38f; cutx.n2f = 3.0e38f; }
-        if (P == PREC_MIX) {
-            if (pbc.type != 0) {
-                ma[0] = fixed_delta(fo.x, fn.x, A.Ls[0]); ma[1] = fixed_delta(fo.y, fn.y, A.Ls[1]); ma[2] = fixed_delta(fo.z, fn.z, A.Ls[2]);
-            } else {
-                ma[0] = (float)(an.x - ao.x); ma[1] = (float)(an.y - ao.y); ma[2] = (float)(an.z - ao.z);
-            }
-        }
         auto visit = [&](int j, bool fourteen, bool apply_cut) {
             int sj = slot(j);
             if (sj >= 0 && j < a) return;       // counted by the lower index's block
@@ -610,19 +605,22 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
                 } else {
                     d[0] = (float)(jo.x - ao.x); d[1] = (float)(jo.y - ao.y); d[2] = (float)(jo.z - ao.z);
                 }
-                if (sj >= 0) {   // both atoms moved: m = d_old - d_new
-                    float dn[3];
-                    if (pbc.type != 0) {
-                        dn[0] = fixed_delta(fn.x, gjn.x, A.Ls[0]); dn[1] = fixed_delta(fn.y, gjn.y, A.Ls[1]); dn[2] = fixed_delta(fn.z, gjn.z, A.Ls[2]);
-                    } else {
-                        dn[0] = (float)(jn.x - an.x); dn[1] = (float)(jn.y - an.y); dn[2] = (float)(jn.z - an.z);
-                    }
-                    m[0] = d[0] - dn[0]; m[1] = d[1] - dn[1]; m[2] = d[2] - dn[2];
-                } else { m[0] = ma[0]; m[1] = ma[1]; m[2] = ma[2]; }
+                // m = d_old - d_new with both displacements taken by minimum image: when the move
+                // carries a pair across half the box (possible without a cutoff) the image changes
+                float dn[3];
+                if (pbc.type != 0) {
+                    dn[0] = fixed_delta(fn.x, gjn.x, A.Ls[0]); dn[1] = fixed_delta(fn.y, gjn.y, A.Ls[1]); dn[2] = fixed_delta(fn.z, gjn.z, A.Ls[2]);
+                } else {
+                    dn[0] = (float)(jn.x - an.x); dn[1] = (float)(jn.y - an.y); dn[2] = (float)(jn.z - an.z);
+                }
+                m[0] = d[0] - dn[0]; m[1] = d[1] - dn[1]; m[2] = d[2] - dn[2];
                 float2 pa = fourteen ? A.esf14[a] : A.esf[a];
                 float2 pb = fourteen ? A.esf14[j] : A.esf[j];
                 float s = pa.y + pb.y;
-                float qk = (float)(CHGCHARMM * KCALTOIU) * __int_as_float(fo.w) * __int_as_float(gjo.w);
+                float2 qa = A.qf[a], qb = A.qf[j];
+                float qh, ql;
+                ff_mul(qa.x, qa.y, qb.x, qb.y, qh, ql);
+                float qk = (float)(CHGCHARMM * KCALTOIU) * (qh + ql);
                 int np_ = 0;
                 dbd += (double)mixed_pair_delta(d[0], d[1], d[2], m[0], m[1], m[2], qk, 4.0f * pa.x * pb.x, s * s,
                                                 apply_cut ? cut : cutx, np_);
@@ -745,7 +743,7 @@ static int dupload(T** p, const std::vector<T>& v, cudaStream_t st) {
 SingleEngine::~SingleEngine() { release(); }
 
 void SingleEngine::release() {
-    void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
+    void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
                     d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
                     d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_out, d_maxrow,
                     d_stage};
@@ -771,17 +769,19 @@ int SingleEngine::init(const HostSystem& h) {
     cut.c2f = (float)cut.c2; cut.n2f = (float)cut.n2; cut.sw2f = (float)cut.sw2;
     std::vector<double4> pq(n);
     std::vector<double2> es(n), es14(n);
-    std::vector<float2> esf(n), esf14(n);
+    std::vector<float2> esf(n), esf14(n), qf(n);
     for (int i = 0; i < n; i++) {
         pq[i] = make_double4(hs.x[i], hs.y[i], hs.z[i], hs.q[i]);
         es[i] = make_double2(hs.eps[i], hs.sig[i]);
         es14[i] = make_double2(hs.eps14[i], hs.sig14[i]);
         esf[i] = make_float2((float)hs.eps[i], (float)hs.sig[i]);
         esf14[i] = make_float2((float)hs.eps14[i], (float)hs.sig14[i]);
+        float qh = (float)hs.q[i];
+        qf[i] = make_float2(qh, (float)(hs.q[i] - (double)qh));
     }
     int rc;
     if ((rc = dupload(&d_pq, pq, stream)) || (rc = dupload(&d_es, es, stream)) || (rc = dupload(&d_es14, es14, stream)) ||
-        (rc = dupload(&d_esf, esf, stream)) || (rc = dupload(&d_esf14, esf14, stream)) ||
+        (rc = dupload(&d_esf, esf, stream)) || (rc = dupload(&d_esf14, esf14, stream)) || (rc = dupload(&d_qf, qf, stream)) ||
         (rc = dupload(&d_frozen, hs.frozen, stream)) || (rc = dupload(&d_xs, hs.exclStart, stream)) ||
         (rc = dupload(&d_xd, hs.exclData, stream)) || (rc = dupload(&d_fxs, hs.fexclStart, stream)) ||
         (rc = dupload(&d_fxd, hs.fexclData, stream)))
@@ -841,7 +841,7 @@ int SingleEngine::init(const HostSystem& h) {
 
 AtomsDev SingleEngine::atoms() const {
     AtomsDev A;
-    A.pq = d_pq; A.es = d_es; A.es14 = d_es14; A.fx = d_fx; A.esf = d_esf; A.esf14 = d_esf14;
+    A.pq = d_pq; A.es = d_es; A.es14 = d_es14; A.fx = d_fx; A.esf = d_esf; A.esf14 = d_esf14; A.qf = d_qf;
     for (int k = 0; k < 3; k++) A.Ls[k] = (float)(hs.L[k] / 4294967296.0);
     return A;
 }

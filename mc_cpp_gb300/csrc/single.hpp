@@ -46,7 +46,7 @@ private:
     double4* d_pq = nullptr;
     double2 *d_es = nullptr, *d_es14 = nullptr;
     uint4* d_fx = nullptr;
-    float2 *d_esf = nullptr, *d_esf14 = nullptr;
+    float2 *d_esf = nullptr, *d_esf14 = nullptr, *d_qf = nullptr;
     uint8_t* d_frozen = nullptr;
     int *d_xs = nullptr, *d_xd = nullptr, *d_fxs = nullptr, *d_fxd = nullptr;
     int2* d_p14 = nullptr;

@@ -138,10 +138,9 @@ def test_host_buffer_run_roundtrip():
 def test_invalid_batches_rejected():
     w = systems.water_box(512, seed=3)
     flexible = w.copy()
-    flexible.angles = flexible.angles[:0]     # H-H no longer excluded: not a rigid residue
-    flexible.angle_type = flexible.angle_type[:0]
-    flexible.angle_k = flexible.angle_k[:0]
-    flexible.angle_theta0 = flexible.angle_theta0[:0]
+    # without bonds and angles no intra-residue pair is excluded: not a rigid residue
+    for k in ("angles", "angle_type", "angle_k", "angle_theta0", "bonds", "bond_type", "bond_k", "bond_r0", "bond_beta"):
+        setattr(flexible, k, getattr(flexible, k)[:0])
     with pytest.raises(native.McgError) as ei:
         BatchChains([w, flexible])
     assert ei.value.code == native.MCG_ENOTSUP

@@ -183,7 +183,7 @@ def test_half_box_ties_and_cell_boundaries():
     # atoms exactly L/2 apart (MIC tie) and on cell boundaries; rint rounds half away from zero
     L = 30.0
     s = _tiny(6, L=L)
-    xyz = np.array([[0.0, 0, 0], [15.0, 0, 0], [-15.0, 0.0, 0.0], [7.5, 7.5, 7.5], [-7.5, 0, 14.0], [3.0, -15.0, 0.0]])
+    xyz = np.array([[0.0, 0, 0], [15.0, 0, 0], [-7.5, 3.0, 0.0], [7.5, 7.5, 7.5], [-7.5, 0, 14.0], [3.0, -15.0, 4.0]])
     s.set_coords(xyz)
     s.cutoff, s.cuton, s.dcut = 14.0, 10.0, 1.0
     for mode in ("full", "switch"):
