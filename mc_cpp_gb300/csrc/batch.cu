@@ -85,7 +85,7 @@ struct ChainDev {
     float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
-    float Ls[3];          // L / 2^32 : mirror units -> Angstrom
+    float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
     double beta;
     float dmax_trn, dmax_rot;
     int ntypes_move;      // 1: TRN only, 2: TRN + ROT
@@ -111,7 +111,7 @@ struct BatchGeom {
     int cap;
 };
 
-__device__ __forceinline__ float fdelta(uint32_t a, uint32_t b, float Ls) { return __int2float_rn((int)(b - a)) * Ls; }
+__device__ __forceinline__ float fdelta(uint32_t a, uint32_t b, float Lh, float Ll) { return fixed_delta(a, b, Lh, Ll); }
 
 __device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
     return (int)((((v + 0x80000000u) >> 8) * (uint64_t)nc) >> 24);
@@ -194,13 +194,13 @@ __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4*
         bool ok = false;
         if (valid && q != r) {
             const uint4 pq = Fc[q * apr];
-            const float dx = fdelta(pa[0].x, pq.x, C.Ls[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2]);
+            const float dx = fdelta(pa[0].x, pq.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2], C.Lsl[2]);
             if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
                 for (int b = 0; b < apr && !ok; b++) {
                     const uint4 pb = Fc[q * apr + b];
                     for (int k = 0; k < apr; k++) {
-                        const float ex = fdelta(pa[k].x, pb.x, C.Ls[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1]),
-                                    ez = fdelta(pa[k].z, pb.z, C.Ls[2]);
+                        const float ex = fdelta(pa[k].x, pb.x, C.Ls[0], C.Lsl[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1], C.Lsl[1]),
+                                    ez = fdelta(pa[k].z, pb.z, C.Ls[2], C.Lsl[2]);
                         if (ex * ex + ey * ey + ez * ez <= G.rlist2) { ok = true; break; }
                     }
                 }
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                     sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
                     const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
                     const uint4 fp = Fc[res * apr + piv];
-                    const float ox = fdelta(fp.x, fo.x, C.Ls[0]), oy = fdelta(fp.y, fo.y, C.Ls[1]), oz = fdelta(fp.z, fo.z, C.Ls[2]);
+                    const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]), oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
                     const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
                     dx = qw * tx + (qy * tz - qz * ty);
                     dy = qw * ty + (qz * tx - qx * tz);
@@ -367,9 +367,9 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                 P.fo[lane] = fo;
                 P.fn[lane] = fn;
                 P.mn[lane][0] = nx; P.mn[lane][1] = ny; P.mn[lane][2] = nz;
-                P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0]);
-                P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1]);
-                P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2]);
+                P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
+                P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
+                P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
             }
             if (lane == 0) {
                 P.res = res;
@@ -406,8 +406,8 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                     if (k >= apr) break;
                     const float4 t = s_tab[fo[k].w][pb.w];
                     // d_old = b - a_old, d_new = b - a_new = d_old - m
-                    acc += mixed_pair_delta(fdelta(fo[k].x, pb.x, C.Ls[0]), fdelta(fo[k].y, pb.y, C.Ls[1]),
-                                            fdelta(fo[k].z, pb.z, C.Ls[2]), m[k][0], m[k][1], m[k][2], t.x, t.y, t.z, cut, np);
+                    acc += mixed_pair_delta(fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]), fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]),
+                                            fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]), m[k][0], m[k][1], m[k][2], t.x, t.y, t.z, cut, np);
                 }
             }
         }
@@ -457,9 +457,9 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
                 Mc[a] = make_ulonglong4(P.mn[lane][0], P.mn[lane][1], P.mn[lane][2], 0ull);
                 Fc[a] = P.fn[lane];
                 const uint4 bpos = FB[C.atom0 + a];
-                const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0]);
-                const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1]);
-                const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2]);
+                const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0], C.Lsl[0]);
+                const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1], C.Lsl[1]);
+                const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2], C.Lsl[2]);
                 far = ex * ex + ey * ey + ez * ez > G.half_skin2;
             }
             if (__any_sync(0xffffffffu, far) && lane == 0) P.rebuild = 1;
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __res
     const ChainDev& C = chains[c];
     if (APR && C.apr != APR) return;
     const int apr = APR ? APR : C.apr;
-    for (int k = threadIdx.x; k < MAX_APR * MAX_APR; k += blockDim.x) s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1], C.tab[k / MAX_APR][k % MAX_APR][2], 0.f);
+    for (int k = threadIdx.x; k < MAX_APR * MAX_APR; k += blockDim.x) s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1], C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
     __syncthreads();
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __res
                 const uint4 pa = Fc[r * apr + k];
                 for (int b = 0; b < apr; b++) {
                     const uint4 pb = Fc[q * apr + b];
-                    const float dx = fdelta(pa.x, pb.x, C.Ls[0]), dy = fdelta(pa.y, pb.y, C.Ls[1]), dz = fdelta(pa.z, pb.z, C.Ls[2]);
+                    const float dx = fdelta(pa.x, pb.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa.y, pb.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa.z, pb.z, C.Ls[2], C.Lsl[2]);
                     const float u = dx * dx + dy * dy + dz * dz;
                     if (u > cut.c2f) continue;
                     const float4 t = s_tab[pa.w][pb.w];
@@ -790,6 +790,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             C.L[k] = hs.L[k]; C.rL[k] = hs.rL[k];
             C.tofix32[k] = (float)(4294967296.0 / hs.L[k]);
             C.Ls[k] = (float)(hs.L[k] / 4294967296.0);
+            C.Lsl[k] = (float)(hs.L[k] / 4294967296.0 - (double)C.Ls[k]);
         }
         C.beta = 1.0 / ((RBOLTZUI / KCALTOIU) * hs.temp);
         if (opts->acceptance_units == MCG_ACCEPT_PHYSICAL) C.beta /= KCALTOIU;

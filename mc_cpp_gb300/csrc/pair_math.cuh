@@ -75,10 +75,13 @@ __device__ __forceinline__ uint32_t to_fixed(double x, double rL) {
     return (uint32_t)(unsigned long long)v;
 }
 
-// exact minimum-image displacement b - a in box units of 2^-32, converted to Angstrom (FP32)
-__device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float Lscale) {
-    int d = (int)(b - a);
-    return __int2float_rn(d) * Lscale;
+// exact minimum-image displacement b - a in box units of 2^-32, converted to Angstrom (FP32).
+// The scale L/2^32 is a float-float pair (Lh + Ll): a scale rounded to float would shrink or
+// stretch every distance by the same factor, a systematic error that the virial of an unrelaxed
+// configuration amplifies about fifty-fold in the total energy.
+__device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float Lh, float Ll) {
+    const float f = __int2float_rn((int)(b - a));
+    return fmaf(f, Lh, f * Ll);
 }
 
 // FP32 switched LJ + Coulomb on r^2 (unscaled el, vd as in ref64_pair).  The charge product is

@@ -246,7 +246,7 @@ struct AtomsDev {
     const float2* esf;
     const float2* esf14;
     const float2* qf;     // charge as float-float (hi, lo)
-    float Ls[3];          // box / 2^32 (mixed displacement scale)
+    float Ls[3], Lsl[3];  // box / 2^32 as float-float (mixed displacement scale)
 };
 
 template <int P>
@@ -263,9 +263,9 @@ __device__ __forceinline__ void pair_energy(const AtomsDev& A, const PbcDev& pbc
     } else {
         float dx, dy, dz;
         if (pbc.type != 0) {
-            dx = fixed_delta(fi.x, fj.x, A.Ls[0]);
-            dy = fixed_delta(fi.y, fj.y, A.Ls[1]);
-            dz = fixed_delta(fi.z, fj.z, A.Ls[2]);
+            dx = fixed_delta(fi.x, fj.x, A.Ls[0], A.Lsl[0]);
+            dy = fixed_delta(fi.y, fj.y, A.Ls[1], A.Lsl[1]);
+            dz = fixed_delta(fi.z, fj.z, A.Ls[2], A.Lsl[2]);
         } else {
             dx = (float)(pj.x - pi.x); dy = (float)(pj.y - pi.y); dz = (float)(pj.z - pi.z);
         }
@@ -583,6 +583,16 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         const uint4 fn = P == PREC_MIX ? s_fx[ka] : make_uint4(0, 0, 0, 0);
         CutDev cutx = cut;   // full mode: no cutoff and no switch
         if (!sw) { cutx.c2f = 3.0e38f; cutx.n2f = 3.0e38f; }
+        float ma[3] = {0.f, 0.f, 0.f};   // the exact move of a, as the fixed-point mirror sees it
+        if (P == PREC_MIX) {
+            if (pbc.type != 0) {
+                ma[0] = fixed_delta(fo.x, fn.x, A.Ls[0], A.Lsl[0]);
+                ma[1] = fixed_delta(fo.y, fn.y, A.Ls[1], A.Lsl[1]);
+                ma[2] = fixed_delta(fo.z, fn.z, A.Ls[2], A.Lsl[2]);
+            } else {
+                ma[0] = (float)(an.x - ao.x); ma[1] = (float)(an.y - ao.y); ma[2] = (float)(an.z - ao.z);
+            }
+        }
         auto visit = [&](int j, bool fourteen, bool apply_cut) {
             int sj = slot(j);
             if (sj >= 0 && j < a) return;       // counted by the lower index's block
@@ -601,19 +611,25 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
                 // d_old = j_old - a_old, d_new = j_new - a_new = d_old - m
                 float d[3], m[3];
                 if (pbc.type != 0) {
-                    d[0] = fixed_delta(fo.x, gjo.x, A.Ls[0]); d[1] = fixed_delta(fo.y, gjo.y, A.Ls[1]); d[2] = fixed_delta(fo.z, gjo.z, A.Ls[2]);
+                    d[0] = fixed_delta(fo.x, gjo.x, A.Ls[0], A.Lsl[0]); d[1] = fixed_delta(fo.y, gjo.y, A.Ls[1], A.Lsl[1]); d[2] = fixed_delta(fo.z, gjo.z, A.Ls[2], A.Lsl[2]);
                 } else {
                     d[0] = (float)(jo.x - ao.x); d[1] = (float)(jo.y - ao.y); d[2] = (float)(jo.z - ao.z);
                 }
-                // m = d_old - d_new with both displacements taken by minimum image: when the move
-                // carries a pair across half the box (possible without a cutoff) the image changes
+                // d_new by minimum image; m = d_old - d_new is taken from the exact move of a when
+                // only a moved (so the analytic difference keeps its accuracy), and the pair is
+                // differenced directly when the move carries it across half the box
                 float dn[3];
                 if (pbc.type != 0) {
-                    dn[0] = fixed_delta(fn.x, gjn.x, A.Ls[0]); dn[1] = fixed_delta(fn.y, gjn.y, A.Ls[1]); dn[2] = fixed_delta(fn.z, gjn.z, A.Ls[2]);
+                    dn[0] = fixed_delta(fn.x, gjn.x, A.Ls[0], A.Lsl[0]); dn[1] = fixed_delta(fn.y, gjn.y, A.Ls[1], A.Lsl[1]); dn[2] = fixed_delta(fn.z, gjn.z, A.Ls[2], A.Lsl[2]);
                 } else {
                     dn[0] = (float)(jn.x - an.x); dn[1] = (float)(jn.y - an.y); dn[2] = (float)(jn.z - an.z);
                 }
-                m[0] = d[0] - dn[0]; m[1] = d[1] - dn[1]; m[2] = d[2] - dn[2];
+                bool flip = false;
+                if (sj >= 0) { m[0] = d[0] - dn[0]; m[1] = d[1] - dn[1]; m[2] = d[2] - dn[2]; }
+                else {
+                    m[0] = ma[0]; m[1] = ma[1]; m[2] = ma[2];
+                    for (int t = 0; t < 3; t++) flip |= fabsf(d[t] - m[t] - dn[t]) > 1.0f;
+                }
                 float2 pa = fourteen ? A.esf14[a] : A.esf[a];
                 float2 pb = fourteen ? A.esf14[j] : A.esf[j];
                 float s = pa.y + pb.y;
@@ -622,8 +638,18 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
                 ff_mul(qa.x, qa.y, qb.x, qb.y, qh, ql);
                 float qk = (float)(CHGCHARMM * KCALTOIU) * (qh + ql);
                 int np_ = 0;
-                dbd += (double)mixed_pair_delta(d[0], d[1], d[2], m[0], m[1], m[2], qk, 4.0f * pa.x * pb.x, s * s,
-                                                apply_cut ? cut : cutx, np_);
+                if (!flip) {
+                    dbd += (double)mixed_pair_delta(d[0], d[1], d[2], m[0], m[1], m[2], qk, 4.0f * pa.x * pb.x, s * s,
+                                                    apply_cut ? cut : cutx, np_);
+                } else {
+                    float e0, v0, e1, v1;
+                    const CutDev& cc = apply_cut ? cut : cutx;
+                    const float u0 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2], u1 = dn[0] * dn[0] + dn[1] * dn[1] + dn[2] * dn[2];
+                    e0 = v0 = e1 = v1 = 0.f;
+                    if (!apply_cut || u0 <= cc.c2f) mixed_pair(u0, qh, ql, pa.x * pb.x, s * s, apply_cut, cc, e0, v0);
+                    if (!apply_cut || u1 <= cc.c2f) mixed_pair(u1, qh, ql, pa.x * pb.x, s * s, apply_cut, cc, e1, v1);
+                    dbd += (double)(CHGCHARMM * KCALTOIU) * ((double)e1 - (double)e0) + 4.0 * ((double)v1 - (double)v0);
+                }
             }
         };
         if (sw) {
@@ -842,7 +868,11 @@ int SingleEngine::init(const HostSystem& h) {
 AtomsDev SingleEngine::atoms() const {
     AtomsDev A;
     A.pq = d_pq; A.es = d_es; A.es14 = d_es14; A.fx = d_fx; A.esf = d_esf; A.esf14 = d_esf14; A.qf = d_qf;
-    for (int k = 0; k < 3; k++) A.Ls[k] = (float)(hs.L[k] / 4294967296.0);
+    for (int k = 0; k < 3; k++) {
+        const double ls = hs.L[k] / 4294967296.0;
+        A.Ls[k] = (float)ls;
+        A.Lsl[k] = (float)(ls - (double)A.Ls[k]);
+    }
     return A;
 }
 
