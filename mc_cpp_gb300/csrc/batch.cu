@@ -91,6 +91,7 @@ struct ChainDev {
     int ntypes_move;      // 1: TRN only, 2: TRN + ROT
     uint32_t key0, key1;
     float tab[MAX_APR][MAX_APR][4];   // (qk, e4, ss, qk_lo) per slot pair; qk + qk_lo = K q_a q_b
+    float tablo[MAX_APR][MAX_APR][2]; // (e4_lo, ss_lo): float-float parts for total-energy kernels
 };
 
 struct ChainState {
@@ -538,54 +539,67 @@ __global__ void k_batch_energy64(const ChainDev* __restrict__ chains, const int*
 }
 
 // ---- mixed-precision energy of every chain over its neighbour lists (each pair once: q > r)
+// One warp per residue over the GPU writes the residue's share; one block per chain then sums the
+// shares in residue order, so the result does not depend on scheduling.
 template <int APR>
-__global__ void __launch_bounds__(256) k_batch_energy_list(const ChainDev* __restrict__ chains, BatchGeom G,
-                                                           const uint4* __restrict__ F, const uint16_t* __restrict__ LST,
-                                                           const int* __restrict__ NL, ChainState* state, int nchains) {
-    __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
-    __shared__ double s_red[8];
-    const int c = blockIdx.x;
-    if (c >= nchains) return;
-    const ChainDev& C = chains[c];
-    if (APR && C.apr != APR) return;
-    const int apr = APR ? APR : C.apr;
-    for (int k = threadIdx.x; k < MAX_APR * MAX_APR; k += blockDim.x) s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1], C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
-    __syncthreads();
+__global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __restrict__ chains, BatchGeom G,
+                                                          const uint4* __restrict__ F, const int* __restrict__ res_chain,
+                                                          const uint16_t* __restrict__ LST, const int* __restrict__ NL,
+                                                          double* e_res, int64_t nres_total) {
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
     cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
-    const uint4* Fc = F + C.atom0;
-    F32Acc acc;
-    for (int r = threadIdx.x; r < C.nres; r += blockDim.x) {
-        const uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
-        const int nl = NL[C.res0 + r];
-        for (int e = 0; e < nl; e++) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
+        const int c = res_chain[gr];
+        const ChainDev& C = chains[c];
+        if (APR && C.apr != APR) continue;
+        const int apr = APR ? APR : C.apr;
+        const int r = (int)(gr - C.res0);
+        const uint4* Fc = F + C.atom0;
+        const uint16_t* row = LST + (size_t)gr * G.cap;
+        const int nl = NL[gr];
+        F32Acc acc;
+        for (int e = lane; e < nl; e += 32) {
             const int q = row[e];
             if (q <= r) continue;
             for (int k = 0; k < apr; k++) {
                 const uint4 pa = Fc[r * apr + k];
                 for (int b = 0; b < apr; b++) {
                     const uint4 pb = Fc[q * apr + b];
-                    const float dx = fdelta(pa.x, pb.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa.y, pb.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa.z, pb.z, C.Ls[2], C.Lsl[2]);
+                    const float dx = fdelta(pa.x, pb.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa.y, pb.y, C.Ls[1], C.Lsl[1]),
+                                dz = fdelta(pa.z, pb.z, C.Ls[2], C.Lsl[2]);
                     const float u = dx * dx + dy * dy + dz * dz;
                     if (u > cut.c2f) continue;
-                    const float4 t = s_tab[pa.w][pb.w];
                     float el, vd;
-                    mixed_pair(u, t.x, t.w, t.y, t.z, true, cut, el, vd);
-                    acc.add(el + vd);
+                    mixed_pair(u, C.tab[pa.w][pb.w][0], C.tab[pa.w][pb.w][3], C.tab[pa.w][pb.w][1], C.tab[pa.w][pb.w][2],
+                               true, cut, el, vd, C.tablo[pa.w][pb.w][0], C.tablo[pa.w][pb.w][1]);
+                    acc.add(el);
+                    acc.add(vd);
                 }
             }
         }
+        const double v = warp_sum(acc.value());
+        if (lane == 0) e_res[gr] = v;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const double v = warp_sum(acc.value());
-    if (lane == 0) s_red[warp] = v;
+}
+
+__global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const double* __restrict__ e_res,
+                                   ChainState* state, int nchains) {
+    __shared__ double sh[256];
+    const int c = blockIdx.x;
+    if (c >= nchains) return;
+    const ChainDev& C = chains[c];
+    double s = 0.0;
+    for (int r = threadIdx.x; r < C.nres; r += blockDim.x) s += e_res[C.res0 + r];
+    sh[threadIdx.x] = s;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double e = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) e += s_red[w];
-        state[c].etot = e;
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
     }
+    if (threadIdx.x == 0) state[c].etot = sh[0];
 }
 
 // FP64 coordinates (all chains concatenated) -> 64-bit masters and 32-bit mirrors
@@ -638,6 +652,12 @@ static uint64_t host_master(double v, double rL) {
 
 static double host_view(uint64_t v, double L) { return (double)(int64_t)v * (L / TWO64); }
 
+static int balloc_d(double** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(1, n) * sizeof(double));
+    if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return MCG_OK;
+}
+
 struct mcg_batch {
     int nchains = 0;
     int64_t natoms = 0, nres = 0;
@@ -661,13 +681,14 @@ struct mcg_batch {
     CutDev cut64{};
     cudaGraphExec_t graph = nullptr;
     double* d_xyz = nullptr;      // staging for host-buffer runs (3 x natoms)
+    double* d_eres = nullptr;     // per-residue energy shares (mixed recompute)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int threads = 256;
     int64_t rebuilds_seen = 0, launches = 0;
     ~mcg_batch() {
         if (graph) cudaGraphExecDestroy(graph);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
-                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain};
+                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -689,14 +710,18 @@ struct mcg_batch {
     }
     int launch_build() { return launch_build(stream); }
     int launch_energy_list() {
+        int r;
+        if (!d_eres && (r = balloc_d(&d_eres, (size_t)nres))) return r;
+        const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_energy_list<3><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+            k_batch_energy_res<3><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
         else if (apr_all == 1)
-            k_batch_energy_list<1><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+            k_batch_energy_res<1><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
         else
-            k_batch_energy_list<0><<<nchains, 256, 0, stream>>>(d_chains, G, d_F, d_LST, d_NL, d_state, nchains);
+            k_batch_energy_res<0><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
+        k_batch_energy_sum<<<nchains, 256, 0, stream>>>(d_chains, d_eres, d_state, nchains);
         BK(cudaGetLastError());
-        launches++;
+        launches += 2;
         return MCG_OK;
     }
     int ensure_graph() {
@@ -805,9 +830,12 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
                 const double qk = K * hs.q[a] * hs.q[b];
                 C.tab[a][b][0] = (float)qk;
                 C.tab[a][b][3] = (float)(qk - (double)(float)qk);
-                C.tab[a][b][1] = (float)(4.0 * hs.eps[a] * hs.eps[b]);
+                const double e4 = 4.0 * hs.eps[a] * hs.eps[b];
+                C.tab[a][b][1] = (float)e4;
+                C.tablo[a][b][0] = (float)(e4 - (double)(float)e4);
                 double s = hs.sig[a] + hs.sig[b];
                 C.tab[a][b][2] = (float)(s * s);
+                C.tablo[a][b][1] = (float)(s * s - (double)(float)(s * s));
             }
         for (int i = 0; i < hs.n; i++) {
             ulonglong4 m;

@@ -89,10 +89,11 @@ __device__ __forceinline__ float fixed_delta(uint32_t a, uint32_t b, float Lh, f
 // the cancellation between positive and negative Coulomb terms would amplify to ~1e-6 of the
 // total.  ee = eps_i eps_j, ss = (sig_i + sig_j)^2.
 __device__ __forceinline__ void mixed_pair(float r2, float qq, float qq_lo, float ee, float ss, bool do_switch,
-                                           const CutDev& c, float& el, float& vd) {
+                                           const CutDev& c, float& el, float& vd, float ee_lo = 0.f, float ss_lo = 0.f) {
     float rinv = rsqrtf(r2);
     rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step on the hardware estimate
-    float x2 = ss * (rinv * rinv);
+    const float ri2 = rinv * rinv;
+    float x2 = fmaf(ss, ri2, ss_lo * ri2);               // (sig_i+sig_j)^2 / r^2, float-float constant
     float x6 = x2 * x2 * x2;
     float f = 1.0f;
     if (do_switch && r2 > c.n2f) {
@@ -100,7 +101,8 @@ __device__ __forceinline__ void mixed_pair(float r2, float qq, float qq_lo, floa
         f = s1 * s1 * (c.c2f + 2.0f * r2 - 3.0f * c.n2f) * c.sw2f;
     }
     el = fmaf(qq, rinv, qq_lo * rinv) * f;
-    vd = ee * (x6 * x6 - x6) * f;
+    const float l = x6 * x6 - x6;
+    vd = fmaf(ee, l, ee_lo * l) * f;
 }
 
 // float-float product of two float-float values (hi parts exact by FMA, cross terms rounded)
