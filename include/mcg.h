@@ -150,9 +150,10 @@ typedef struct mcg_batch_opts {
     double dmax_trn;          /* Angstrom */
     double dmax_rot;          /* degrees */
     int acceptance_units;     /* enum mcg_acceptance */
-    int threads_per_chain;    /* 0 = autotuned */
+    int threads_per_chain;    /* threads of the CTA that runs a chain's moves (64..256, 0 = 256) */
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
+    int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
 } mcg_batch_opts;
 
 /* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */

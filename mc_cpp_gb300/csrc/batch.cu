@@ -299,19 +299,22 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 template <int APR>
 __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                      uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
-                                                     int* g_cell, ChainState* state, const int* __restrict__ order,
-                                                     int nchains) {
+                                                     int* g_cell, ChainState* state, const int* __restrict__ cta_start,
+                                                     const int* __restrict__ cta_chains, int nchains) {
     __shared__ Proposal P;
     __shared__ float2 s_red[8];
     __shared__ int s_cell[MAX_CELLS + 1];
     __shared__ int s_err;
     __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int c = order[blockIdx.x];
-    if (c >= nchains) return;
+    // this CTA's chains, largest first (host-side longest-processing-time packing)
+    for (int slot = cta_start[blockIdx.x]; slot < cta_start[blockIdx.x + 1]; slot++) {
+    const int c = cta_chains[slot];
+    if (c >= nchains) continue;
     const ChainDev& C = chains[c];
-    if (APR && C.apr != APR) return;
+    if (APR && C.apr != APR) continue;
     const int apr = APR ? APR : C.apr;
+    __syncthreads();   // the previous chain's last reads of the shared tables are done
     for (int k = tid; k < MAX_APR * MAX_APR; k += blockDim.x)
         s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
                                                       C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
@@ -489,6 +492,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
         if (s_err) S.err = s_err;
         state[c] = S;
     }
+    }  // chains of this CTA
 }
 
 // FP64 view of a master coordinate
@@ -664,11 +668,13 @@ struct mcg_batch {
     int apr_all = 0;            // common residue size (0 if mixed)
     BatchGeom G{};
     std::vector<ChainDev> chains;
-    std::vector<int> order;
+    std::vector<int> order, cta_start;
     cudaStream_t stream = nullptr;
     ChainDev* d_chains = nullptr;
     ChainState* d_state = nullptr;
-    int* d_order = nullptr;
+    int* d_order = nullptr;       // chains of each CTA, CTA after CTA (d_cta_start: CSR offsets)
+    int* d_cta_start = nullptr;
+    int ncta = 0;
     ulonglong4* d_M = nullptr;
     uint4 *d_F = nullptr, *d_FB = nullptr;
     uint16_t* d_LST = nullptr;
@@ -688,7 +694,7 @@ struct mcg_batch {
     ~mcg_batch() {
         if (graph) cudaGraphExecDestroy(graph);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
-                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres};
+                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -740,11 +746,11 @@ struct mcg_batch {
     }
     int launch_sweep(cudaStream_t st) {
         if (apr_all == 3)
-            k_batch_sweep<3><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+            k_batch_sweep<3><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
         else if (apr_all == 1)
-            k_batch_sweep<1><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+            k_batch_sweep<1><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
         else
-            k_batch_sweep<0><<<nchains, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_order, nchains);
+            k_batch_sweep<0><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
         BK(cudaGetLastError());
         return MCG_OK;
     }
@@ -895,10 +901,41 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if (G.cap > 65535) G.cap = 65535;
     B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 256;
     if (B->threads % 32 || B->threads > 256 || B->threads < 64) return fail(MCG_EINVAL, "threads_per_chain must be a multiple of 32 in [64, 256]");
-    // chain order: largest first, so the longest sweeps start first
-    B->order.resize(nchains);
-    std::iota(B->order.begin(), B->order.end(), 0);
-    std::stable_sort(B->order.begin(), B->order.end(), [&](int a, int b) { return B->chains[a].nres > B->chains[b].nres; });
+    // Longest-processing-time packing of chains onto persistent CTAs (one per SM): the cost of a
+    // chain's sweep is its move count times the pairs one move touches.  The largest chains get a
+    // CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    B->ncta = std::min(nchains, std::max(1, nsm * std::max(1, opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 1)));
+    {
+        std::vector<double> cost(nchains);
+        const double rl = rc + skin;
+        for (int c = 0; c < nchains; c++) {
+            const ChainDev& C = B->chains[c];
+            const double dens = C.nres / (C.L[0] * C.L[1] * C.L[2]);
+            const double neigh = std::min((double)C.nres, dens * 4.0 / 3.0 * PI * rl * rl * rl);
+            cost[c] = (double)C.nres * neigh * C.apr * C.apr + 1.0;
+        }
+        std::vector<int> idx(nchains);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+        std::vector<double> load(B->ncta, 0.0);
+        std::vector<std::vector<int>> per(B->ncta);
+        for (int c : idx) {
+            int best = 0;
+            for (int k = 1; k < B->ncta; k++) if (load[k] < load[best]) best = k;
+            load[best] += cost[c];
+            per[best].push_back(c);
+        }
+        B->order.clear();
+        B->cta_start.assign(B->ncta + 1, 0);
+        for (int k = 0; k < B->ncta; k++) {
+            B->cta_start[k] = (int)B->order.size();
+            B->order.insert(B->order.end(), per[k].begin(), per[k].end());
+        }
+        B->cta_start[B->ncta] = (int)B->order.size();
+    }
     BK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
     int r;
     if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) || (r = balloc(&B->d_order, nchains)) ||
@@ -914,7 +951,9 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         BK(cudaMemcpy(B->d_res_chain, rcn.data(), sizeof(int) * res0, cudaMemcpyHostToDevice));
     }
     BK(cudaMemcpyAsync(B->d_chains, B->chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, B->stream));
+    if ((r = balloc(&B->d_cta_start, B->ncta + 1))) return r;
     BK(cudaMemcpyAsync(B->d_order, B->order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_cta_start, B->cta_start.data(), sizeof(int) * (B->ncta + 1), cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_F, F.data(), sizeof(uint4) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice, B->stream));

@@ -172,7 +172,7 @@ __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float do
     if (io && in) {
         const float du = -(mx * (dox + dnx) + my * (doy + dny) + mz * (doz + dnz));
         const float p = ro * rn;
-        const float dinv = -du * p * p / (ro + rn);
+        const float dinv = __fdividef(-du * p * p, ro + rn);   // relative error a few ulp of the change
         float ds = 0.0f;
         const float ua = fmaxf(uo, c.n2f), ub = fmaxf(un, c.n2f);
         if (ua != ub) {
