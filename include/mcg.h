@@ -190,6 +190,24 @@ int mcg_batch_counters(mcg_batch* b, int64_t* list_rebuilds, int64_t* kernel_lau
  * (the denominator of the pair kernels' roofline). */
 int mcg_probe_fp32_tflops(double* tflops);
 
+/* --- allocation-free energy ------------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory when they need
+ * an energy (a host code whose memory pool owns the whole GPU and forbids side allocations, or a
+ * real-time loop that cannot afford cudaMalloc's implicit synchronisation): the FP64 switched
+ * nonbonded energy over a half Verlet list, with its per-block partial sums in a fixed-size static
+ * device array instead of allocated scratch.  All pointers are device pointers supplied by the
+ * caller: pq[4*natom] = (x, y, z, q) per atom (32-byte aligned), es[2*natom] = (sqrt(eps*418.4),
+ * MDBAS half-sigma) as the reference's AtomList stores them (16-byte aligned), nbr[natom*cap] rows
+ * of partners j > i with nup[natom] entries each; out[2] receives (elec, vdw) in iu.  Launched on
+ * `stream` (a cudaStream_t, NULL for the default stream), asynchronous.  natom is limited to
+ * MCG_NOALLOC_MAX_ATOMS (the static scratch is 512 KiB on every GPU that loads the library).  The
+ * first call on a device looks up the scratch address (cudaGetSymbolAddress) with that device
+ * current.  Calls share the scratch: calls that overlap on the GPU race and must be serialised. */
+#define MCG_NOALLOC_MAX_ATOMS 262144
+int mcg_energy_switch_fp64_noalloc(int natom, const double* pq, const double* es, const int* nbr, const int* nup,
+                                   int cap, int pbc_type, const double box[3], double cutoff, double cuton,
+                                   double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
