@@ -109,6 +109,7 @@ struct BatchGeom {
     float rcent2;      // (rc + skin + 2 rext)^2, residue-centre prefilter
     float half_skin2;  // (skin/2)^2
     float cellmin;     // cell edge for the 5-stencil
+    float skip2;       // (rc + extent from the first atom + largest move)^2: dE prefilter
     int cap;
 };
 
@@ -129,7 +130,7 @@ __device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
 // Block-level binning of chain C: copies the build positions and, when the chain uses cells,
 // fills starts[0..ncell] (shared or global) and g_order (residues sorted by cell, then index).
 __device__ void chain_bin(const ChainDev& C, const uint4* __restrict__ F, uint4* FB, int* starts, int* g_order,
-                          int* g_cell) {
+                          int* g_cell, uint4* g_pos) {
     const int apr = C.apr, nres = C.nres;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     const uint4* Fc = F + C.atom0;
@@ -178,23 +179,32 @@ __device__ void chain_bin(const ChainDev& C, const uint4* __restrict__ F, uint4*
         }
     }
     __syncthreads();
+    // first-atom positions in cell order: the candidate scan reads them contiguously
+    for (int t = tid; t < nres; t += T) g_pos[t] = Fc[g_order[t] * apr];
+    __syncthreads();
 }
 
 // Warp-level list of residue r (all 32 lanes of the calling warp).
 template <int APR>
 __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int r,
-                             const int* __restrict__ starts, const int* __restrict__ g_order, uint16_t* LST, int* NL,
-                             int* err_out) {
+                             const int* __restrict__ starts, const int* __restrict__ g_order,
+                             const uint4* __restrict__ g_pos, uint16_t* LST, int* NL, int* err_out) {
     const int apr = APR ? APR : C.apr;
     const int lane = threadIdx.x & 31;
     uint4 pa[APR ? APR : MAX_APR];
     for (int k = 0; k < apr; k++) pa[k] = Fc[r * apr + k];
     uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
     int cnt = 0;
-    auto consider = [&](int q, bool valid) {
+    // cells: `slot` indexes the cell-sorted arrays; otherwise it is the residue itself
+    auto consider = [&](int slot, bool valid) {
         bool ok = false;
+        int q = slot;
+        uint4 pq = make_uint4(0, 0, 0, 0);
+        if (valid) {
+            if (C.use_cells) { pq = g_pos[slot]; q = g_order[slot]; }
+            else pq = Fc[q * apr];
+        }
         if (valid && q != r) {
-            const uint4 pq = Fc[q * apr];
             const float dx = fdelta(pa[0].x, pq.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2], C.Lsl[2]);
             if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
                 for (int b = 0; b < apr && !ok; b++) {
@@ -217,16 +227,27 @@ __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4*
     if (C.use_cells) {
         const int cx = cell_coord(pa[0].x, C.nc[0]), cy = cell_coord(pa[0].y, C.nc[1]), cz = cell_coord(pa[0].z, C.nc[2]);
         for (int dz = -2; dz <= 2; dz++)
-            for (int dy = -2; dy <= 2; dy++)
-                for (int dx = -2; dx <= 2; dx++) {
-                    const int x = (cx + dx + C.nc[0]) % C.nc[0], y = (cy + dy + C.nc[1]) % C.nc[1], z = (cz + dz + C.nc[2]) % C.nc[2];
-                    const int cc = (z * C.nc[1] + y) * C.nc[0] + x;
-                    const int b = starts[cc], e = starts[cc + 1];
-                    for (int base = b; base < e; base += 32) {
-                        const int t = base + lane;
-                        consider(t < e ? g_order[t] : 0, t < e);
+            for (int dy = -2; dy <= 2; dy++) {
+                const int y = (cy + dy + C.nc[1]) % C.nc[1], z = (cz + dz + C.nc[2]) % C.nc[2];
+                const int rowc = (z * C.nc[1] + y) * C.nc[0];
+                // the five x cells of this stencil row, merged into contiguous slot ranges
+                int rb = -1, re = -1;
+                for (int dx = -2; dx <= 3; dx++) {
+                    int b = 0, e = 0;
+                    if (dx <= 2) {
+                        const int x = (cx + dx + C.nc[0]) % C.nc[0];
+                        b = starts[rowc + x];
+                        e = starts[rowc + x + 1];
                     }
+                    if (dx <= 2 && b == re) { re = e; continue; }
+                    for (int base = rb; base >= 0 && base < re; base += 32) {
+                        const int t = base + lane;
+                        consider(t < re ? t : rb, t < re);
+                    }
+                    rb = b;
+                    re = e;
                 }
+            }
     } else {
         for (int base = 0; base < C.nres; base += 32) {
             const int q = base + lane;
@@ -241,11 +262,11 @@ __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4*
 
 // Per-chain binning before a sweep: one CTA per chain, cell starts to global memory.
 __global__ void k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __restrict__ F, uint4* FB, int* g_starts,
-                            int* g_order, int* g_cell, int nchains) {
+                            int* g_order, int* g_cell, uint4* g_pos, int nchains) {
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
-    chain_bin(C, F, FB, g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0, g_cell + C.res0);
+    chain_bin(C, F, FB, g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0, g_cell + C.res0, g_pos + C.res0);
 }
 
 // Lists of every residue of every chain: one warp per residue over the whole GPU.
@@ -253,25 +274,27 @@ template <int APR>
 __global__ void __launch_bounds__(256) k_batch_lists(const ChainDev* __restrict__ chains, BatchGeom G,
                                                      const uint4* __restrict__ F, const int* __restrict__ res_chain,
                                                      const int* __restrict__ g_starts, const int* __restrict__ g_order,
-                                                     uint16_t* LST, int* NL, ChainState* state, int64_t nres_total) {
+                                                     const uint4* __restrict__ g_pos, uint16_t* LST, int* NL,
+                                                     ChainState* state, int64_t nres_total) {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
         const int c = res_chain[gr];
         const ChainDev& C = chains[c];
         if (APR && C.apr != APR) continue;
         residue_list<APR>(C, G, F + C.atom0, (int)(gr - C.res0), g_starts + (size_t)c * (MAX_CELLS + 1),
-                          g_order + C.res0, LST, NL, &state[c].err);
+                          g_order + C.res0, g_pos + C.res0, LST, NL, &state[c].err);
     }
 }
 
 // In-sweep rebuild of one chain by its own CTA (shared-memory cell starts).
 template <int APR>
 __device__ void chain_rebuild(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ F, uint4* FB,
-                              uint16_t* LST, int* NL, int* s_starts, int* g_order, int* g_cell, int* err_out) {
-    chain_bin(C, F, FB, s_starts, g_order, g_cell);
+                              uint16_t* LST, int* NL, int* s_starts, int* g_order, int* g_cell, uint4* g_pos,
+                              int* err_out) {
+    chain_bin(C, F, FB, s_starts, g_order, g_cell, g_pos);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     (void)lane;
-    for (int r = warp; r < C.nres; r += nw) residue_list<APR>(C, G, F + C.atom0, r, s_starts, g_order, LST, NL, err_out);
+    for (int r = warp; r < C.nres; r += nw) residue_list<APR>(C, G, F + C.atom0, r, s_starts, g_order, g_pos, LST, NL, err_out);
     __syncthreads();
 }
 
@@ -299,7 +322,7 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 template <int APR>
 __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                      uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
-                                                     int* g_cell, ChainState* state, const int* __restrict__ cta_start,
+                                                     int* g_cell, uint4* g_pos, ChainState* state, const int* __restrict__ cta_start,
                                                      const int* __restrict__ cta_chains, int nchains) {
     __shared__ Proposal P;
     __shared__ float2 s_red[8];
@@ -384,7 +407,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
         }
         __syncthreads();
         if (P.rebuild) {  // requested by the previous accepted move
-            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
             if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
             __syncthreads();
         }
@@ -399,20 +422,27 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
         const int nl = NL[C.res0 + res];
         float acc = 0.0f;
         int np = 0;
-        for (int e = tid; e < nl; e += blockDim.x) {
-            const int q = row[e];
+        // one neighbour atom per thread and step; an atom farther than rc + extent + largest move
+        // from the moved residue's first atom cannot be within rc of any of its atoms, old or new
+        for (int t = tid; t < nl * apr; t += blockDim.x) {
+            const int q = row[t / apr];
+            const int b = t - (t / apr) * apr;
+            const uint4 pb = Fc[q * apr + b];
+            const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
+                        d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
+            if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
 #pragma unroll
-            for (int b = 0; b < (APR ? APR : MAX_APR); b++) {
-                if (b >= apr) break;
-                const uint4 pb = Fc[q * apr + b];
-#pragma unroll
-                for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
-                    if (k >= apr) break;
-                    const float4 t = s_tab[fo[k].w][pb.w];
-                    // d_old = b - a_old, d_new = b - a_new = d_old - m
-                    acc += mixed_pair_delta(fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]), fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]),
-                                            fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]), m[k][0], m[k][1], m[k][2], t.x, t.y, t.z, cut, np);
+            for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
+                if (k >= apr) break;
+                const float4 tb = s_tab[fo[k].w][pb.w];
+                float dx = d0x, dy = d0y, dz = d0z;
+                if (k > 0) {
+                    dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
+                    dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
+                    dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
                 }
+                // d_old = b - a_old, d_new = b - a_new = d_old - m
+                acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
             }
         }
         npairs += np;
@@ -475,7 +505,7 @@ __global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict_
     }
     __syncthreads();
     if (P.rebuild) {
-        chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, &s_err);
+        chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
         if (tid == 0) S.rebuilds++;
     }
     {
@@ -679,6 +709,7 @@ struct mcg_batch {
     uint4 *d_F = nullptr, *d_FB = nullptr;
     uint16_t* d_LST = nullptr;
     int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr, *d_gstarts = nullptr, *d_res_chain = nullptr;
+    uint4* d_gpos = nullptr;      // first-atom positions in cell order (list builds)
     double* d_prm = nullptr;
     int* d_tile_chain = nullptr;
     int* d_tile_first = nullptr;
@@ -694,7 +725,7 @@ struct mcg_batch {
     ~mcg_batch() {
         if (graph) cudaGraphExecDestroy(graph);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
-                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start};
+                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -702,14 +733,14 @@ struct mcg_batch {
     }
     // list rebuild of every chain: per-chain binning, then one warp per residue over the GPU
     int launch_build(cudaStream_t st) {
-        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, nchains);
+        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, d_gpos, nchains);
         const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_lists<3><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
+            k_batch_lists<3><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
         else if (apr_all == 1)
-            k_batch_lists<1><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
+            k_batch_lists<1><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
         else
-            k_batch_lists<0><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_LST, d_NL, d_state, nres);
+            k_batch_lists<0><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
         BK(cudaGetLastError());
         launches += 2;
         return MCG_OK;
@@ -746,11 +777,11 @@ struct mcg_batch {
     }
     int launch_sweep(cudaStream_t st) {
         if (apr_all == 3)
-            k_batch_sweep<3><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<3><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
         else if (apr_all == 1)
-            k_batch_sweep<1><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<1><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
         else
-            k_batch_sweep<0><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<0><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
         BK(cudaGetLastError());
         return MCG_OK;
     }
@@ -880,6 +911,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     // the cutoff only while rc + |m| <= L/2 (m: the largest move of one atom)
     const double span = span_max + 0.01;   // rigid residues keep their intra-residue distances
     const double mmax = std::max((double)opts->dmax_trn, 2.0 * span * std::sin(0.5 * opts->dmax_rot * PI / 180.0)) + 1e-6;
+    G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
     for (auto& C : B->chains) {
         for (int k = 0; k < 3; k++) {
             if (rc + mmax > 0.5 * C.L[k])
@@ -942,7 +974,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         (r = balloc(&B->d_M, atom0)) || (r = balloc(&B->d_F, atom0)) || (r = balloc(&B->d_FB, atom0)) ||
         (r = balloc(&B->d_LST, (size_t)res0 * G.cap)) || (r = balloc(&B->d_NL, res0)) || (r = balloc(&B->d_gorder, res0)) ||
         (r = balloc(&B->d_gcell, res0)) || (r = balloc(&B->d_prm, prm.size())) ||
-        (r = balloc(&B->d_gstarts, (size_t)nchains * (MAX_CELLS + 1))) || (r = balloc(&B->d_res_chain, res0)))
+        (r = balloc(&B->d_gstarts, (size_t)nchains * (MAX_CELLS + 1))) || (r = balloc(&B->d_res_chain, res0)) ||
+        (r = balloc(&B->d_gpos, res0)))
         return r;
     {
         std::vector<int> rcn(res0);
