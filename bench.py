@@ -222,7 +222,8 @@ def run_ours(args):
         return float(t.item())
 
     chains = make_chains(rank, args.chains)
-    B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank)
+    B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank,
+                    threads_per_chain=args.threads, ctas_per_sm=args.ctas_per_sm)
     natoms = B.natoms
     B.sweep(args.warmup)
     barrier()
@@ -325,6 +326,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work per sampled chain")
     ap.add_argument("--ref-budget", type=float, default=3.0, help="seconds per sampled chain per reference step")
     ap.add_argument("--plain-steps", type=int, default=2000)
+    ap.add_argument("--threads", type=int, default=0, help="threads per chain CTA (0 = library default)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()

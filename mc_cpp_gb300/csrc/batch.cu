@@ -191,8 +191,8 @@ __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4*
                              const uint4* __restrict__ g_pos, uint16_t* LST, int* NL, int* err_out) {
     const int apr = APR ? APR : C.apr;
     const int lane = threadIdx.x & 31;
-    uint4 pa[APR ? APR : MAX_APR];
-    for (int k = 0; k < apr; k++) pa[k] = Fc[r * apr + k];
+    uint4 pa[1];
+    pa[0] = Fc[r * apr];
     uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
     int cnt = 0;
     // cells: `slot` indexes the cell-sorted arrays; otherwise it is the residue itself
@@ -206,16 +206,9 @@ __device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4*
         }
         if (valid && q != r) {
             const float dx = fdelta(pa[0].x, pq.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2], C.Lsl[2]);
-            if (dx * dx + dy * dy + dz * dz <= G.rcent2) {
-                for (int b = 0; b < apr && !ok; b++) {
-                    const uint4 pb = Fc[q * apr + b];
-                    for (int k = 0; k < apr; k++) {
-                        const float ex = fdelta(pa[k].x, pb.x, C.Ls[0], C.Lsl[0]), ey = fdelta(pa[k].y, pb.y, C.Ls[1], C.Lsl[1]),
-                                    ez = fdelta(pa[k].z, pb.z, C.Ls[2], C.Lsl[2]);
-                        if (ex * ex + ey * ey + ez * ez <= G.rlist2) { ok = true; break; }
-                    }
-                }
-            }
+            // first atoms within rc + skin + 2 extents: a superset of the residues with an atom pair
+            // within rc + skin, found with one distance per candidate
+            ok = dx * dx + dy * dy + dz * dz <= G.rcent2;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, ok);
         if (ok) {
@@ -303,10 +296,13 @@ struct Proposal {
     uint4 fo[MAX_APR], fn[MAX_APR];
     unsigned long long mn[MAX_APR][3];   // new master coordinates
     float m[MAX_APR][3];                 // fn - fo in Angstrom (exact mirror difference)
+    uint4 fb[MAX_APR];                   // build positions of the moved atoms
     int res;
     float lna;                           // -ln(alpha), FP32 estimate
     double alpha;                        // alpha in (0, 1]
     int rebuild;
+    int prev_res, prev_acc;              // the previous move, and whether it was committed
+    uint4 prev_fn[MAX_APR];              // its committed mirror positions
 };
 
 // Master-unit increment for a displacement d (Angstrom): d * 2^64 / L as a 64-bit integer, formed
@@ -319,209 +315,238 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
     return ((unsigned long long)(long long)hi << 32) + lo;
 }
 
-template <int APR>
-__global__ void __launch_bounds__(256) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
-                                                     uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
-                                                     int* g_cell, uint4* g_pos, ChainState* state, const int* __restrict__ cta_start,
-                                                     const int* __restrict__ cta_chains, int nchains) {
+// One move = [every thread: residue of the move from the Philox stream, prefetch of its first
+// neighbour atom | warp 0: the proposal] -> barrier -> dE over the neighbour list -> barrier ->
+// warp 0: Metropolis test and commit.  Prefetching before the first barrier takes the three
+// dependent global loads (list length, list entry, neighbour coordinates) off the critical path;
+// a neighbour that belongs to the residue committed by the previous move may have been read
+// before that commit landed, so its positions are taken from the previous proposal instead.
+template <int APR, int NT>
+__global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
+                                                       uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
+                                                       int* g_cell, uint4* g_pos, ChainState* state,
+                                                       const int* __restrict__ cta_start,
+                                                       const int* __restrict__ cta_chains, int nchains) {
+    constexpr int NW = NT / 32;
     __shared__ Proposal P;
-    __shared__ float2 s_red[8];
+    __shared__ float2 s_red[NW];
     __shared__ int s_cell[MAX_CELLS + 1];
     __shared__ int s_err;
     __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    __shared__ unsigned long long s_pairs;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // this CTA's chains, largest first (host-side longest-processing-time packing)
     for (int slot = cta_start[blockIdx.x]; slot < cta_start[blockIdx.x + 1]; slot++) {
-    const int c = cta_chains[slot];
-    if (c >= nchains) continue;
-    const ChainDev& C = chains[c];
-    if (APR && C.apr != APR) continue;
-    const int apr = APR ? APR : C.apr;
-    __syncthreads();   // the previous chain's last reads of the shared tables are done
-    for (int k = tid; k < MAX_APR * MAX_APR; k += blockDim.x)
-        s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
-                                                      C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
-    CutDev cut;
-    cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
-    cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
-    ChainState S = state[c];
-    if (tid == 0) { s_err = 0; P.rebuild = 0; }
-    __syncthreads();
-    const int nmoves = C.nres;
-    long long npairs = 0;
-    uint4* Fc = F + C.atom0;
-    ulonglong4* Mc = M + C.atom0;
-    for (int mv = 0; mv < nmoves; mv++) {
-        const unsigned long long cnt = S.moves + (unsigned long long)mv;
-        if (warp == 0) {
-            // ---- proposal: lanes 0..apr-1 own one atom each; FP32 and integer work only
-            __syncwarp();
+        const int c = cta_chains[slot];
+        if (c >= nchains) continue;
+        const ChainDev& C = chains[c];
+        if (APR && C.apr != APR) continue;
+        const int apr = APR ? APR : C.apr;
+        __syncthreads();   // the previous chain's last reads of shared state are done
+        for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
+            s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
+                                                          C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
+        CutDev cut;
+        cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
+        cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
+        ChainState S = state[c];
+        if (tid == 0) { s_err = 0; P.rebuild = 0; P.prev_res = -1; P.prev_acc = 0; s_pairs = 0ull; }
+        __syncthreads();
+        const int nmoves = C.nres;
+        long long npairs = 0;
+        uint4* Fc = F + C.atom0;
+        ulonglong4* Mc = M + C.atom0;
+        for (int mv = 0; mv < nmoves; mv++) {
+            const unsigned long long cnt = S.moves + (unsigned long long)mv;
             const U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
-            const U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
-            const bool rot = C.ntypes_move == 2 && (r0.x & 1u);
             const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
-            const int piv = (int)(((uint64_t)r0.z * (uint64_t)apr) >> 32);
-            const float ct = 2.0f * u01f(r0.w) - 1.0f;   // uniform direction: cos(theta), phi
-            const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
-            float sphi, cphi;
-            sincospif(2.0f * u01f(r1.x), &sphi, &cphi);
-            const float ux = st * cphi, uy = st * sphi, uz = ct;
-            if (lane < apr) {
-                const int a = res * apr + lane;
-                const uint4 fo = Fc[a];
-                const ulonglong4 mo = Mc[a];
-                float dx, dy, dz;
-                if (!rot) {
-                    const float rad = C.dmax_trn * cbrtf(u01f(r1.y));
-                    dx = rad * ux; dy = rad * uy; dz = rad * uz;
-                } else {
-                    // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
-                    // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
-                    float sh, ch;
-                    sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
-                    const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
-                    const uint4 fp = Fc[res * apr + piv];
-                    const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]), oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
-                    const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
-                    dx = qw * tx + (qy * tz - qz * ty);
-                    dy = qw * ty + (qz * tx - qx * tz);
-                    dz = qw * tz + (qx * ty - qy * tx);
+            // prefetch this thread's first neighbour atom (valid unless the lists are rebuilt below)
+            const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
+            int nl = NL[C.res0 + res];
+            int q0 = 0;
+            uint4 pb0 = make_uint4(0, 0, 0, 0);
+            if (tid < nl * apr) {
+                q0 = row[tid / apr];
+                pb0 = Fc[q0 * apr + (tid - (tid / apr) * apr)];
+            }
+            if (warp == 0) {
+                // ---- proposal: lanes 0..apr-1 own one atom each; FP32 and integer work only
+                __syncwarp();
+                const U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
+                const bool rot = C.ntypes_move == 2 && (r0.x & 1u);
+                const int piv = (int)(((uint64_t)r0.z * (uint64_t)apr) >> 32);
+                const float ct = 2.0f * u01f(r0.w) - 1.0f;   // uniform direction: cos(theta), phi
+                const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                float sphi, cphi;
+                sincospif(2.0f * u01f(r1.x), &sphi, &cphi);
+                const float ux = st * cphi, uy = st * sphi, uz = ct;
+                if (lane < apr) {
+                    const int a = res * apr + lane;
+                    const uint4 fo = Fc[a];
+                    const ulonglong4 mo = Mc[a];
+                    const uint4 fb = FB[C.atom0 + a];
+                    float dx, dy, dz;
+                    if (!rot) {
+                        const float rad = C.dmax_trn * cbrtf(u01f(r1.y));
+                        dx = rad * ux; dy = rad * uy; dz = rad * uz;
+                    } else {
+                        // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
+                        // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
+                        float sh, ch;
+                        sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
+                        const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
+                        const uint4 fp = Fc[res * apr + piv];
+                        const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]),
+                                    oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
+                        const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
+                        dx = qw * tx + (qy * tz - qz * ty);
+                        dy = qw * ty + (qz * tx - qx * tz);
+                        dz = qw * tz + (qx * ty - qy * tx);
+                    }
+                    const unsigned long long nx = mo.x + master_step(dx, C.tofix32[0]);
+                    const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
+                    const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
+                    const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
+                    P.fo[lane] = fo;
+                    P.fn[lane] = fn;
+                    P.fb[lane] = fb;
+                    P.mn[lane][0] = nx; P.mn[lane][1] = ny; P.mn[lane][2] = nz;
+                    P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
+                    P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
+                    P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
                 }
-                const unsigned long long nx = mo.x + master_step(dx, C.tofix32[0]);
-                const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
-                const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
-                const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
-                P.fo[lane] = fo;
-                P.fn[lane] = fn;
-                P.mn[lane][0] = nx; P.mn[lane][1] = ny; P.mn[lane][2] = nz;
-                P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
-                P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
-                P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
+                if (lane == 0) {
+                    P.res = res;
+                    const double alpha = u01d_open0(r1.z, r1.w);
+                    P.alpha = alpha;
+                    P.lna = -__logf((float)alpha);
+                }
             }
-            if (lane == 0) {
-                P.res = res;
-                const double alpha = u01d_open0(r1.z, r1.w);
-                P.alpha = alpha;
-                P.lna = -__logf((float)alpha);
-            }
-        }
-        __syncthreads();
-        if (P.rebuild) {  // requested by the previous accepted move
-            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
-            if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
             __syncthreads();
-        }
-        // ---- dE over the residue's neighbour list
-        const int res = P.res;
-        uint4 fo[APR ? APR : MAX_APR];
-        float m[APR ? APR : MAX_APR][3];
-#pragma unroll
-        for (int k = 0; k < (APR ? APR : MAX_APR); k++)
-            if (k < apr) { fo[k] = P.fo[k]; m[k][0] = P.m[k][0]; m[k][1] = P.m[k][1]; m[k][2] = P.m[k][2]; }
-        const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
-        const int nl = NL[C.res0 + res];
-        float acc = 0.0f;
-        int np = 0;
-        // one neighbour atom per thread and step; an atom farther than rc + extent + largest move
-        // from the moved residue's first atom cannot be within rc of any of its atoms, old or new
-        for (int t = tid; t < nl * apr; t += blockDim.x) {
-            const int q = row[t / apr];
-            const int b = t - (t / apr) * apr;
-            const uint4 pb = Fc[q * apr + b];
-            const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
-                        d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
-            if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
-#pragma unroll
-            for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
-                if (k >= apr) break;
-                const float4 tb = s_tab[fo[k].w][pb.w];
-                float dx = d0x, dy = d0y, dz = d0z;
-                if (k > 0) {
-                    dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
-                    dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
-                    dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
+            if (P.rebuild) {  // requested by the previous accepted move: lists and prefetch are stale
+                chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
+                if (warp == 0 && lane < apr) P.fb[lane] = FB[C.atom0 + res * apr + lane];
+                if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
+                __syncthreads();
+                nl = NL[C.res0 + res];
+                if (tid < nl * apr) {
+                    q0 = row[tid / apr];
+                    pb0 = Fc[q0 * apr + (tid - (tid / apr) * apr)];
                 }
-                // d_old = b - a_old, d_new = b - a_new = d_old - m
-                acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
             }
-        }
-        npairs += np;
-        // float-float warp reduction (TwoSum), then across warps by warp 0
-        float hi = acc, lo = 0.0f;
+            // ---- dE over the residue's neighbour list
+            uint4 fo[APR ? APR : MAX_APR];
+            float m[APR ? APR : MAX_APR][3];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
-            float s, e;
-            two_sum(hi, oh, s, e);
-            hi = s;
-            lo = lo + ol + e;
-        }
-        if (lane == 0) s_red[warp] = make_float2(hi, lo);
-        __syncthreads();
-        if (warp == 0) {
-            float2 v = lane < nw ? s_red[lane] : make_float2(0.f, 0.f);
-            hi = v.x; lo = v.y;
+            for (int k = 0; k < (APR ? APR : MAX_APR); k++)
+                if (k < apr) { fo[k] = P.fo[k]; m[k][0] = P.m[k][0]; m[k][1] = P.m[k][1]; m[k][2] = P.m[k][2]; }
+            const int prev = P.prev_acc ? P.prev_res : -1;
+            float acc = 0.0f;
+            int np = 0;
+            // one neighbour atom per thread and step; an atom farther than rc + extent + largest
+            // move from the moved residue's first atom cannot be within rc of any of its atoms
+            for (int t = tid; t < nl * apr; t += NT) {
+                int q;
+                uint4 pb;
+                const int b = t - (t / apr) * apr;
+                if (t == tid) { q = q0; pb = pb0; }
+                else { q = row[t / apr]; pb = Fc[q * apr + b]; }
+                if (q == prev) pb = P.prev_fn[b];
+                const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
+                            d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
+                if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
 #pragma unroll
-            for (int o = 4; o > 0; o >>= 1) {
+                for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
+                    if (k >= apr) break;
+                    const float4 tb = s_tab[fo[k].w][pb.w];
+                    float dx = d0x, dy = d0y, dz = d0z;
+                    if (k > 0) {
+                        dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
+                        dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
+                        dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
+                    }
+                    // d_old = b - a_old, d_new = b - a_new = d_old - m
+                    acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
+                }
+            }
+            npairs += np;
+            // float-float warp reduction (TwoSum), then across warps by warp 0
+            float hi = acc, lo = 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
                 const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
-                float s, e;
-                two_sum(hi, oh, s, e);
-                hi = s;
+                float sm, e;
+                two_sum(hi, oh, sm, e);
+                hi = sm;
                 lo = lo + ol + e;
             }
-            // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in FP32
-            // when the margin is clear and in FP64 otherwise
-            bool accept;
-            double de = 0.0;
-            if (lane == 0) {
-                de = (double)hi + (double)lo;
-                if (de <= 2.220446049250313e-16) accept = true;
-                else {
-                    const double t = C.beta * de;
-                    const float tf = (float)t;
-                    if (tf < P.lna - 1e-4f * fmaxf(1.0f, P.lna)) accept = true;
-                    else if (tf > P.lna + 1e-4f * fmaxf(1.0f, P.lna)) accept = false;
-                    else accept = P.alpha < exp(-t);
+            if (lane == 0) s_red[warp] = make_float2(hi, lo);
+            __syncthreads();
+            if (warp == 0) {
+                const float2 v = lane < NW ? s_red[lane] : make_float2(0.f, 0.f);
+                hi = v.x; lo = v.y;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    if (o >= NW) continue;
+                    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+                    float sm, e;
+                    two_sum(hi, oh, sm, e);
+                    hi = sm;
+                    lo = lo + ol + e;
+                }
+                // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in FP32
+                // when the margin is clear and in FP64 otherwise
+                bool accept = false;
+                double de = 0.0;
+                if (lane == 0) {
+                    de = (double)hi + (double)lo;
+                    if (de <= 2.220446049250313e-16) accept = true;
+                    else {
+                        const double tt = C.beta * de;
+                        const float tf = (float)tt;
+                        if (tf < P.lna - 1e-4f * fmaxf(1.0f, P.lna)) accept = true;
+                        else if (tf > P.lna + 1e-4f * fmaxf(1.0f, P.lna)) accept = false;
+                        else accept = P.alpha < exp(-tt);
+                    }
+                }
+                accept = __shfl_sync(0xffffffffu, accept, 0);
+                bool far = false;
+                if (lane < apr) {
+                    if (accept) {
+                        const int a = res * apr + lane;
+                        Mc[a] = make_ulonglong4(P.mn[lane][0], P.mn[lane][1], P.mn[lane][2], 0ull);
+                        Fc[a] = P.fn[lane];
+                        const uint4 bpos = P.fb[lane];
+                        const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0], C.Lsl[0]);
+                        const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1], C.Lsl[1]);
+                        const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2], C.Lsl[2]);
+                        far = ex * ex + ey * ey + ez * ez > G.half_skin2;
+                    }
+                    P.prev_fn[lane] = P.fn[lane];
+                }
+                if (__any_sync(0xffffffffu, far) && lane == 0) P.rebuild = 1;
+                if (lane == 0) {
+                    P.prev_res = res;
+                    P.prev_acc = accept ? 1 : 0;
+                    S.trials++;
+                    if (accept) { S.accepted++; S.etot += de; }
                 }
             }
-            accept = __shfl_sync(0xffffffffu, accept, 0);
-            bool far = false;
-            if (accept && lane < apr) {
-                const int a = res * apr + lane;
-                Mc[a] = make_ulonglong4(P.mn[lane][0], P.mn[lane][1], P.mn[lane][2], 0ull);
-                Fc[a] = P.fn[lane];
-                const uint4 bpos = FB[C.atom0 + a];
-                const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0], C.Lsl[0]);
-                const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1], C.Lsl[1]);
-                const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2], C.Lsl[2]);
-                far = ex * ex + ey * ey + ez * ez > G.half_skin2;
-            }
-            if (__any_sync(0xffffffffu, far) && lane == 0) P.rebuild = 1;
-            if (lane == 0) {
-                S.trials++;
-                if (accept) { S.accepted++; S.etot += de; }
-            }
         }
-    }
-    __syncthreads();
-    if (P.rebuild) {
-        chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
-        if (tid == 0) S.rebuilds++;
-    }
-    {
-        __shared__ unsigned long long s_pairs;
-        if (tid == 0) s_pairs = 0ull;
         __syncthreads();
+        if (P.rebuild) {
+            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
+            if (tid == 0) S.rebuilds++;
+        }
         for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
         if (lane == 0) atomicAdd(&s_pairs, (unsigned long long)npairs);
         __syncthreads();
-        if (tid == 0) S.pairs += (long long)s_pairs;
-    }
-    if (tid == 0) {
-        S.moves += (unsigned long long)nmoves;
-        if (s_err) S.err = s_err;
-        state[c] = S;
-    }
+        if (tid == 0) {
+            S.pairs += (long long)s_pairs;
+            S.moves += (unsigned long long)nmoves;
+            if (s_err) S.err = s_err;
+            state[c] = S;
+        }
     }  // chains of this CTA
 }
 
@@ -775,14 +800,23 @@ struct mcg_batch {
         if (ie != cudaSuccess) return fail(MCG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
         return MCG_OK;
     }
-    int launch_sweep(cudaStream_t st) {
-        if (apr_all == 3)
-            k_batch_sweep<3><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
-        else if (apr_all == 1)
-            k_batch_sweep<1><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
+    template <int APR>
+    void sweep_kernel(cudaStream_t st) {
+        if (threads == 512)
+            k_batch_sweep<APR, 512><<<ncta, 512, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
+                                                          d_state, d_cta_start, d_order, nchains);
+        else if (threads == 128)
+            k_batch_sweep<APR, 128><<<ncta, 128, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
+                                                          d_state, d_cta_start, d_order, nchains);
         else
-            k_batch_sweep<0><<<ncta, threads, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos, d_state, d_cta_start, d_order, nchains);
-        BK(cudaGetLastError());
+            k_batch_sweep<APR, 256><<<ncta, 256, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
+                                                          d_state, d_cta_start, d_order, nchains);
+    }
+    int launch_sweep(cudaStream_t st) {
+        if (apr_all == 3) sweep_kernel<3>(st);
+        else if (apr_all == 1) sweep_kernel<1>(st);
+        else sweep_kernel<0>(st);
+    BK(cudaGetLastError());
         return MCG_OK;
     }
 };
@@ -931,8 +965,9 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         G.cap = std::min((G.cap + 31) & ~31, ((maxres + 31) & ~31) + 32);
     }
     if (G.cap > 65535) G.cap = 65535;
-    B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 256;
-    if (B->threads % 32 || B->threads > 256 || B->threads < 64) return fail(MCG_EINVAL, "threads_per_chain must be a multiple of 32 in [64, 256]");
+    B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 512;
+    if (B->threads != 128 && B->threads != 256 && B->threads != 512)
+        return fail(MCG_EINVAL, "threads_per_chain must be 128, 256 or 512");
     // Longest-processing-time packing of chains onto persistent CTAs (one per SM): the cost of a
     // chain's sweep is its move count times the pairs one move touches.  The largest chains get a
     // CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
