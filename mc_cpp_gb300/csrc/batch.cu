@@ -321,7 +321,7 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // dependent global loads (list length, list entry, neighbour coordinates) off the critical path;
 // a neighbour that belongs to the residue committed by the previous move may have been read
 // before that commit landed, so its positions are taken from the previous proposal instead.
-template <int APR, int NT>
+template <int APR, int NT, int PF = (NT >= 512 ? 4 : 8)>
 __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
@@ -360,14 +360,21 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
             const unsigned long long cnt = S.moves + (unsigned long long)mv;
             const U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
             const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
-            // prefetch this thread's first neighbour atom (valid unless the lists are rebuilt below)
+            // prefetch this thread's first PF neighbour atoms (valid unless the lists are rebuilt
+            // below), all loads in flight together
             const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
             int nl = NL[C.res0 + res];
-            int q0 = 0;
-            uint4 pb0 = make_uint4(0, 0, 0, 0);
-            if (tid < nl * apr) {
-                q0 = row[tid / apr];
-                pb0 = Fc[q0 * apr + (tid - (tid / apr) * apr)];
+            int qp[PF];
+            uint4 pbp[PF];
+#pragma unroll
+            for (int u = 0; u < PF; u++) {
+                const int t = tid + u * NT;
+                qp[u] = t < nl * apr ? row[t / apr] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < PF; u++) {
+                const int t = tid + u * NT;
+                pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
             }
             if (warp == 0) {
                 // ---- proposal: lanes 0..apr-1 own one atom each; FP32 and integer work only
@@ -380,9 +387,12 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 float sphi, cphi;
                 sincospif(2.0f * u01f(r1.x), &sphi, &cphi);
                 const float ux = st * cphi, uy = st * sphi, uz = ct;
+                const int a = res * apr + (lane < apr ? lane : 0);
+                const uint4 fo = Fc[a];
+                // pivot atom of a rotation: owned by lane piv
+                const uint4 fp = make_uint4(__shfl_sync(0xffffffffu, fo.x, piv), __shfl_sync(0xffffffffu, fo.y, piv),
+                                            __shfl_sync(0xffffffffu, fo.z, piv), 0u);
                 if (lane < apr) {
-                    const int a = res * apr + lane;
-                    const uint4 fo = Fc[a];
                     const ulonglong4 mo = Mc[a];
                     const uint4 fb = FB[C.atom0 + a];
                     float dx, dy, dz;
@@ -395,7 +405,6 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                         float sh, ch;
                         sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
                         const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
-                        const uint4 fp = Fc[res * apr + piv];
                         const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]),
                                     oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
                         const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
@@ -429,9 +438,11 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
                 __syncthreads();
                 nl = NL[C.res0 + res];
-                if (tid < nl * apr) {
-                    q0 = row[tid / apr];
-                    pb0 = Fc[q0 * apr + (tid - (tid / apr) * apr)];
+#pragma unroll
+                for (int u = 0; u < PF; u++) {
+                    const int t = tid + u * NT;
+                    qp[u] = t < nl * apr ? row[t / apr] : 0;
+                    pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
                 }
             }
             // ---- dE over the residue's neighbour list
@@ -445,12 +456,16 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
             int np = 0;
             // one neighbour atom per thread and step; an atom farther than rc + extent + largest
             // move from the moved residue's first atom cannot be within rc of any of its atoms
-            for (int t = tid; t < nl * apr; t += NT) {
+#pragma unroll 1
+            for (int t = tid, u = 0; t < nl * apr; t += NT, u++) {
                 int q;
                 uint4 pb;
                 const int b = t - (t / apr) * apr;
-                if (t == tid) { q = q0; pb = pb0; }
-                else { q = row[t / apr]; pb = Fc[q * apr + b]; }
+                if (u < PF) {
+                    // static indices into the prefetch registers
+#pragma unroll
+                    for (int v = 0; v < PF; v++) if (v == u) { q = qp[v]; pb = pbp[v]; }
+                } else { q = row[t / apr]; pb = Fc[q * apr + b]; }
                 if (q == prev) pb = P.prev_fn[b];
                 const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
                             d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
