@@ -154,6 +154,7 @@ typedef struct mcg_batch_opts {
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
+    int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4 */
 } mcg_batch_opts;
 
 /* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */

@@ -85,6 +85,7 @@ struct ChainDev {
     float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
+    int kspec;            // moves evaluated together by the sweep (1, 2 or 4)
     float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
     double beta;
     float dmax_trn, dmax_rot;
@@ -110,6 +111,7 @@ struct BatchGeom {
     float half_skin2;  // (skin/2)^2
     float cellmin;     // cell edge for the 5-stencil
     float skip2;       // (rc + extent from the first atom + largest move)^2: dE prefilter
+    float indep2;      // (rc + 2 extents + 2 largest moves)^2: two moves cannot interact beyond it
     int cap;
 };
 
@@ -300,10 +302,9 @@ struct Proposal {
     int res;
     float lna;                           // -ln(alpha), FP32 estimate
     double alpha;                        // alpha in (0, 1]
-    int rebuild;
-    int prev_res, prev_acc;              // the previous move, and whether it was committed
-    uint4 prev_fn[MAX_APR];              // its committed mirror positions
 };
+
+constexpr int KSPEC = 4;                 // moves evaluated together, at most
 
 // Master-unit increment for a displacement d (Angstrom): d * 2^64 / L as a 64-bit integer, formed
 // in FP32 + integer arithmetic (v = d * 2^32 / L; integer part -> high word, fraction -> low word).
@@ -315,12 +316,19 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
     return ((unsigned long long)(long long)hi << 32) + lo;
 }
 
-// One move = [every thread: residue of the move from the Philox stream, prefetch of its first
-// neighbour atom | warp 0: the proposal] -> barrier -> dE over the neighbour list -> barrier ->
-// warp 0: Metropolis test and commit.  Prefetching before the first barrier takes the three
-// dependent global loads (list length, list entry, neighbour coordinates) off the critical path;
-// a neighbour that belongs to the residue committed by the previous move may have been read
-// before that commit landed, so its positions are taken from the previous proposal instead.
+// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2 or 4
+// per chain, from its box size); thread group g (NT/K threads) evaluates move mv+g.  Moves mv..mv+n-1
+// are applied when their residues are pairwise out of interaction range for any combination of
+// old and new positions (first-atom distance > rc + 2 extents + 2 largest moves): then each dE is
+// the one the sequential chain would compute, the decisions use the same random numbers, and the
+// result is the sequential Metropolis chain.  The remaining moves are re-proposed next iteration
+// from the same Philox counters.
+//
+// Iteration = [warp 0: the K proposals, one lane per moved atom | every other thread: the residue
+// of its group's move from the Philox stream and a prefetch of its first neighbour atoms]
+// -> barrier -> dE of the independent prefix -> barrier -> warp 0: Metropolis tests and commits.
+// Neighbours that belong to residues committed by the previous iteration may have been read before
+// the commit landed; their positions come from the previous proposals instead.
 template <int APR, int NT, int PF = (NT >= 512 ? 4 : 8)>
 __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
@@ -328,20 +336,24 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                                                        const int* __restrict__ cta_start,
                                                        const int* __restrict__ cta_chains, int nchains) {
     constexpr int NW = NT / 32;
-    __shared__ Proposal P;
+    __shared__ Proposal P[KSPEC];
     __shared__ float2 s_red[NW];
     __shared__ int s_cell[MAX_CELLS + 1];
-    __shared__ int s_err;
-    __shared__ float4 s_tab[MAX_APR][MAX_APR];   // 16-byte aligned: read as float4
+    __shared__ int s_err, s_rebuild;
+    __shared__ int s_prev_res[KSPEC];                 // residues committed by the previous iteration
+    __shared__ uint4 s_prev_fn[KSPEC][MAX_APR];
+    __shared__ float4 s_tab[MAX_APR][MAX_APR];        // 16-byte aligned: read as float4
     __shared__ unsigned long long s_pairs;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // this CTA's chains, largest first (host-side longest-processing-time packing)
     for (int slot = cta_start[blockIdx.x]; slot < cta_start[blockIdx.x + 1]; slot++) {
         const int c = cta_chains[slot];
         if (c >= nchains) continue;
         const ChainDev& C = chains[c];
         if (APR && C.apr != APR) continue;
         const int apr = APR ? APR : C.apr;
+        const int K = C.kspec;                 // 1, 2 or 4
+        const int GS = NT / K;                 // threads per move
+        const int grp = tid / GS, tg = tid - grp * GS;
         __syncthreads();   // the previous chain's last reads of shared state are done
         for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
             s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
@@ -350,60 +362,69 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
         cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
         cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
         ChainState S = state[c];
-        if (tid == 0) { s_err = 0; P.rebuild = 0; P.prev_res = -1; P.prev_acc = 0; s_pairs = 0ull; }
+        if (tid < KSPEC) s_prev_res[tid] = -1;
+        if (tid == 0) { s_err = 0; s_rebuild = 0; s_pairs = 0ull; }
         __syncthreads();
         const int nmoves = C.nres;
         long long npairs = 0;
         uint4* Fc = F + C.atom0;
         ulonglong4* Mc = M + C.atom0;
-        for (int mv = 0; mv < nmoves; mv++) {
-            const unsigned long long cnt = S.moves + (unsigned long long)mv;
+        int mv = 0;
+        while (mv < nmoves) {
+            const int kk = min(K, nmoves - mv);      // moves proposed this iteration
+            // ---- my group's move: residue and prefetch of its first neighbour atoms
+            const bool gact = grp < kk;
+            const unsigned long long cnt = S.moves + (unsigned long long)(mv + (gact ? grp : 0));
             const U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
             const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
-            // prefetch this thread's first PF neighbour atoms (valid unless the lists are rebuilt
-            // below), all loads in flight together
             const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
-            int nl = NL[C.res0 + res];
+            int nl = gact ? NL[C.res0 + res] : 0;
             int qp[PF];
             uint4 pbp[PF];
 #pragma unroll
             for (int u = 0; u < PF; u++) {
-                const int t = tid + u * NT;
+                const int t = tg + u * GS;
                 qp[u] = t < nl * apr ? row[t / apr] : 0;
             }
 #pragma unroll
             for (int u = 0; u < PF; u++) {
-                const int t = tid + u * NT;
+                const int t = tg + u * GS;
                 pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
             }
             if (warp == 0) {
-                // ---- proposal: lanes 0..apr-1 own one atom each; FP32 and integer work only
+                // ---- the kk proposals: lane = g * apr + k owns atom k of move g's residue
                 __syncwarp();
-                const U4 r1 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
-                const bool rot = C.ntypes_move == 2 && (r0.x & 1u);
-                const int piv = (int)(((uint64_t)r0.z * (uint64_t)apr) >> 32);
-                const float ct = 2.0f * u01f(r0.w) - 1.0f;   // uniform direction: cos(theta), phi
+                const int g = lane / apr, k = lane - g * apr;
+                const bool lact = g < kk;
+                const unsigned long long cg = S.moves + (unsigned long long)(mv + (lact ? g : 0));
+                const U4 q0 = philox4x32_10(U4{(uint32_t)cg, (uint32_t)(cg >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
+                const U4 q1 = philox4x32_10(U4{(uint32_t)cg, (uint32_t)(cg >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
+                const int rg = (int)(((uint64_t)q0.y * (uint64_t)C.nres) >> 32);
+                const bool rot = C.ntypes_move == 2 && (q0.x & 1u);
+                const int piv = (int)(((uint64_t)q0.z * (uint64_t)apr) >> 32);
+                const float ct = 2.0f * u01f(q0.w) - 1.0f;   // uniform direction: cos(theta), phi
                 const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
                 float sphi, cphi;
-                sincospif(2.0f * u01f(r1.x), &sphi, &cphi);
+                sincospif(2.0f * u01f(q1.x), &sphi, &cphi);
                 const float ux = st * cphi, uy = st * sphi, uz = ct;
-                const int a = res * apr + (lane < apr ? lane : 0);
+                const int a = rg * apr + (lact ? k : 0);
                 const uint4 fo = Fc[a];
-                // pivot atom of a rotation: owned by lane piv
-                const uint4 fp = make_uint4(__shfl_sync(0xffffffffu, fo.x, piv), __shfl_sync(0xffffffffu, fo.y, piv),
-                                            __shfl_sync(0xffffffffu, fo.z, piv), 0u);
-                if (lane < apr) {
+                // the rotation pivot is atom piv of the same move, owned by lane g * apr + piv
+                const int pl = min(31, (lact ? g : 0) * apr + piv);
+                const uint4 fp = make_uint4(__shfl_sync(0xffffffffu, fo.x, pl), __shfl_sync(0xffffffffu, fo.y, pl),
+                                            __shfl_sync(0xffffffffu, fo.z, pl), 0u);
+                if (lact && g * apr + k == lane) {
                     const ulonglong4 mo = Mc[a];
                     const uint4 fb = FB[C.atom0 + a];
                     float dx, dy, dz;
                     if (!rot) {
-                        const float rad = C.dmax_trn * cbrtf(u01f(r1.y));
+                        const float rad = C.dmax_trn * cbrtf(u01f(q1.y));
                         dx = rad * ux; dy = rad * uy; dz = rad * uz;
                     } else {
                         // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
                         // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
                         float sh, ch;
-                        sincospif(C.dmax_rot * (2.0f * u01f(r1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
+                        sincospif(C.dmax_rot * (2.0f * u01f(q1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
                         const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
                         const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]),
                                     oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
@@ -416,76 +437,97 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                     const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
                     const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
                     const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
-                    P.fo[lane] = fo;
-                    P.fn[lane] = fn;
-                    P.fb[lane] = fb;
-                    P.mn[lane][0] = nx; P.mn[lane][1] = ny; P.mn[lane][2] = nz;
-                    P.m[lane][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
-                    P.m[lane][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
-                    P.m[lane][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
-                }
-                if (lane == 0) {
-                    P.res = res;
-                    const double alpha = u01d_open0(r1.z, r1.w);
-                    P.alpha = alpha;
-                    P.lna = -__logf((float)alpha);
+                    Proposal& Q = P[g];
+                    Q.fo[k] = fo;
+                    Q.fn[k] = fn;
+                    Q.fb[k] = fb;
+                    Q.mn[k][0] = nx; Q.mn[k][1] = ny; Q.mn[k][2] = nz;
+                    Q.m[k][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
+                    Q.m[k][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
+                    Q.m[k][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
+                    if (k == 0) {
+                        Q.res = rg;
+                        const double alpha = u01d_open0(q1.z, q1.w);
+                        Q.alpha = alpha;
+                        Q.lna = -__logf((float)alpha);
+                    }
                 }
             }
             __syncthreads();
-            if (P.rebuild) {  // requested by the previous accepted move: lists and prefetch are stale
+            if (s_rebuild) {  // requested by the previous iteration: lists and prefetches are stale
                 chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
-                if (warp == 0 && lane < apr) P.fb[lane] = FB[C.atom0 + res * apr + lane];
-                if (tid == 0) { P.rebuild = 0; S.rebuilds++; }
+                if (warp == 0) {
+                    const int g = lane / apr, k = lane - g * apr;
+                    if (g < kk) P[g].fb[k] = FB[C.atom0 + P[g].res * apr + k];
+                }
+                if (tid == 0) { s_rebuild = 0; S.rebuilds++; }
                 __syncthreads();
-                nl = NL[C.res0 + res];
+                nl = gact ? NL[C.res0 + res] : 0;
 #pragma unroll
                 for (int u = 0; u < PF; u++) {
-                    const int t = tid + u * NT;
+                    const int t = tg + u * GS;
                     qp[u] = t < nl * apr ? row[t / apr] : 0;
                     pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
                 }
             }
-            // ---- dE over the residue's neighbour list
-            uint4 fo[APR ? APR : MAX_APR];
-            float m[APR ? APR : MAX_APR][3];
-#pragma unroll
-            for (int k = 0; k < (APR ? APR : MAX_APR); k++)
-                if (k < apr) { fo[k] = P.fo[k]; m[k][0] = P.m[k][0]; m[k][1] = P.m[k][1]; m[k][2] = P.m[k][2]; }
-            const int prev = P.prev_acc ? P.prev_res : -1;
-            float acc = 0.0f;
-            int np = 0;
-            // one neighbour atom per thread and step; an atom farther than rc + extent + largest
-            // move from the moved residue's first atom cannot be within rc of any of its atoms
-#pragma unroll 1
-            for (int t = tid, u = 0; t < nl * apr; t += NT, u++) {
-                int q;
-                uint4 pb;
-                const int b = t - (t / apr) * apr;
-                if (u < PF) {
-                    // static indices into the prefetch registers
-#pragma unroll
-                    for (int v = 0; v < PF; v++) if (v == u) { q = qp[v]; pb = pbp[v]; }
-                } else { q = row[t / apr]; pb = Fc[q * apr + b]; }
-                if (q == prev) pb = P.prev_fn[b];
-                const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
-                            d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
-                if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
-#pragma unroll
-                for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
-                    if (k >= apr) break;
-                    const float4 tb = s_tab[fo[k].w][pb.w];
-                    float dx = d0x, dy = d0y, dz = d0z;
-                    if (k > 0) {
-                        dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
-                        dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
-                        dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
-                    }
-                    // d_old = b - a_old, d_new = b - a_new = d_old - m
-                    acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
+            // ---- independent prefix (every thread computes it from the proposals)
+            int ng = 1;
+            for (int g = 1; g < kk; g++) {
+                bool ok = true;
+                for (int h = 0; h < g && ok; h++) {
+                    if (P[g].res == P[h].res) { ok = false; break; }
+                    const float dx = fdelta(P[h].fo[0].x, P[g].fo[0].x, C.Ls[0], C.Lsl[0]);
+                    const float dy = fdelta(P[h].fo[0].y, P[g].fo[0].y, C.Ls[1], C.Lsl[1]);
+                    const float dz = fdelta(P[h].fo[0].z, P[g].fo[0].z, C.Ls[2], C.Lsl[2]);
+                    ok = dx * dx + dy * dy + dz * dz > G.indep2;
                 }
+                if (!ok) break;
+                ng = g + 1;
             }
-            npairs += np;
-            // float-float warp reduction (TwoSum), then across warps by warp 0
+            // ---- dE of my group's move over its neighbour list
+            float acc = 0.0f;
+            if (grp < ng) {
+                const Proposal& Q = P[grp];
+                uint4 fo[APR ? APR : MAX_APR];
+                float m[APR ? APR : MAX_APR][3];
+#pragma unroll
+                for (int k = 0; k < (APR ? APR : MAX_APR); k++)
+                    if (k < apr) { fo[k] = Q.fo[k]; m[k][0] = Q.m[k][0]; m[k][1] = Q.m[k][1]; m[k][2] = Q.m[k][2]; }
+                int np = 0;
+                // an atom farther than rc + extent + largest move from the moved residue's first atom
+                // cannot be within rc of any of its atoms, old or new
+#pragma unroll 1
+                for (int t = tg, u = 0; t < nl * apr; t += GS, u++) {
+                    int q = 0;
+                    uint4 pb = make_uint4(0, 0, 0, 0);
+                    const int b = t - (t / apr) * apr;
+                    if (u < PF) {
+#pragma unroll
+                        for (int v = 0; v < PF; v++) if (v == u) { q = qp[v]; pb = pbp[v]; }
+                    } else { q = row[t / apr]; pb = Fc[q * apr + b]; }
+#pragma unroll
+                    for (int v = 0; v < KSPEC; v++)
+                        if (v < K && q == s_prev_res[v]) pb = s_prev_fn[v][b];
+                    const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
+                                d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
+                    if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
+#pragma unroll
+                    for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
+                        if (k >= apr) break;
+                        const float4 tb = s_tab[fo[k].w][pb.w];
+                        float dx = d0x, dy = d0y, dz = d0z;
+                        if (k > 0) {
+                            dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
+                            dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
+                            dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
+                        }
+                        // d_old = b - a_old, d_new = b - a_new = d_old - m
+                        acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
+                    }
+                }
+                npairs += np;
+            }
+            // float-float warp reduction (TwoSum); a group's warps are consecutive
             float hi = acc, lo = 0.0f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -498,58 +540,64 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
             if (lane == 0) s_red[warp] = make_float2(hi, lo);
             __syncthreads();
             if (warp == 0) {
-                const float2 v = lane < NW ? s_red[lane] : make_float2(0.f, 0.f);
-                hi = v.x; lo = v.y;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    if (o >= NW) continue;
-                    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
-                    float sm, e;
-                    two_sum(hi, oh, sm, e);
-                    hi = sm;
-                    lo = lo + ol + e;
-                }
-                // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in FP32
-                // when the margin is clear and in FP64 otherwise
-                bool accept = false;
+                // lane g < ng: dE of move g from its group's warp partials, in warp order
+                const int wpg = GS / 32;
                 double de = 0.0;
-                if (lane == 0) {
-                    de = (double)hi + (double)lo;
+                bool accept = false;
+                if (lane < ng) {
+                    float h = 0.0f, l = 0.0f;
+                    for (int w = 0; w < wpg; w++) {
+                        const float2 v = s_red[lane * wpg + w];
+                        float sm, e;
+                        two_sum(h, v.x, sm, e);
+                        h = sm;
+                        l = l + v.y + e;
+                    }
+                    de = (double)h + (double)l;
+                    // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in
+                    // FP32 when the margin is clear and in FP64 otherwise
+                    const Proposal& Q = P[lane];
                     if (de <= 2.220446049250313e-16) accept = true;
                     else {
                         const double tt = C.beta * de;
                         const float tf = (float)tt;
-                        if (tf < P.lna - 1e-4f * fmaxf(1.0f, P.lna)) accept = true;
-                        else if (tf > P.lna + 1e-4f * fmaxf(1.0f, P.lna)) accept = false;
-                        else accept = P.alpha < exp(-tt);
+                        if (tf < Q.lna - 1e-4f * fmaxf(1.0f, Q.lna)) accept = true;
+                        else if (tf > Q.lna + 1e-4f * fmaxf(1.0f, Q.lna)) accept = false;
+                        else accept = Q.alpha < exp(-tt);
                     }
                 }
-                accept = __shfl_sync(0xffffffffu, accept, 0);
+                const unsigned accmask = __ballot_sync(0xffffffffu, accept);
+                // commits: lane = g * apr + k
+                const int g = lane / apr, k = lane - g * apr;
                 bool far = false;
-                if (lane < apr) {
-                    if (accept) {
-                        const int a = res * apr + lane;
-                        Mc[a] = make_ulonglong4(P.mn[lane][0], P.mn[lane][1], P.mn[lane][2], 0ull);
-                        Fc[a] = P.fn[lane];
-                        const uint4 bpos = P.fb[lane];
-                        const float ex = fdelta(bpos.x, P.fn[lane].x, C.Ls[0], C.Lsl[0]);
-                        const float ey = fdelta(bpos.y, P.fn[lane].y, C.Ls[1], C.Lsl[1]);
-                        const float ez = fdelta(bpos.z, P.fn[lane].z, C.Ls[2], C.Lsl[2]);
+                if (g < ng) {
+                    const Proposal& Q = P[g];
+                    if ((accmask >> g) & 1u) {
+                        const int a = Q.res * apr + k;
+                        Mc[a] = make_ulonglong4(Q.mn[k][0], Q.mn[k][1], Q.mn[k][2], 0ull);
+                        Fc[a] = Q.fn[k];
+                        const float ex = fdelta(Q.fb[k].x, Q.fn[k].x, C.Ls[0], C.Lsl[0]);
+                        const float ey = fdelta(Q.fb[k].y, Q.fn[k].y, C.Ls[1], C.Lsl[1]);
+                        const float ez = fdelta(Q.fb[k].z, Q.fn[k].z, C.Ls[2], C.Lsl[2]);
                         far = ex * ex + ey * ey + ez * ez > G.half_skin2;
+                        s_prev_fn[g][k] = Q.fn[k];
                     }
-                    P.prev_fn[lane] = P.fn[lane];
                 }
-                if (__any_sync(0xffffffffu, far) && lane == 0) P.rebuild = 1;
-                if (lane == 0) {
-                    P.prev_res = res;
-                    P.prev_acc = accept ? 1 : 0;
-                    S.trials++;
-                    if (accept) { S.accepted++; S.etot += de; }
+                if (lane < KSPEC) s_prev_res[lane] = (lane < ng && ((accmask >> lane) & 1u)) ? P[lane].res : -1;
+                if (__any_sync(0xffffffffu, far) && lane == 0) s_rebuild = 1;
+                // statistics and the running energy, in move order
+                for (int gg = 0; gg < ng; gg++) {
+                    const double d = __shfl_sync(0xffffffffu, de, gg);
+                    if (lane == 0) {
+                        S.trials++;
+                        if ((accmask >> gg) & 1u) { S.accepted++; S.etot += d; }
+                    }
                 }
             }
+            mv += ng;
         }
         __syncthreads();
-        if (P.rebuild) {
+        if (s_rebuild) {
             chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
             if (tid == 0) S.rebuilds++;
         }
@@ -961,6 +1009,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     const double span = span_max + 0.01;   // rigid residues keep their intra-residue distances
     const double mmax = std::max((double)opts->dmax_trn, 2.0 * span * std::sin(0.5 * opts->dmax_rot * PI / 180.0)) + 1e-6;
     G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
+    const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
+    G.indep2 = (float)(rind * rind);
     for (auto& C : B->chains) {
         for (int k = 0; k < 3; k++) {
             if (rc + mmax > 0.5 * C.L[k])
@@ -968,6 +1018,14 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             C.nc[k] = (int)std::floor(C.L[k] / G.cellmin);
         }
         C.use_cells = (C.nc[0] >= 5 && C.nc[1] >= 5 && C.nc[2] >= 5 && C.nc[0] * C.nc[1] * C.nc[2] <= MAX_CELLS) ? 1 : 0;
+        // speculation width from the chance that two random residues are out of interaction range
+        {
+            const double vol = C.L[0] * C.L[1] * C.L[2];
+            const double frac = 4.0 / 3.0 * PI * rind * rind * rind / vol;
+            const bool any_half = rind > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]));
+            C.kspec = (opts->speculation == 1 || any_half || frac > 0.35) ? 1 : (frac > 0.12 || opts->speculation == 2 ? 2 : 4);
+            if (opts->speculation == 4 && !any_half) C.kspec = 4;
+        }
         if (!C.use_cells) C.nc[0] = C.nc[1] = C.nc[2] = 1;
     }
     if (opts->list_capacity > 0) G.cap = opts->list_capacity;

@@ -147,7 +147,8 @@ class BatchChains:
     """Hundreds of independent NVT chains advanced by one persistent kernel per sweep."""
 
     def __init__(self, chains, dmax_trn: float = 0.15, dmax_rot: float = 15.0, acceptance: str = "physical",
-                 seed: int = 1, threads_per_chain: int = 0, list_capacity: int = 0, ctas_per_sm: int = 0):
+                 seed: int = 1, threads_per_chain: int = 0, list_capacity: int = 0, ctas_per_sm: int = 0,
+                 speculation: int = 0):
         L = native.lib()
         self.nchains = len(chains)
         arr = (native.SystemDesc * self.nchains)()
@@ -157,7 +158,7 @@ class BatchChains:
             arr[k] = d
             self._keep.append(keep)
         opts = native.BatchOpts(dmax_trn, dmax_rot, native.ACCEPT[acceptance], threads_per_chain, list_capacity, seed,
-                                ctas_per_sm)
+                                ctas_per_sm, speculation)
         h = C.c_void_p()
         native.check(L.mcg_batch_create(arr, self.nchains, C.byref(opts), C.byref(h)))
         self.h = h

@@ -148,3 +148,22 @@ def test_invalid_batches_rejected():
     with pytest.raises(native.McgError) as ei:
         BatchChains([small])
     assert ei.value.code == native.MCG_EINVAL
+
+
+def test_speculative_sweep_reproduces_sequential_chain():
+    """Moves evaluated together (speculation 4) must give the sequential chain: same random
+    numbers, same decisions, same coordinates.  dE sums differ only in float summation order, so
+    a decision could flip only at an exact tie (probability ~1e-7 per move)."""
+    ch = _waters((4000, 2600, 1500), seed=31)
+    seq = BatchChains(ch, seed=17, speculation=1)
+    spec = BatchChains(ch, seed=17, speculation=4)
+    seq.sweep(2)
+    spec.sweep(2)
+    t1, a1, e1 = seq.stats()
+    t2, a2, e2 = spec.stats()
+    assert np.array_equal(t1, t2)
+    assert np.abs(a1 - a2).max() <= 1
+    same = [np.array_equal(seq.coords(k), spec.coords(k)) for k in range(len(ch))]
+    assert sum(same) >= len(ch) - 1, same
+    ef = spec.energy_fp64()
+    assert (np.abs(e2 - ef) / np.abs(ef)).max() <= 1e-6
