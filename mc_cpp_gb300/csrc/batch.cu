@@ -490,9 +490,15 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 const Proposal& Q = P[grp];
                 uint4 fo[APR ? APR : MAX_APR];
                 float m[APR ? APR : MAX_APR][3];
+                float off[APR ? APR : MAX_APR][3];   // atom k - atom 0 of the moved residue (old)
 #pragma unroll
                 for (int k = 0; k < (APR ? APR : MAX_APR); k++)
-                    if (k < apr) { fo[k] = Q.fo[k]; m[k][0] = Q.m[k][0]; m[k][1] = Q.m[k][1]; m[k][2] = Q.m[k][2]; }
+                    if (k < apr) {
+                        fo[k] = Q.fo[k]; m[k][0] = Q.m[k][0]; m[k][1] = Q.m[k][1]; m[k][2] = Q.m[k][2];
+                        off[k][0] = fdelta(Q.fo[0].x, Q.fo[k].x, C.Ls[0], C.Lsl[0]);
+                        off[k][1] = fdelta(Q.fo[0].y, Q.fo[k].y, C.Ls[1], C.Lsl[1]);
+                        off[k][2] = fdelta(Q.fo[0].z, Q.fo[k].z, C.Ls[2], C.Lsl[2]);
+                    }
                 int np = 0;
                 // an atom farther than rc + extent + largest move from the moved residue's first atom
                 // cannot be within rc of any of its atoms, old or new
@@ -515,12 +521,10 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                     for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
                         if (k >= apr) break;
                         const float4 tb = s_tab[fo[k].w][pb.w];
-                        float dx = d0x, dy = d0y, dz = d0z;
-                        if (k > 0) {
-                            dx = fdelta(fo[k].x, pb.x, C.Ls[0], C.Lsl[0]);
-                            dy = fdelta(fo[k].y, pb.y, C.Ls[1], C.Lsl[1]);
-                            dz = fdelta(fo[k].z, pb.z, C.Ls[2], C.Lsl[2]);
-                        }
+                        // b - a_k = (b - a_0) - (a_k - a_0)
+                        const float dx = k ? d0x - off[k][0] : d0x;
+                        const float dy = k ? d0y - off[k][1] : d0y;
+                        const float dz = k ? d0z - off[k][2] : d0z;
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
                         acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
                     }

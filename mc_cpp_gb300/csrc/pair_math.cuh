@@ -147,44 +147,41 @@ namespace mcg {
 //   S_b - S_a = sw2 du' [2 A_a^2 - (A_a + A_b) B_b],  A = c2 - u, B = c2 + 2u - 3 n2
 // on the switch polynomial (u clamped to [n2, c2]).  LJ is small at these distances and is
 // differenced directly.  Pairs crossing the cutoff fall back to the direct difference.
-// npair counts pair interactions (inside the cutoff before or after the move).
+// npair counts pair interactions (inside the cutoff before or after the move).  Branch-free
+// apart from the early exit for a pair outside the cutoff both before and after, so a warp whose
+// lanes hold pairs in different regions (inner, switch, crossing the cutoff) does not execute
+// every region's code in turn.
 __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float doz, float mx, float my, float mz,
                                                   float qk, float e4, float ss, const CutDev& c, int& npair) {
     const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
-    const float uo = dox * dox + doy * doy + doz * doz;
-    const float un = dnx * dnx + dny * dny + dnz * dnz;
+    const float uo = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
+    const float un = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
     const bool io = uo <= c.c2f, in = un <= c.c2f;
     if (!io && !in) return 0.0f;
     npair++;
     const float ro = rsqrtf(uo), rn = rsqrtf(un);
-    auto sw = [&](float u) {
-        if (u <= c.n2f) return 1.0f;
-        float a = c.c2f - u;
-        return a * a * (c.c2f + 2.0f * u - 3.0f * c.n2f) * c.sw2f;
-    };
-    auto lj = [&](float u, float r) {
-        float x2 = ss * r * r;
-        float x6 = x2 * x2 * x2;
-        return e4 * (x6 * x6 - x6);
-    };
-    const float so = io ? sw(uo) : 0.0f, sn = in ? sw(un) : 0.0f;
-    float d = (in ? lj(un, rn) * sn : 0.0f) - (io ? lj(uo, ro) * so : 0.0f);
-    if (io && in) {
-        const float du = -(mx * (dox + dnx) + my * (doy + dny) + mz * (doz + dnz));
-        const float p = ro * rn;
-        const float dinv = __fdividef(-du * p * p, ro + rn);   // relative error a few ulp of the change
-        float ds = 0.0f;
-        const float ua = fmaxf(uo, c.n2f), ub = fmaxf(un, c.n2f);
-        if (ua != ub) {
-            const float dd = (uo > c.n2f && un > c.n2f) ? du : (ub - ua);
-            const float Aa = c.c2f - ua, Ab = c.c2f - ub, Bb = c.c2f + 2.0f * ub - 3.0f * c.n2f;
-            ds = c.sw2f * dd * (2.0f * Aa * Aa - (Aa + Ab) * Bb);
-        }
-        d += qk * (dinv * sn + ro * ds);
-    } else {
-        d += (in ? qk * rn * sn : 0.0f) - (io ? qk * ro * so : 0.0f);
-    }
-    return d;
+    // switch S(u) = (c2-u)^2 (c2+2u-3n2) sw2 above n2, 1 below; evaluated on u clamped to [n2, c2]
+    const float ua = fmaxf(uo, c.n2f), ub = fmaxf(un, c.n2f);
+    const float Aa = c.c2f - ua, Ab = c.c2f - ub;
+    const float k3 = c.c2f - 3.0f * c.n2f;
+    const float Ba = fmaf(2.0f, ua, k3), Bb = fmaf(2.0f, ub, k3);
+    const float so = io ? (uo <= c.n2f ? 1.0f : Aa * Aa * Ba * c.sw2f) : 0.0f;
+    const float sn = in ? (un <= c.n2f ? 1.0f : Ab * Ab * Bb * c.sw2f) : 0.0f;
+    // Lennard-Jones, differenced directly (small at these distances)
+    const float xo = ss * (ro * ro), xn = ss * (rn * rn);
+    const float xo3 = xo * xo * xo, xn3 = xn * xn * xn;
+    const float d_lj = fmaf(e4 * fmaf(xn3, xn3, -xn3), sn, -(e4 * fmaf(xo3, xo3, -xo3) * so));
+    // Coulomb: analytic difference when both ends are inside the cutoff
+    //   1/r_new - 1/r_old = -du (rn ro)^2 / (rn + ro),  du = u_new - u_old = -m.(d_old + d_new)
+    //   S_b - S_a = sw2 du' [2 A_a^2 - (A_a + A_b) B_b] on the clamped u (du' = du when both are above n2)
+    const float du = -fmaf(mx, dox + dnx, fmaf(my, doy + dny, mz * (doz + dnz)));
+    const float p = ro * rn;
+    const float dinv = __fdividef(-du * p * p, ro + rn);
+    const float dd = (uo > c.n2f && un > c.n2f) ? du : (ub - ua);
+    const float ds = c.sw2f * dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
+    const float c_both = qk * fmaf(dinv, sn, ro * ds);
+    const float c_one = qk * fmaf(rn, sn, -ro * so);
+    return d_lj + ((io && in) ? c_both : c_one);
 }
 
 }  // namespace mcg
