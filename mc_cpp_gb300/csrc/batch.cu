@@ -86,6 +86,8 @@ struct ChainDev {
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
     int kspec;            // moves evaluated together by the sweep (1, 2 or 4)
+    int wrap_offsets;     // box small enough that (b - a_0) - (a_k - a_0) may leave the minimum image
+    float Lf[3], Lhalf[3];
     float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
     double beta;
     float dmax_trn, dmax_rot;
@@ -521,10 +523,15 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                     for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
                         if (k >= apr) break;
                         const float4 tb = s_tab[fo[k].w][pb.w];
-                        // b - a_k = (b - a_0) - (a_k - a_0)
-                        const float dx = k ? d0x - off[k][0] : d0x;
-                        const float dy = k ? d0y - off[k][1] : d0y;
-                        const float dz = k ? d0z - off[k][2] : d0z;
+                        // b - a_k = (b - a_0) - (a_k - a_0), back to the minimum image in small boxes
+                        float dx = k ? d0x - off[k][0] : d0x;
+                        float dy = k ? d0y - off[k][1] : d0y;
+                        float dz = k ? d0z - off[k][2] : d0z;
+                        if (C.wrap_offsets) {
+                            dx -= (dx > C.Lhalf[0]) ? C.Lf[0] : ((dx < -C.Lhalf[0]) ? -C.Lf[0] : 0.0f);
+                            dy -= (dy > C.Lhalf[1]) ? C.Lf[1] : ((dy < -C.Lhalf[1]) ? -C.Lf[1] : 0.0f);
+                            dz -= (dz > C.Lhalf[2]) ? C.Lf[2] : ((dz < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
+                        }
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
                         acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
                     }
@@ -1022,6 +1029,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             C.nc[k] = (int)std::floor(C.L[k] / G.cellmin);
         }
         C.use_cells = (C.nc[0] >= 5 && C.nc[1] >= 5 && C.nc[2] >= 5 && C.nc[0] * C.nc[1] * C.nc[2] <= MAX_CELLS) ? 1 : 0;
+        for (int k = 0; k < 3; k++) { C.Lf[k] = (float)C.L[k]; C.Lhalf[k] = (float)(0.5 * C.L[k]); }
+        C.wrap_offsets = (rc + rext + mmax + span > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]))) ? 1 : 0;
         // speculation width from the chance that two random residues are out of interaction range
         {
             const double vol = C.L[0] * C.L[1] * C.L[2];

@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         const uint4 fo = P == PREC_MIX ? A.fx[a] : make_uint4(0, 0, 0, 0);
         const uint4 fn = P == PREC_MIX ? s_fx[ka] : make_uint4(0, 0, 0, 0);
         CutDev cutx = cut;   // full mode: no cutoff and no switch
-        if (!sw) { cutx.c2f = 3.0e38f; cutx.n2f = 3.0e38f; }
+        if (!sw) { cutx.c2f = 1.0e30f; cutx.n2f = 1.0e30f; }   // "no cutoff": finite, so c2 - 3 n2 stays finite
         float ma[3] = {0.f, 0.f, 0.f};   // the exact move of a, as the fixed-point mirror sees it
         if (P == PREC_MIX) {
             if (pbc.type != 0) {
