@@ -10,12 +10,17 @@ as it has molecules, in one persistent kernel launch (replayed from a CUDA graph
 synthetic (seeded), the working set (2.1 M atoms, 1.5 GB of neighbour lists) exceeds L2, so no
 flush is needed between steps.
 
-Reported: `value` = accepted moves/s over all GPUs (device time, CUDA events on the library's
-stream, max over ranks); `e2e` = the same through the host-buffer API (coordinates copied in and
-out every step, wall clock); `roofline` = FP32 throughput of the sweep kernel (68 flops per pair
-interaction, SURVEY's count) against an FFMA probe measured in the same run; `cpu_baseline` = the
-reference's algorithm (oracle/ port, two full energies per move, OpenMP-free per chain, chains in
-parallel on all host cores) on a bounded stratified sample of the same chains.
+Before the warm-up the autotuner picks the sweep's launch shape (threads per chain, CTAs per SM,
+speculation width) from two trial sweeps per candidate; those sweeps are untimed.
+
+Reported: `value` = accepted moves/s over all GPUs (device time of whole sweeps, list rebuild
+included, CUDA events on the library's stream, max over ranks); `e2e` = the same through the
+host-buffer API (coordinates copied in and out every step, wall clock); `roofline` = FP32
+throughput of the sweep kernel alone (its launches timed by event-record nodes inside the sweep
+graph; 68 flops per pair interaction: distance + minimum image 23, square root and inverse 5,
+Coulomb + LJ 30, accumulation 2, switch polynomial 8) against an FFMA probe measured in the same
+run; `cpu_baseline` = the reference's algorithm (oracle/ port, two full energies per move, one
+chain per host thread) on a bounded stratified sample of the same chains.
 """
 from __future__ import annotations
 
@@ -225,13 +230,14 @@ def run_ours(args):
     B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank,
                     threads_per_chain=args.threads, ctas_per_sm=args.ctas_per_sm)
     natoms = B.natoms
+    tuning = B.autotune(trial_sweeps=2) if not (args.threads or args.ctas_per_sm) else dict(B.tuning(), from_cache=False)
     B.sweep(args.warmup)
     barrier()
     t0, a0, _ = B.stats()
     p0 = B.pairs()
     with ClockSampler(local) as clk:
         barrier()
-        ms = B.time_sweeps(args.steps)
+        ms, ms_lists, ms_sweep = B.time_phases(args.steps)
         barrier()
     t1, a1, e1 = B.stats()
     p1 = B.pairs()
@@ -246,7 +252,7 @@ def run_ours(args):
     import ctypes as C
     tf = C.c_double(0)
     native.check(peak.mcg_probe_fp32_tflops(C.byref(tf)))
-    achieved = pairs * FLOPS_PER_PAIR / (ms * 1e-3 / args.steps) / args.steps / 1e12
+    achieved = pairs * FLOPS_PER_PAIR / (ms_sweep * 1e-3) / 1e12
     traffic = traffic_from_profiles()
     # e2e: host buffers in and out through the public API every step (pinned host memory)
     hin = torch.empty((3, natoms), dtype=torch.float64, pin_memory=True).numpy()
@@ -292,7 +298,9 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "chains": args.chains, "atoms_per_gpu": natoms,
                        "molecules_per_sweep_per_gpu": int(natoms // 3),
                        "l2": "no flush: per-sweep working set (1.5 GB lists, 134 MB coordinates) > 129 MB L2",
-                       "acceptance": "physical", "parallelism": "independent chains, weak scaling over GPUs"},
+                       "acceptance": "physical", "parallelism": "independent chains, weak scaling over GPUs",
+                       "tuning": tuning},
+            "phase_ms_per_step": {"list_rebuild": ms_lists / args.steps, "sweep_kernel": ms_sweep / args.steps},
             "trials_per_s": allsum(trials) / (ms_max * 1e-3),
             "acceptance_ratio": acc / max(1.0, trials),
             "pair_interactions_per_s": allsum(pairs) / (ms_max * 1e-3),
@@ -302,7 +310,7 @@ def run_ours(args):
                          "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
             "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(3 * natoms * 8),
                     "d2h_bytes_per_step": int(3 * natoms * 8 + args.chains * 16)},
-            "gpu_launches": args.steps,
+            "gpu_launches": 3 * args.steps,
             "list_rebuilds_total": int(rb),
             "clocks": clk.summary(),
             "plain_fp64": plain,

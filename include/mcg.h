@@ -150,7 +150,7 @@ typedef struct mcg_batch_opts {
     double dmax_trn;          /* Angstrom */
     double dmax_rot;          /* degrees */
     int acceptance_units;     /* enum mcg_acceptance */
-    int threads_per_chain;    /* threads of the CTA that runs a chain's moves (64..256, 0 = 256) */
+    int threads_per_chain;    /* threads of the CTA that runs a chain's moves (128, 256 or 512; 0 = 512) */
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
@@ -171,6 +171,29 @@ int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double*
 /* Run nsweeps sweeps and return their device time in milliseconds (CUDA events on the handle's
  * stream, synchronised on both sides). */
 int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms);
+/* Run nsweeps sweeps, each replayed from a graph that records events around its two phases, and
+ * return the device time of all of them (ms_total), of the list rebuilds (k_batch_bin +
+ * k_batch_lists, ms_lists) and of the sweep kernel alone (ms_sweep), summed over the sweeps.  The
+ * host waits for each sweep before it reads that sweep's phase times. */
+int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_lists, float* ms_sweep);
+
+/* Launch shape of the sweep kernel chosen by the autotuner. */
+typedef struct mcg_batch_tuning {
+    int threads_per_chain;    /* 256 or 512 */
+    int ctas_per_sm;          /* persistent CTAs per SM (1 or 2) */
+    int speculation;          /* cap on moves evaluated together (0 = box-size heuristic) */
+    float ms_per_sweep;       /* device time of one sweep at that shape (0 if not measured) */
+    int from_cache;           /* 1 when taken from the cache without trial sweeps */
+} mcg_batch_tuning;
+/* Autotuner: times trial_sweeps sweeps (1..64) of every candidate launch shape (threads per chain
+ * x CTAs per SM x speculation cap) on this batch and keeps the fastest.  The trial sweeps are
+ * ordinary Metropolis sweeps: they advance the chains and count in their statistics.  With
+ * use_cache != 0 a shape already tuned for the same workload signature (chain sizes and boxes,
+ * cutoffs, move sizes, device name) in this process, or in the file named by the environment
+ * variable MCG_TUNE_CACHE, is applied without trial sweeps; new results are appended there. */
+int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_tuning* out);
+/* Current launch shape (ms_per_sweep = 0). */
+int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out);
 /* Host-buffer run: when xyz_in != NULL, copy all chains' coordinates in (3*natoms doubles: x for
  * every atom of every chain, then y, then z), rebuild the lists and recompute the running
  * energies; run nsweeps sweeps; when xyz_out != NULL copy the coordinates back; fill accepted and

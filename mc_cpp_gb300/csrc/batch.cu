@@ -31,8 +31,12 @@
 // threshold is computed by a warp that would otherwise wait at the barrier.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -816,6 +820,12 @@ struct mcg_batch {
     int ntiles = 0;
     CutDev cut64{};
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t tgraph = nullptr;   // the same sweep with event records around its two phases
+    cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
+    std::vector<double> cost;     // LPT cost of each chain's sweep
+    std::vector<int> kgeom, kheur; // speculation: geometric maximum and the box-size heuristic per chain
+    int nsm = 152, ctas_per_sm = 1, spec_cap = 0;
+    std::string signature;        // workload + device key of the autotuner cache
     double* d_xyz = nullptr;      // staging for host-buffer runs (3 x natoms)
     double* d_eres = nullptr;     // per-residue energy shares (mixed recompute)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -823,6 +833,8 @@ struct mcg_batch {
     int64_t rebuilds_seen = 0, launches = 0;
     ~mcg_batch() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (tgraph) cudaGraphExecDestroy(tgraph);
+        for (cudaEvent_t e : tev) if (e) cudaEventDestroy(e);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
                      d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos};
         for (void* q : p) if (q) cudaFree(q);
@@ -860,18 +872,92 @@ struct mcg_batch {
         launches += 2;
         return MCG_OK;
     }
-    int ensure_graph() {
-        if (graph) return MCG_OK;
+    // One sweep as a CUDA graph: [bin, lists, sweep].  The timed variant records an event before,
+    // between and after the two phases (event-record nodes) so each phase can be timed per launch.
+    int capture(cudaGraphExec_t* out, bool timed) {
+        const int64_t l0 = launches;
         BK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        int r = launch_build(stream);
-        if (!r) r = launch_sweep(stream);
+        cudaError_t er = cudaSuccess;
+        if (timed) er = cudaEventRecordWithFlags(tev[0], stream, cudaEventRecordExternal);
+        int r = er == cudaSuccess ? launch_build(stream) : MCG_ECUDA;
+        if (!r && timed) er = cudaEventRecordWithFlags(tev[1], stream, cudaEventRecordExternal);
+        if (!r && er == cudaSuccess) r = launch_sweep(stream);
+        if (!r && timed) er = cudaEventRecordWithFlags(tev[2], stream, cudaEventRecordExternal);
         cudaGraph_t g = nullptr;
         cudaError_t ee = cudaStreamEndCapture(stream, &g);
-        if (r) { if (g) cudaGraphDestroy(g); return r; }
+        launches = l0;            // capturing launches nothing; replays are counted per sweep
+        if (r || er != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return r ? r : fail(MCG_ECUDA, std::string("event record in capture: ") + cudaGetErrorString(er));
+        }
         if (ee != cudaSuccess) return fail(MCG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
-        cudaError_t ie = cudaGraphInstantiate(&graph, g, 0);
+        cudaError_t ie = cudaGraphInstantiate(out, g, 0);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return fail(MCG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        return MCG_OK;
+    }
+    int ensure_graph() { return graph ? MCG_OK : capture(&graph, false); }
+    int ensure_timed_graph() {
+        if (tgraph) return MCG_OK;
+        for (cudaEvent_t& e : tev)
+            if (!e) BK(cudaEventCreate(&e));
+        return capture(&tgraph, true);
+    }
+    void drop_graphs() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (tgraph) cudaGraphExecDestroy(tgraph);
+        graph = tgraph = nullptr;
+    }
+    // Longest-processing-time packing of chains onto ctas_per_sm persistent CTAs per SM: the cost
+    // of a chain's sweep is its move count times the pairs one move touches.  The largest chains
+    // get a CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
+    int pack(int per_sm) {
+        ncta = std::min(nchains, std::max(1, nsm * std::max(1, per_sm)));
+        std::vector<int> idx(nchains);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+        std::vector<double> load(ncta, 0.0);
+        std::vector<std::vector<int>> per(ncta);
+        for (int c : idx) {
+            int best = 0;
+            for (int k = 1; k < ncta; k++) if (load[k] < load[best]) best = k;
+            load[best] += cost[c];
+            per[best].push_back(c);
+        }
+        order.clear();
+        cta_start.assign(ncta + 1, 0);
+        for (int k = 0; k < ncta; k++) {
+            cta_start[k] = (int)order.size();
+            order.insert(order.end(), per[k].begin(), per[k].end());
+        }
+        cta_start[ncta] = (int)order.size();
+        ctas_per_sm = per_sm;
+        if (!d_order) {
+            cudaError_t e = cudaMalloc((void**)&d_order, sizeof(int) * nchains);
+            if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        if (d_cta_start) { cudaFree(d_cta_start); d_cta_start = nullptr; }
+        cudaError_t e = cudaMalloc((void**)&d_cta_start, sizeof(int) * (ncta + 1));
+        if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        BK(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, stream));
+        BK(cudaMemcpyAsync(d_cta_start, cta_start.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, stream));
+        return MCG_OK;
+    }
+    // Speculation width of every chain: the box-size heuristic (cap 0) or min(cap, geometric limit).
+    void set_speculation(int cap) {
+        for (int c = 0; c < nchains; c++) chains[c].kspec = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
+        spec_cap = cap;
+    }
+    // Launch shape of the sweep; takes effect at the next sweep (the graphs are captured again).
+    int reconfigure(int nthreads, int per_sm, int spec) {
+        BK(cudaStreamSynchronize(stream));
+        threads = nthreads;
+        set_speculation(spec);
+        int r = pack(per_sm);
+        if (r) return r;
+        BK(cudaMemcpyAsync(d_chains, chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, stream));
+        BK(cudaStreamSynchronize(stream));
+        drop_graphs();
         return MCG_OK;
     }
     template <int APR>
@@ -1036,8 +1122,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             const double vol = C.L[0] * C.L[1] * C.L[2];
             const double frac = 4.0 / 3.0 * PI * rind * rind * rind / vol;
             const bool any_half = rind > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]));
-            C.kspec = (opts->speculation == 1 || any_half || frac > 0.35) ? 1 : (frac > 0.12 || opts->speculation == 2 ? 2 : 4);
-            if (opts->speculation == 4 && !any_half) C.kspec = 4;
+            B->kgeom.push_back(any_half ? 1 : 4);
+            B->kheur.push_back((any_half || frac > 0.35) ? 1 : (frac > 0.12 ? 2 : 4));
         }
         if (!C.use_cells) C.nc[0] = C.nc[1] = C.nc[2] = 1;
     }
@@ -1054,44 +1140,38 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 512;
     if (B->threads != 128 && B->threads != 256 && B->threads != 512)
         return fail(MCG_EINVAL, "threads_per_chain must be 128, 256 or 512");
-    // Longest-processing-time packing of chains onto persistent CTAs (one per SM): the cost of a
-    // chain's sweep is its move count times the pairs one move touches.  The largest chains get a
-    // CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
-    int dev = 0, nsm = 152;
+    if (opts->speculation < 0 || opts->speculation == 3 || opts->speculation > 4)
+        return fail(MCG_EINVAL, "speculation must be 0, 1, 2 or 4");
+    if (opts->ctas_per_sm < 0 || opts->ctas_per_sm > 8) return fail(MCG_EINVAL, "ctas_per_sm must be in [0, 8]");
+    B->set_speculation(opts->speculation);
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    B->ncta = std::min(nchains, std::max(1, nsm * std::max(1, opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 1)));
+    cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, dev);
+    B->cost.resize(nchains);
     {
-        std::vector<double> cost(nchains);
         const double rl = rc + skin;
+        uint64_t h = 1469598103934665603ull;       // FNV-1a over the workload's shape
+        auto mix = [&](uint64_t v) { for (int k = 0; k < 8; k++) { h ^= (v >> (8 * k)) & 0xff; h *= 1099511628211ull; } };
         for (int c = 0; c < nchains; c++) {
             const ChainDev& C = B->chains[c];
             const double dens = C.nres / (C.L[0] * C.L[1] * C.L[2]);
             const double neigh = std::min((double)C.nres, dens * 4.0 / 3.0 * PI * rl * rl * rl);
-            cost[c] = (double)C.nres * neigh * C.apr * C.apr + 1.0;
+            B->cost[c] = (double)C.nres * neigh * C.apr * C.apr + 1.0;
+            mix((uint64_t)C.nres); mix((uint64_t)C.apr); mix((uint64_t)llround(C.L[0] * 1000));
         }
-        std::vector<int> idx(nchains);
-        std::iota(idx.begin(), idx.end(), 0);
-        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-        std::vector<double> load(B->ncta, 0.0);
-        std::vector<std::vector<int>> per(B->ncta);
-        for (int c : idx) {
-            int best = 0;
-            for (int k = 1; k < B->ncta; k++) if (load[k] < load[best]) best = k;
-            load[best] += cost[c];
-            per[best].push_back(c);
-        }
-        B->order.clear();
-        B->cta_start.assign(B->ncta + 1, 0);
-        for (int k = 0; k < B->ncta; k++) {
-            B->cta_start[k] = (int)B->order.size();
-            B->order.insert(B->order.end(), per[k].begin(), per[k].end());
-        }
-        B->cta_start[B->ncta] = (int)B->order.size();
+        mix((uint64_t)llround(rc * 1000)); mix((uint64_t)llround(skin * 1000));
+        mix((uint64_t)llround(opts->dmax_trn * 1e4)); mix((uint64_t)llround(opts->dmax_rot * 1e4));
+        cudaDeviceProp prop;
+        std::string name = cudaGetDeviceProperties(&prop, dev) == cudaSuccess ? prop.name : "unknown";
+        for (char& ch : name) if (ch == ' ') ch = '_';
+        char buf[64];
+        snprintf(buf, sizeof buf, "%016llx", (unsigned long long)h);
+        B->signature = name + ":" + std::to_string(nchains) + ":" + buf;
     }
     BK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
     int r;
-    if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) || (r = balloc(&B->d_order, nchains)) ||
+    if ((r = B->pack(opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 1))) return r;
+    if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) ||
         (r = balloc(&B->d_M, atom0)) || (r = balloc(&B->d_F, atom0)) || (r = balloc(&B->d_FB, atom0)) ||
         (r = balloc(&B->d_LST, (size_t)res0 * G.cap)) || (r = balloc(&B->d_NL, res0)) || (r = balloc(&B->d_gorder, res0)) ||
         (r = balloc(&B->d_gcell, res0)) || (r = balloc(&B->d_prm, prm.size())) ||
@@ -1105,9 +1185,6 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         BK(cudaMemcpy(B->d_res_chain, rcn.data(), sizeof(int) * res0, cudaMemcpyHostToDevice));
     }
     BK(cudaMemcpyAsync(B->d_chains, B->chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, B->stream));
-    if ((r = balloc(&B->d_cta_start, B->ncta + 1))) return r;
-    BK(cudaMemcpyAsync(B->d_order, B->order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, B->stream));
-    BK(cudaMemcpyAsync(B->d_cta_start, B->cta_start.data(), sizeof(int) * (B->ncta + 1), cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_F, F.data(), sizeof(uint4) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice, B->stream));
@@ -1168,6 +1245,116 @@ int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms) {
     BK(cudaEventSynchronize(b->ev1));
     BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
     b->launches += 3 * (int64_t)nsweeps;
+    return MCG_OK;
+}
+
+int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_lists, float* ms_sweep) {
+    if (!b || nsweeps < 0 || !ms_total || !ms_lists || !ms_sweep) return fail(MCG_EINVAL, "bad arguments");
+    int r = b->ensure_timed_graph();
+    if (r) return r;
+    if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
+    BK(cudaStreamSynchronize(b->stream));
+    BK(cudaEventRecord(b->ev0, b->stream));
+    double tl = 0.0, ts = 0.0;
+    for (int s = 0; s < nsweeps; s++) {
+        BK(cudaGraphLaunch(b->tgraph, b->stream));
+        BK(cudaEventSynchronize(b->tev[2]));       // the phase events hold only the latest replay
+        float a = 0.f, c = 0.f;
+        BK(cudaEventElapsedTime(&a, b->tev[0], b->tev[1]));
+        BK(cudaEventElapsedTime(&c, b->tev[1], b->tev[2]));
+        tl += a;
+        ts += c;
+    }
+    BK(cudaEventRecord(b->ev1, b->stream));
+    BK(cudaEventSynchronize(b->ev1));
+    BK(cudaEventElapsedTime(ms_total, b->ev0, b->ev1));
+    *ms_lists = (float)tl;
+    *ms_sweep = (float)ts;
+    b->launches += 3 * (int64_t)nsweeps;
+    return MCG_OK;
+}
+
+// Autotuner cache: signature -> (threads, ctas per SM, speculation), kept for the process and,
+// when MCG_TUNE_CACHE names a file, in that file (one "signature threads ctas spec ms" per line).
+static std::mutex g_tune_mu;
+static std::map<std::string, mcg_batch_tuning> g_tune_cache;
+
+static bool tune_lookup(const std::string& sig, mcg_batch_tuning* t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(sig);
+    if (it != g_tune_cache.end()) { *t = it->second; return true; }
+    const char* path = getenv("MCG_TUNE_CACHE");
+    if (!path || !*path) return false;
+    FILE* f = fopen(path, "r");
+    if (!f) return false;
+    char key[256];
+    mcg_batch_tuning v{};
+    bool found = false;
+    while (fscanf(f, "%255s %d %d %d %f", key, &v.threads_per_chain, &v.ctas_per_sm, &v.speculation, &v.ms_per_sweep) == 5)
+        if (sig == key) { *t = v; found = true; }
+    fclose(f);
+    if (found) g_tune_cache[sig] = *t;
+    return found;
+}
+
+static void tune_store(const std::string& sig, const mcg_batch_tuning& t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[sig] = t;
+    const char* path = getenv("MCG_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = fopen(path, "a");
+    if (!f) return;
+    fprintf(f, "%s %d %d %d %.4f\n", sig.c_str(), t.threads_per_chain, t.ctas_per_sm, t.speculation, t.ms_per_sweep);
+    fclose(f);
+}
+
+int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_tuning* out) {
+    if (!b || trial_sweeps < 1 || trial_sweeps > 64) return fail(MCG_EINVAL, "trial_sweeps must be in [1, 64]");
+    mcg_batch_tuning best{};
+    if (use_cache && tune_lookup(b->signature, &best)) {
+        int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation);
+        if (r) return r;
+        best.from_cache = 1;
+        if (out) *out = best;
+        return MCG_OK;
+    }
+    static const int kThreads[] = {256, 512};
+    static const int kCtas[] = {1, 2};
+    static const int kSpec[] = {1, 2, 4, 0};
+    best.ms_per_sweep = 3.0e38f;
+    if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
+    for (int th : kThreads)
+        for (int cp : kCtas)
+            for (int sp : kSpec) {
+                int r = b->reconfigure(th, cp, sp);
+                if (r) return r;
+                if ((r = b->ensure_graph())) return r;
+                BK(cudaGraphLaunch(b->graph, b->stream));      // upload + warm
+                BK(cudaEventRecord(b->ev0, b->stream));
+                for (int s = 0; s < trial_sweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
+                BK(cudaEventRecord(b->ev1, b->stream));
+                BK(cudaEventSynchronize(b->ev1));
+                float ms = 0.f;
+                BK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                b->launches += 3 * (int64_t)(trial_sweeps + 1);
+                ms /= (float)trial_sweeps;
+                if (ms < best.ms_per_sweep) { best.threads_per_chain = th; best.ctas_per_sm = cp; best.speculation = sp; best.ms_per_sweep = ms; }
+            }
+    int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation);
+    if (r) return r;
+    best.from_cache = 0;
+    tune_store(b->signature, best);
+    if (out) *out = best;
+    return MCG_OK;
+}
+
+int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out) {
+    if (!b || !out) return fail(MCG_EINVAL, "null argument");
+    out->threads_per_chain = b->threads;
+    out->ctas_per_sm = b->ctas_per_sm;
+    out->speculation = b->spec_cap;
+    out->ms_per_sweep = 0.f;
+    out->from_cache = 0;
     return MCG_OK;
 }
 

@@ -184,6 +184,24 @@ class BatchChains:
         native.check(native.lib().mcg_batch_time_sweeps(self.h, n, C.byref(ms)))
         return ms.value
 
+    def time_phases(self, n: int):
+        """Device ms of n sweeps: (total, list rebuilds, sweep kernel alone)."""
+        a, b, c = C.c_float(0), C.c_float(0), C.c_float(0)
+        native.check(native.lib().mcg_batch_time_phases(self.h, n, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def autotune(self, trial_sweeps: int = 2, use_cache: bool = True) -> dict:
+        """Times every candidate launch shape on trial_sweeps real sweeps and keeps the fastest."""
+        t = native.BatchTuning()
+        native.check(native.lib().mcg_batch_autotune(self.h, trial_sweeps, int(use_cache), C.byref(t)))
+        return {"threads_per_chain": t.threads_per_chain, "ctas_per_sm": t.ctas_per_sm, "speculation": t.speculation,
+                "ms_per_sweep": t.ms_per_sweep, "from_cache": bool(t.from_cache)}
+
+    def tuning(self) -> dict:
+        t = native.BatchTuning()
+        native.check(native.lib().mcg_batch_get_tuning(self.h, C.byref(t)))
+        return {"threads_per_chain": t.threads_per_chain, "ctas_per_sm": t.ctas_per_sm, "speculation": t.speculation}
+
     def stats(self):
         t = np.zeros(self.nchains, np.int64)
         a = np.zeros(self.nchains, np.int64)

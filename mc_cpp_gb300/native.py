@@ -61,6 +61,11 @@ class BatchOpts(C.Structure):
                 ("ctas_per_sm", C.c_int), ("speculation", C.c_int)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("threads_per_chain", C.c_int), ("ctas_per_sm", C.c_int), ("speculation", C.c_int),
+                ("ms_per_sweep", C.c_float), ("from_cache", C.c_int)]
+
+
 _lib = None
 
 
@@ -110,6 +115,9 @@ def lib():
         "mcg_batch_chain_natoms": (C.c_int, [P, C.c_int]),
         "mcg_batch_counters": (C.c_int, [P, _i64, _i64]),
         "mcg_batch_time_sweeps": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
+        "mcg_batch_time_phases": (C.c_int, [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "mcg_batch_autotune": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(BatchTuning)]),
+        "mcg_batch_get_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
         "mcg_batch_run_host": (C.c_int, [P, _d, C.c_int, _d, _i64, _d]),
         "mcg_batch_energy_mixed": (C.c_int, [P, _d]),
         "mcg_batch_pairs": (C.c_int, [P, _i64]),

@@ -167,3 +167,37 @@ def test_speculative_sweep_reproduces_sequential_chain():
     assert sum(same) >= len(ch) - 1, same
     ef = spec.energy_fp64()
     assert (np.abs(e2 - ef) / np.abs(ef)).max() <= 1e-6
+
+
+def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch):
+    monkeypatch.setenv("MCG_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    ch = _waters((512, 1500, 3000), seed=41)
+    B = BatchChains(ch, seed=8)
+    t = B.autotune(trial_sweeps=1, use_cache=False)
+    assert t["threads_per_chain"] in (256, 512) and t["ctas_per_sm"] in (1, 2)
+    assert t["speculation"] in (0, 1, 2, 4) and t["ms_per_sweep"] > 0 and not t["from_cache"]
+    assert {k: t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")} == B.tuning()
+    tr, a, etot = B.stats()
+    assert np.all(tr == 16 * 2 * (B.sizes // 3))      # 16 shapes x (1 warm-up + 1 timed sweep)
+    B.sweep(2)
+    _, _, etot = B.stats()
+    e = B.energy_fp64()
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+    # a second batch of the same workload takes the cached shape without trial sweeps
+    B2 = BatchChains(ch, seed=8)
+    t2 = B2.autotune(trial_sweeps=1, use_cache=True)
+    assert t2["from_cache"]
+    assert [t2[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")] == \
+           [t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")]
+    assert np.all(B2.stats()[0] == 0)
+    assert (tmp_path / "tune.txt").read_text().count("\n") == 1
+
+
+def test_phase_timing_adds_up():
+    ch = _waters((800, 2000), seed=43)
+    B = BatchChains(ch, seed=2)
+    B.sweep(1)
+    tot, lists, sweep = B.time_phases(3)
+    assert lists > 0 and sweep > 0
+    assert lists + sweep <= tot * 1.01 + 0.05
+    assert np.all(B.stats()[0] == 4 * (B.sizes // 3))
