@@ -154,7 +154,7 @@ typedef struct mcg_batch_opts {
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
-    int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4 */
+    int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4, 8 */
 } mcg_batch_opts;
 
 /* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */
@@ -204,6 +204,9 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
 int mcg_batch_energy_mixed(mcg_batch* b, double* e);
 /* Pair interactions evaluated so far by each chain (pairs inside the cutoff before or after a move). */
 int mcg_batch_pairs(mcg_batch* b, int64_t* pairs);
+/* Rebuild every chain's neighbour lists now (the batched counterpart of FField::askListUpdate,
+ * FField.cpp:222-235).  Sweeps rebuild lists by themselves when atoms have moved enough. */
+int mcg_batch_update_lists(mcg_batch* b);
 /* Total number of atoms over all chains, and a chain's atom count. */
 int64_t mcg_batch_natoms(mcg_batch* b);
 int mcg_batch_chain_natoms(mcg_batch* b, int chain);

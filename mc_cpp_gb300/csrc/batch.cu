@@ -89,11 +89,12 @@ struct ChainDev {
     float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
-    int kspec;            // moves evaluated together by the sweep (1, 2 or 4)
+    int kspec;            // moves evaluated together by the sweep (1, 2, 4 or 8)
     int wrap_offsets;     // box small enough that (b - a_0) - (a_k - a_0) may leave the minimum image
     float Lf[3], Lhalf[3];
     float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
     double beta;
+    float beta_f;         // beta rounded to FP32 (clear-margin Metropolis decisions)
     float dmax_trn, dmax_rot;
     int ntypes_move;      // 1: TRN only, 2: TRN + ROT
     uint32_t key0, key1;
@@ -106,8 +107,10 @@ struct ChainState {
     long long trials, accepted;
     long long pairs;            // pair interactions evaluated (inside rc before or after a move)
     unsigned long long moves;   // Philox counter
-    int rebuilds;
+    int rebuilds;               // list builds (before or during sweeps)
     int err;
+    float maxd2;                // largest squared displacement of a committed atom since the last build
+    int pad_;
 };
 
 struct BatchGeom {
@@ -118,6 +121,8 @@ struct BatchGeom {
     float cellmin;     // cell edge for the 5-stencil
     float skip2;       // (rc + extent from the first atom + largest move)^2: dE prefilter
     float indep2;      // (rc + 2 extents + 2 largest moves)^2: two moves cannot interact beyond it
+    float subst2;      // (list centre radius + skin)^2: a residue farther than this is in no list of the other
+    float pre2;        // a chain whose atoms moved less than this (squared) since the build keeps its lists
     int cap;
 };
 
@@ -130,10 +135,12 @@ __device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
 // ---- neighbour lists ----------------------------------------------------------------------
 // Residues are binned by their first atom into cells of edge >= (rc + skin + 2 rext)/2 and a
 // 5x5x5 stencil is scanned; boxes with fewer than 5 cells per edge scan every residue.  A residue
-// q enters the list of r when any atom pair is within rc + skin (exact fixed-point displacement).
-// Lists are rebuilt for every chain before every sweep by a grid-wide kernel (k_batch_bin +
-// k_batch_lists); inside a sweep, a chain whose atom has moved more than half the skin since the
-// build rebuilds its own lists with its CTA (chain_rebuild) before the next move.
+// q enters the list of r when their first atoms are within rc + skin + 2 extents (a superset of the
+// residues with an atom pair within rc + skin).  Before a sweep, a grid-wide pass (k_batch_bin +
+// k_batch_lists) rebuilds the lists of the chains whose atoms have moved more than ~0.55 half-skins
+// since their last build; inside a sweep, a chain whose atom has moved more than half the skin
+// rebuilds its own lists with its CTA (chain_rebuild) before the next move.  Lists are built a home
+// cell per warp: lane = home residue, candidates staged 32 at a time in shared memory.
 
 // Block-level binning of chain C: copies the build positions and, when the chain uses cells,
 // fills starts[0..ncell] (shared or global) and g_order (residues sorted by cell, then index).
@@ -188,129 +195,185 @@ __device__ void chain_bin(const ChainDev& C, const uint4* __restrict__ F, uint4*
     }
     __syncthreads();
     // first-atom positions in cell order: the candidate scan reads them contiguously
-    for (int t = tid; t < nres; t += T) g_pos[t] = Fc[g_order[t] * apr];
+    for (int t = tid; t < nres; t += T) {
+        uint4 p = Fc[g_order[t] * apr];
+        p.w = (uint32_t)g_order[t];
+        g_pos[t] = p;
+    }
     __syncthreads();
 }
 
-// Warp-level list of residue r (all 32 lanes of the calling warp).
+// The contiguous slot ranges of the 5x5x5 stencil around home cell (hx, hy, hz), in stencil
+// order: the 25 (dz, dy) rows, each the merged ranges of its five x cells in dx order.
+template <typename Fn>
+__device__ __forceinline__ void stencil_ranges(const ChainDev& C, const int* __restrict__ starts, int hx, int hy, int hz,
+                                               Fn&& f) {
+    const int nx = C.nc[0], ny = C.nc[1], nz = C.nc[2];
+    for (int dz = -2; dz <= 2; dz++) {
+        int z = hz + dz;
+        z += z < 0 ? nz : (z >= nz ? -nz : 0);
+        for (int dy = -2; dy <= 2; dy++) {
+            int y = hy + dy;
+            y += y < 0 ? ny : (y >= ny ? -ny : 0);
+            const int rowc = (z * ny + y) * nx;
+            int rb = -1, re = -1;
+            for (int dx = -2; dx <= 2; dx++) {
+                int x = hx + dx;
+                x += x < 0 ? nx : (x >= nx ? -nx : 0);
+                const int b = starts[rowc + x], e = starts[rowc + x + 1];
+                if (b == re) { re = e; continue; }
+                if (re > rb) f(rb, re);
+                rb = b;
+                re = e;
+            }
+            if (re > rb) f(rb, re);
+        }
+    }
+}
+
+// Lists of the residues of one work item of chain C (all 32 lanes of the calling warp): a home
+// cell when the chain uses cells, else 32 consecutive residues scanning every residue.  Lane =
+// home residue; each chunk of 32 candidates is staged in `stage` (32 entries, shared memory) and
+// tested by every lane, so a candidate costs one broadcast load and one distance per home residue.
 template <int APR>
-__device__ void residue_list(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int r,
-                             const int* __restrict__ starts, const int* __restrict__ g_order,
-                             const uint4* __restrict__ g_pos, uint16_t* LST, int* NL, int* err_out) {
+__device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int item,
+                           const int* __restrict__ starts, const int* __restrict__ g_order,
+                           const uint4* __restrict__ g_pos, uint16_t* LST, int* NL, int* err_out, uint4* stage) {
+    (void)g_order;
     const int apr = APR ? APR : C.apr;
     const int lane = threadIdx.x & 31;
-    uint4 pa[1];
-    pa[0] = Fc[r * apr];
-    uint16_t* row = LST + (size_t)(C.res0 + r) * G.cap;
-    int cnt = 0;
-    // cells: `slot` indexes the cell-sorted arrays; otherwise it is the residue itself
-    auto consider = [&](int slot, bool valid) {
-        bool ok = false;
-        int q = slot;
-        uint4 pq = make_uint4(0, 0, 0, 0);
-        if (valid) {
-            if (C.use_cells) { pq = g_pos[slot]; q = g_order[slot]; }
-            else pq = Fc[q * apr];
-        }
-        if (valid && q != r) {
-            const float dx = fdelta(pa[0].x, pq.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa[0].y, pq.y, C.Ls[1], C.Lsl[1]), dz = fdelta(pa[0].z, pq.z, C.Ls[2], C.Lsl[2]);
-            // first atoms within rc + skin + 2 extents: a superset of the residues with an atom pair
-            // within rc + skin, found with one distance per candidate
-            ok = dx * dx + dy * dy + dz * dz <= G.rcent2;
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-            if (pos < G.cap) row[pos] = (uint16_t)q;
-        }
-        cnt += __popc(bal);
-    };
-    if (C.use_cells) {
-        const int cx = cell_coord(pa[0].x, C.nc[0]), cy = cell_coord(pa[0].y, C.nc[1]), cz = cell_coord(pa[0].z, C.nc[2]);
-        for (int dz = -2; dz <= 2; dz++)
-            for (int dy = -2; dy <= 2; dy++) {
-                const int y = (cy + dy + C.nc[1]) % C.nc[1], z = (cz + dz + C.nc[2]) % C.nc[2];
-                const int rowc = (z * C.nc[1] + y) * C.nc[0];
-                // the five x cells of this stencil row, merged into contiguous slot ranges
-                int rb = -1, re = -1;
-                for (int dx = -2; dx <= 3; dx++) {
-                    int b = 0, e = 0;
-                    if (dx <= 2) {
-                        const int x = (cx + dx + C.nc[0]) % C.nc[0];
-                        b = starts[rowc + x];
-                        e = starts[rowc + x + 1];
-                    }
-                    if (dx <= 2 && b == re) { re = e; continue; }
-                    for (int base = rb; base >= 0 && base < re; base += 32) {
-                        const int t = base + lane;
-                        consider(t < re ? t : rb, t < re);
-                    }
-                    rb = b;
-                    re = e;
-                }
-            }
+    const bool cells = C.use_cells != 0;
+    const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
+    const float rc2 = G.rcent2;
+    const int cap = G.cap;
+    int hb, he, hx = 0, hy = 0, hz = 0;
+    if (cells) {
+        hb = starts[item];
+        he = starts[item + 1];
+        hx = item % C.nc[0];
+        hy = (item / C.nc[0]) % C.nc[1];
+        hz = item / (C.nc[0] * C.nc[1]);
     } else {
-        for (int base = 0; base < C.nres; base += 32) {
-            const int q = base + lane;
-            consider(q < C.nres ? q : 0, q < C.nres);
-        }
+        hb = item * 32;
+        he = min(C.nres, hb + 32);
     }
-    if (lane == 0) {
-        NL[C.res0 + r] = min(cnt, G.cap);
-        if (cnt > G.cap) atomicExch(err_out, MCG_ECAPACITY);
+    for (int h0 = hb; h0 < he; h0 += 32) {
+        const int hs = h0 + lane;
+        const bool act = hs < he;
+        int r = -1;
+        uint4 pa = make_uint4(0, 0, 0, 0);
+        if (act) {
+            if (cells) { pa = g_pos[hs]; r = (int)pa.w; }
+            else { r = hs; pa = Fc[(size_t)r * apr]; }
+        }
+        uint16_t* row = LST + (size_t)(C.res0 + (act ? r : 0)) * cap;
+        int cnt = 0;
+        auto scan = [&](int b, int e) {
+            for (int k = b; k < e; k += 32) {
+                const int t = k + lane;
+                if (t < e) {
+                    uint4 v;
+                    if (cells) v = g_pos[t];            // w = residue index
+                    else { v = Fc[(size_t)t * apr]; v.w = (uint32_t)t; }
+                    stage[lane] = v;
+                }
+                __syncwarp();
+                const int m = min(32, e - k);
+                if (act) {
+                    for (int j = 0; j < m; j++) {
+                        const uint4 v = stage[j];
+                        const float dx = fdelta(pa.x, v.x, Ls0, Ll0), dy = fdelta(pa.y, v.y, Ls1, Ll1), dz = fdelta(pa.z, v.z, Ls2, Ll2);
+                        if ((int)v.w != r && dx * dx + dy * dy + dz * dz <= rc2) {
+                            if (cnt < cap) row[cnt] = (uint16_t)v.w;
+                            cnt++;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        };
+        if (cells) stencil_ranges(C, starts, hx, hy, hz, scan);
+        else scan(0, C.nres);
+        if (act) {
+            NL[C.res0 + r] = min(cnt, cap);
+            if (cnt > cap) atomicExch(err_out, MCG_ECAPACITY);
+        }
     }
 }
 
-// Per-chain binning before a sweep: one CTA per chain, cell starts to global memory.
+__device__ __forceinline__ int chain_items(const ChainDev& C) {
+    return C.use_cells ? C.nc[0] * C.nc[1] * C.nc[2] : (C.nres + 31) / 32;
+}
+
+// Per-chain binning before a sweep, one CTA per chain: only chains that were asked to (force) or
+// whose atoms moved more than sqrt(pre2) since their last build; build[c] tells k_batch_lists.
 __global__ void k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __restrict__ F, uint4* FB, int* g_starts,
-                            int* g_order, int* g_cell, uint4* g_pos, int nchains) {
+                            int* g_order, int* g_cell, uint4* g_pos, ChainState* state, int* build, float pre2, int force,
+                            int nchains) {
     const int c = blockIdx.x;
     if (c >= nchains) return;
+    const bool need = force || state[c].maxd2 > pre2;
+    if (threadIdx.x == 0) build[c] = need ? 1 : 0;
+    if (!need) return;
     const ChainDev& C = chains[c];
     chain_bin(C, F, FB, g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0, g_cell + C.res0, g_pos + C.res0);
-}
-
-// Lists of every residue of every chain: one warp per residue over the whole GPU.
-template <int APR>
-__global__ void __launch_bounds__(256) k_batch_lists(const ChainDev* __restrict__ chains, BatchGeom G,
-                                                     const uint4* __restrict__ F, const int* __restrict__ res_chain,
-                                                     const int* __restrict__ g_starts, const int* __restrict__ g_order,
-                                                     const uint4* __restrict__ g_pos, uint16_t* LST, int* NL,
-                                                     ChainState* state, int64_t nres_total) {
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
-        const int c = res_chain[gr];
-        const ChainDev& C = chains[c];
-        if (APR && C.apr != APR) continue;
-        residue_list<APR>(C, G, F + C.atom0, (int)(gr - C.res0), g_starts + (size_t)c * (MAX_CELLS + 1),
-                          g_order + C.res0, g_pos + C.res0, LST, NL, &state[c].err);
+    if (threadIdx.x == 0) {
+        state[c].maxd2 = 0.0f;
+        state[c].rebuilds++;
     }
 }
 
-// In-sweep rebuild of one chain by its own CTA (shared-memory cell starts).
+// Lists of the chains binned by k_batch_bin: one warp per work item (home cell) over the GPU.
+template <int APR>
+__global__ void __launch_bounds__(256) k_batch_lists(const ChainDev* __restrict__ chains, BatchGeom G,
+                                                     const uint4* __restrict__ F, const int* __restrict__ item_chain,
+                                                     const int* __restrict__ chain_item0, const int* __restrict__ g_starts,
+                                                     const int* __restrict__ g_order, const uint4* __restrict__ g_pos,
+                                                     uint16_t* LST, int* NL, ChainState* state,
+                                                     const int* __restrict__ build, int nitems) {
+    __shared__ uint4 s_stage[8][32];
+    const int warp = threadIdx.x >> 5;
+    const int warps = gridDim.x * 8;
+    for (int it = blockIdx.x * 8 + warp; it < nitems; it += warps) {
+        const int c = item_chain[it];
+        if (!build[c]) continue;
+        const ChainDev& C = chains[c];
+        if (APR && C.apr != APR) continue;
+        item_lists<APR>(C, G, F + C.atom0, it - chain_item0[c], g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0,
+                        g_pos + C.res0, LST, NL, &state[c].err, s_stage[warp]);
+    }
+}
+
+// In-sweep rebuild of one chain by its own CTA (shared-memory cell starts; `stage`: 32 entries
+// per warp).
 template <int APR>
 __device__ void chain_rebuild(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ F, uint4* FB,
                               uint16_t* LST, int* NL, int* s_starts, int* g_order, int* g_cell, uint4* g_pos,
-                              int* err_out) {
+                              int* err_out, uint4* stage) {
     chain_bin(C, F, FB, s_starts, g_order, g_cell, g_pos);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    (void)lane;
-    for (int r = warp; r < C.nres; r += nw) residue_list<APR>(C, G, F + C.atom0, r, s_starts, g_order, g_pos, LST, NL, err_out);
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nitems = chain_items(C);
+    for (int it = warp; it < nitems; it += nw)
+        item_lists<APR>(C, G, F + C.atom0, it, s_starts, g_order, g_pos, LST, NL, err_out, stage);
     __syncthreads();
 }
 
 // ---- the sweep ------------------------------------------------------------------------------
-struct Proposal {
-    uint4 fo[MAX_APR], fn[MAX_APR];
-    unsigned long long mn[MAX_APR][3];   // new master coordinates
-    float m[MAX_APR][3];                 // fn - fo in Angstrom (exact mirror difference)
-    uint4 fb[MAX_APR];                   // build positions of the moved atoms
-    int res;
-    float lna;                           // -ln(alpha), FP32 estimate
-    double alpha;                        // alpha in (0, 1]
-};
+constexpr int KMAX = 8;                  // moves evaluated together, at most
+constexpr int RING = 64;                 // per-warp ring of compacted neighbour atoms (power of two)
 
-constexpr int KSPEC = 4;                 // moves evaluated together, at most
+// What every warp needs of a move after the iteration's barrier (written by the first warp of the
+// move's group): residue, old first-atom position (conflicts), new and build positions of its
+// atoms (commit substitutes, far check) and the Metropolis draw.
+struct MoveRec {
+    uint4 fn[MAX_APR];                   // new mirror positions (w = slot)
+    unsigned long long mn[MAX_APR][3];   // new master coordinates
+    uint4 fb[MAX_APR];                   // build positions of the moved atoms
+    uint4 fo0;                           // old position of the first atom
+    int res;
+    float lna;                           // -ln(alpha), FP32 estimate (NaN: decide in FP64)
+    uint32_t ahi, alo;                   // Philox words of alpha in (0, 1] (u01d_open0)
+};
 
 // Master-unit increment for a displacement d (Angstrom): d * 2^64 / L as a 64-bit integer, formed
 // in FP32 + integer arithmetic (v = d * 2^32 / L; integer part -> high word, fraction -> low word).
@@ -322,45 +385,61 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
     return ((unsigned long long)(long long)hi << 32) + lo;
 }
 
-// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2 or 4
-// per chain, from its box size); thread group g (NT/K threads) evaluates move mv+g.  Moves mv..mv+n-1
-// are applied when their residues are pairwise out of interaction range for any combination of
-// old and new positions (first-atom distance > rc + 2 extents + 2 largest moves): then each dE is
-// the one the sequential chain would compute, the decisions use the same random numbers, and the
-// result is the sequential Metropolis chain.  The remaining moves are re-proposed next iteration
-// from the same Philox counters.
+// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4 or 8
+// per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
+// before the iteration.  After the iteration's only block barrier every warp decides the moves in
+// order with the same data: move g stands while no earlier ACCEPTED move of the iteration can
+// interact with it (same residue, or first atoms within rc + 2 extents + 2 largest moves for old
+// and new positions), so its dE is the one the sequential chain computes and the chain equals the
+// sequential Metropolis chain.  The first move that fails the test and all later ones are
+// re-proposed next iteration from the same Philox counters.
 //
-// Iteration = [warp 0: the K proposals, one lane per moved atom | every other thread: the residue
-// of its group's move from the Philox stream and a prefetch of its first neighbour atoms]
-// -> barrier -> dE of the independent prefix -> barrier -> warp 0: Metropolis tests and commits.
-// Neighbours that belong to residues committed by the previous iteration may have been read before
-// the commit landed; their positions come from the previous proposals instead.
-template <int APR, int NT, int PF = (NT >= 512 ? 4 : 8)>
+// Per iteration and warp: the warp draws its group's move from the Philox stream and applies it to
+// its residue (lanes = atoms; every warp of a group does this redundantly, so no barrier is needed
+// before the pair loop).  It then scans its share of the residue's neighbour list: neighbour atoms
+// within rc + extent + largest move of the first atom are compacted, as displacements, into the
+// warp's ring in shared memory, and each time 32 are pending they are evaluated with all lanes busy
+// (old and new pair terms, mixed_pair_delta).  Commits are written by the first warp of each group
+// after the barrier; positions that a warp may read before they land come from the previous
+// iteration's move records instead.
+template <int APR, int NT>
 __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
                                                        const int* __restrict__ cta_chains, int nchains) {
     constexpr int NW = NT / 32;
-    __shared__ Proposal P[KSPEC];
-    __shared__ float2 s_red[NW];
+    constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
+    __shared__ MoveRec P[2][KMAX];
+    __shared__ float2 s_red[2][NW];
+    __shared__ float4 s_ring[NW][RING];
     __shared__ int s_cell[MAX_CELLS + 1];
-    __shared__ int s_err, s_rebuild;
-    __shared__ int s_prev_res[KSPEC];                 // residues committed by the previous iteration
-    __shared__ uint4 s_prev_fn[KSPEC][MAX_APR];
+    __shared__ int s_err;
     __shared__ float4 s_tab[MAX_APR][MAX_APR];        // 16-byte aligned: read as float4
     __shared__ unsigned long long s_pairs;
+    __shared__ __align__(16) ChainDev s_chain;        // the chain's constants, off the global-memory path
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    float4* ring = s_ring[warp];
     for (int slot = cta_start[blockIdx.x]; slot < cta_start[blockIdx.x + 1]; slot++) {
         const int c = cta_chains[slot];
         if (c >= nchains) continue;
-        const ChainDev& C = chains[c];
-        if (APR && C.apr != APR) continue;
-        const int apr = APR ? APR : C.apr;
-        const int K = C.kspec;                 // 1, 2 or 4
-        const int GS = NT / K;                 // threads per move
-        const int grp = tid / GS, tg = tid - grp * GS;
+        if (APR && chains[c].apr != APR) continue;
         __syncthreads();   // the previous chain's last reads of shared state are done
+        {
+            static_assert(sizeof(ChainDev) % 4 == 0, "ChainDev copied as words");
+            const int* src = reinterpret_cast<const int*>(&chains[c]);
+            int* dst = reinterpret_cast<int*>(&s_chain);
+            for (int k = tid; k < (int)(sizeof(ChainDev) / 4); k += NT) dst[k] = src[k];
+        }
+        __syncthreads();
+        const ChainDev& C = s_chain;
+        const int apr = APR ? APR : C.apr;
+        const int K = C.kspec;                 // 1, 2, 4 or 8; K * apr <= 32 and NT / K >= 32
+        const int GS = NT / K;                 // threads per move
+        const int WPG = GS >> 5;               // warps per move
+        const int grp = tid / GS, gw = (tid - grp * GS) >> 5;
+        const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
         for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
             s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
                                                           C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
@@ -368,181 +447,175 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
         cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
         cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
         ChainState S = state[c];
-        if (tid < KSPEC) s_prev_res[tid] = -1;
-        if (tid == 0) { s_err = 0; s_rebuild = 0; s_pairs = 0ull; }
+        if (tid == 0) { s_err = 0; s_pairs = 0ull; }
         __syncthreads();
         const int nmoves = C.nres;
         long long npairs = 0;
         uint4* Fc = F + C.atom0;
         ulonglong4* Mc = M + C.atom0;
-        int mv = 0;
+        int mv = 0, buf = 0;
+        unsigned prev_acc = 0;                 // accepted moves of the previous iteration (records P[buf ^ 1])
+        float eh = 0.0f, el = 0.0f;            // accepted dE of this sweep (float-float, warp 0 lane 0)
         while (mv < nmoves) {
-            const int kk = min(K, nmoves - mv);      // moves proposed this iteration
-            // ---- my group's move: residue and prefetch of its first neighbour atoms
+            const int kk = min(K, nmoves - mv);
             const bool gact = grp < kk;
-            const unsigned long long cnt = S.moves + (unsigned long long)(mv + (gact ? grp : 0));
-            const U4 r0 = philox4x32_10(U4{(uint32_t)cnt, (uint32_t)(cnt >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
-            const int res = (int)(((uint64_t)r0.y * (uint64_t)C.nres) >> 32);
-            const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
-            int nl = gact ? NL[C.res0 + res] : 0;
-            int qp[PF];
-            uint4 pbp[PF];
-#pragma unroll
-            for (int u = 0; u < PF; u++) {
-                const int t = tg + u * GS;
-                qp[u] = t < nl * apr ? row[t / apr] : 0;
-            }
-#pragma unroll
-            for (int u = 0; u < PF; u++) {
-                const int t = tg + u * GS;
-                pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
-            }
-            if (warp == 0) {
-                // ---- the kk proposals: lane = g * apr + k owns atom k of move g's residue
-                __syncwarp();
-                const int g = lane / apr, k = lane - g * apr;
-                const bool lact = g < kk;
-                const unsigned long long cg = S.moves + (unsigned long long)(mv + (lact ? g : 0));
+            MoveRec* R = P[buf ^ 1];
+            float acc = 0.0f;
+            int np = 0;
+            if (gact) {
+                // ---- the move of my group (every warp of the group, lanes = atoms)
+                const unsigned long long cg = S.moves + (unsigned long long)(mv + grp);
                 const U4 q0 = philox4x32_10(U4{(uint32_t)cg, (uint32_t)(cg >> 32), (uint32_t)c, 0u}, C.key0, C.key1);
                 const U4 q1 = philox4x32_10(U4{(uint32_t)cg, (uint32_t)(cg >> 32), (uint32_t)c, 1u}, C.key0, C.key1);
-                const int rg = (int)(((uint64_t)q0.y * (uint64_t)C.nres) >> 32);
+                const int res = (int)(((uint64_t)q0.y * (uint64_t)C.nres) >> 32);
                 const bool rot = C.ntypes_move == 2 && (q0.x & 1u);
                 const int piv = (int)(((uint64_t)q0.z * (uint64_t)apr) >> 32);
+                const int k = lane < apr ? lane : 0;
+                const int a = res * apr + k;
+                uint4 fo = Fc[a];
+                ulonglong4 mo = Mc[a];
+                const uint4 fb = FB[C.atom0 + a];
+                // records of the previous iteration: accepted moves whose commits may not have landed
+                unsigned sub = 0;
+                for (unsigned pm = prev_acc; pm; pm &= pm - 1) {
+                    const int h = __ffs(pm) - 1;
+                    if (R[h].res == res) {
+                        fo = R[h].fn[k];
+                        mo = make_ulonglong4(R[h].mn[k][0], R[h].mn[k][1], R[h].mn[k][2], 0ull);
+                    }
+                }
+                const uint4 fo0 = make_uint4(__shfl_sync(0xffffffffu, fo.x, 0), __shfl_sync(0xffffffffu, fo.y, 0),
+                                             __shfl_sync(0xffffffffu, fo.z, 0), 0u);
+                for (unsigned pm = prev_acc; pm; pm &= pm - 1) {
+                    const int h = __ffs(pm) - 1;
+                    const float dx = fdelta(fo0.x, R[h].fo0.x, Ls0, Ll0), dy = fdelta(fo0.y, R[h].fo0.y, Ls1, Ll1),
+                                dz = fdelta(fo0.z, R[h].fo0.z, Ls2, Ll2);
+                    if (dx * dx + dy * dy + dz * dz <= G.subst2) sub |= 1u << h;
+                }
                 const float ct = 2.0f * u01f(q0.w) - 1.0f;   // uniform direction: cos(theta), phi
                 const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
                 float sphi, cphi;
                 sincospif(2.0f * u01f(q1.x), &sphi, &cphi);
                 const float ux = st * cphi, uy = st * sphi, uz = ct;
-                const int a = rg * apr + (lact ? k : 0);
-                const uint4 fo = Fc[a];
-                // the rotation pivot is atom piv of the same move, owned by lane g * apr + piv
-                const int pl = min(31, (lact ? g : 0) * apr + piv);
-                const uint4 fp = make_uint4(__shfl_sync(0xffffffffu, fo.x, pl), __shfl_sync(0xffffffffu, fo.y, pl),
-                                            __shfl_sync(0xffffffffu, fo.z, pl), 0u);
-                if (lact && g * apr + k == lane) {
-                    const ulonglong4 mo = Mc[a];
-                    const uint4 fb = FB[C.atom0 + a];
-                    float dx, dy, dz;
-                    if (!rot) {
-                        const float rad = C.dmax_trn * cbrtf(u01f(q1.y));
-                        dx = rad * ux; dy = rad * uy; dz = rad * uz;
-                    } else {
-                        // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
-                        // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
-                        float sh, ch;
-                        sincospif(C.dmax_rot * (2.0f * u01f(q1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
-                        const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
-                        const float ox = fdelta(fp.x, fo.x, C.Ls[0], C.Lsl[0]), oy = fdelta(fp.y, fo.y, C.Ls[1], C.Lsl[1]),
-                                    oz = fdelta(fp.z, fo.z, C.Ls[2], C.Lsl[2]);
-                        const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
-                        dx = qw * tx + (qy * tz - qz * ty);
-                        dy = qw * ty + (qz * tx - qx * tz);
-                        dz = qw * tz + (qx * ty - qy * tx);
+                float dx, dy, dz;
+                if (!rot) {
+                    const float rad = C.dmax_trn * cbrtf(u01f(q1.y));
+                    dx = rad * ux; dy = rad * uy; dz = rad * uz;
+                } else {
+                    // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
+                    // rotated offset minus offset = 2 q_w (q_v x o) + 2 q_v x (q_v x o)
+                    const uint32_t px = __shfl_sync(0xffffffffu, fo.x, piv), py = __shfl_sync(0xffffffffu, fo.y, piv),
+                                   pz = __shfl_sync(0xffffffffu, fo.z, piv);
+                    float sh, ch;
+                    sincospif(C.dmax_rot * (2.0f * u01f(q1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
+                    const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
+                    const float ox = fdelta(px, fo.x, Ls0, Ll0), oy = fdelta(py, fo.y, Ls1, Ll1),
+                                oz = fdelta(pz, fo.z, Ls2, Ll2);
+                    const float tx = 2.0f * (qy * oz - qz * oy), ty = 2.0f * (qz * ox - qx * oz), tz = 2.0f * (qx * oy - qy * ox);
+                    dx = qw * tx + (qy * tz - qz * ty);
+                    dy = qw * ty + (qz * tx - qx * tz);
+                    dz = qw * tz + (qx * ty - qy * tx);
+                }
+                const unsigned long long nx = mo.x + master_step(dx, C.tofix32[0]);
+                const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
+                const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
+                const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
+                const float mx = fdelta(fo.x, fn.x, Ls0, Ll0), my = fdelta(fo.y, fn.y, Ls1, Ll1),
+                            mz = fdelta(fo.z, fn.z, Ls2, Ll2);
+                const float ofx = fdelta(fo0.x, fo.x, Ls0, Ll0), ofy = fdelta(fo0.y, fo.y, Ls1, Ll1),
+                            ofz = fdelta(fo0.z, fo.z, Ls2, Ll2);
+                if (gw == 0) {
+                    MoveRec& Q = P[buf][grp];
+                    if (lane < apr) {
+                        Q.fn[lane] = fn;
+                        Q.mn[lane][0] = nx; Q.mn[lane][1] = ny; Q.mn[lane][2] = nz;
+                        Q.fb[lane] = fb;
                     }
-                    const unsigned long long nx = mo.x + master_step(dx, C.tofix32[0]);
-                    const unsigned long long ny = mo.y + master_step(dy, C.tofix32[1]);
-                    const unsigned long long nz = mo.z + master_step(dz, C.tofix32[2]);
-                    const uint4 fn = make_uint4((uint32_t)(nx >> 32), (uint32_t)(ny >> 32), (uint32_t)(nz >> 32), fo.w);
-                    Proposal& Q = P[g];
-                    Q.fo[k] = fo;
-                    Q.fn[k] = fn;
-                    Q.fb[k] = fb;
-                    Q.mn[k][0] = nx; Q.mn[k][1] = ny; Q.mn[k][2] = nz;
-                    Q.m[k][0] = fdelta(fo.x, fn.x, C.Ls[0], C.Lsl[0]);
-                    Q.m[k][1] = fdelta(fo.y, fn.y, C.Ls[1], C.Lsl[1]);
-                    Q.m[k][2] = fdelta(fo.z, fn.z, C.Ls[2], C.Lsl[2]);
-                    if (k == 0) {
-                        Q.res = rg;
-                        const double alpha = u01d_open0(q1.z, q1.w);
-                        Q.alpha = alpha;
-                        Q.lna = -__logf((float)alpha);
+                    if (lane == 0) {
+                        Q.fo0 = fo0;
+                        Q.res = res;
+                        Q.ahi = q1.z;
+                        Q.alo = q1.w;
+                        // alpha >= ahi / 2^32 and below it by < 2^-32: for ahi >= 2^16 the FP32
+                        // -ln(alpha) is within 2e-5 of the exact one, inside the decision margin
+                        Q.lna = q1.z >= 65536u ? -__logf(__uint2float_rn(q1.z) * 2.3283064365386963e-10f) : __int_as_float(0x7fc00000);
                     }
                 }
-            }
-            __syncthreads();
-            if (s_rebuild) {  // requested by the previous iteration: lists and prefetches are stale
-                chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
-                if (warp == 0) {
-                    const int g = lane / apr, k = lane - g * apr;
-                    if (g < kk) P[g].fb[k] = FB[C.atom0 + P[g].res * apr + k];
+                float m[A][3], off[A][3];
+#pragma unroll
+                for (int j = 0; j < A; j++) {
+                    m[j][0] = __shfl_sync(0xffffffffu, mx, j); m[j][1] = __shfl_sync(0xffffffffu, my, j);
+                    m[j][2] = __shfl_sync(0xffffffffu, mz, j);
+                    off[j][0] = __shfl_sync(0xffffffffu, ofx, j); off[j][1] = __shfl_sync(0xffffffffu, ofy, j);
+                    off[j][2] = __shfl_sync(0xffffffffu, ofz, j);
                 }
-                if (tid == 0) { s_rebuild = 0; S.rebuilds++; }
-                __syncthreads();
-                nl = gact ? NL[C.res0 + res] : 0;
+                // ---- neighbour atoms: compaction into the ring, evaluation 32 at a time
+                const bool wrap = C.wrap_offsets != 0;
+                auto eval = [&](const float4 v) {
+                    const uint32_t w = __float_as_uint(v.w);
 #pragma unroll
-                for (int u = 0; u < PF; u++) {
-                    const int t = tg + u * GS;
-                    qp[u] = t < nl * apr ? row[t / apr] : 0;
-                    pbp[u] = t < nl * apr ? Fc[qp[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
-                }
-            }
-            // ---- independent prefix (every thread computes it from the proposals)
-            int ng = 1;
-            for (int g = 1; g < kk; g++) {
-                bool ok = true;
-                for (int h = 0; h < g && ok; h++) {
-                    if (P[g].res == P[h].res) { ok = false; break; }
-                    const float dx = fdelta(P[h].fo[0].x, P[g].fo[0].x, C.Ls[0], C.Lsl[0]);
-                    const float dy = fdelta(P[h].fo[0].y, P[g].fo[0].y, C.Ls[1], C.Lsl[1]);
-                    const float dz = fdelta(P[h].fo[0].z, P[g].fo[0].z, C.Ls[2], C.Lsl[2]);
-                    ok = dx * dx + dy * dy + dz * dz > G.indep2;
-                }
-                if (!ok) break;
-                ng = g + 1;
-            }
-            // ---- dE of my group's move over its neighbour list
-            float acc = 0.0f;
-            if (grp < ng) {
-                const Proposal& Q = P[grp];
-                uint4 fo[APR ? APR : MAX_APR];
-                float m[APR ? APR : MAX_APR][3];
-                float off[APR ? APR : MAX_APR][3];   // atom k - atom 0 of the moved residue (old)
-#pragma unroll
-                for (int k = 0; k < (APR ? APR : MAX_APR); k++)
-                    if (k < apr) {
-                        fo[k] = Q.fo[k]; m[k][0] = Q.m[k][0]; m[k][1] = Q.m[k][1]; m[k][2] = Q.m[k][2];
-                        off[k][0] = fdelta(Q.fo[0].x, Q.fo[k].x, C.Ls[0], C.Lsl[0]);
-                        off[k][1] = fdelta(Q.fo[0].y, Q.fo[k].y, C.Ls[1], C.Lsl[1]);
-                        off[k][2] = fdelta(Q.fo[0].z, Q.fo[k].z, C.Ls[2], C.Lsl[2]);
-                    }
-                int np = 0;
-                // an atom farther than rc + extent + largest move from the moved residue's first atom
-                // cannot be within rc of any of its atoms, old or new
-#pragma unroll 1
-                for (int t = tg, u = 0; t < nl * apr; t += GS, u++) {
-                    int q = 0;
-                    uint4 pb = make_uint4(0, 0, 0, 0);
-                    const int b = t - (t / apr) * apr;
-                    if (u < PF) {
-#pragma unroll
-                        for (int v = 0; v < PF; v++) if (v == u) { q = qp[v]; pb = pbp[v]; }
-                    } else { q = row[t / apr]; pb = Fc[q * apr + b]; }
-#pragma unroll
-                    for (int v = 0; v < KSPEC; v++)
-                        if (v < K && q == s_prev_res[v]) pb = s_prev_fn[v][b];
-                    const float d0x = fdelta(fo[0].x, pb.x, C.Ls[0], C.Lsl[0]), d0y = fdelta(fo[0].y, pb.y, C.Ls[1], C.Lsl[1]),
-                                d0z = fdelta(fo[0].z, pb.z, C.Ls[2], C.Lsl[2]);
-                    if (d0x * d0x + d0y * d0y + d0z * d0z > G.skip2) continue;
-#pragma unroll
-                    for (int k = 0; k < (APR ? APR : MAX_APR); k++) {
-                        if (k >= apr) break;
-                        const float4 tb = s_tab[fo[k].w][pb.w];
-                        // b - a_k = (b - a_0) - (a_k - a_0), back to the minimum image in small boxes
-                        float dx = k ? d0x - off[k][0] : d0x;
-                        float dy = k ? d0y - off[k][1] : d0y;
-                        float dz = k ? d0z - off[k][2] : d0z;
-                        if (C.wrap_offsets) {
-                            dx -= (dx > C.Lhalf[0]) ? C.Lf[0] : ((dx < -C.Lhalf[0]) ? -C.Lf[0] : 0.0f);
-                            dy -= (dy > C.Lhalf[1]) ? C.Lf[1] : ((dy < -C.Lhalf[1]) ? -C.Lf[1] : 0.0f);
-                            dz -= (dz > C.Lhalf[2]) ? C.Lf[2] : ((dz < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
+                    for (int j = 0; j < A; j++) {
+                        if (j >= apr) break;
+                        const float4 tb = s_tab[j][w];
+                        // b - a_j = (b - a_0) - (a_j - a_0), back to the minimum image in small boxes
+                        float ex = j ? v.x - off[j][0] : v.x;
+                        float ey = j ? v.y - off[j][1] : v.y;
+                        float ez = j ? v.z - off[j][2] : v.z;
+                        if (wrap) {
+                            ex -= (ex > C.Lhalf[0]) ? C.Lf[0] : ((ex < -C.Lhalf[0]) ? -C.Lf[0] : 0.0f);
+                            ey -= (ey > C.Lhalf[1]) ? C.Lf[1] : ((ey < -C.Lhalf[1]) ? -C.Lf[1] : 0.0f);
+                            ez -= (ez > C.Lhalf[2]) ? C.Lf[2] : ((ez < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
                         }
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
-                        acc += mixed_pair_delta(dx, dy, dz, m[k][0], m[k][1], m[k][2], tb.x, tb.y, tb.z, cut, np);
+                        acc += mixed_pair_delta(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, cut, np);
+                    }
+                };
+                const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
+                const int nitems = NL[C.res0 + res] * apr;
+                int head = 0, tail = 0;
+                constexpr int CH = 4;
+                for (int base = gw * 32; base < nitems; base += CH * GS) {
+                    int q[CH];
+                    uint4 pb[CH];
+#pragma unroll
+                    for (int u = 0; u < CH; u++) {
+                        const int t = base + u * GS + lane;
+                        q[u] = t < nitems ? row[t / apr] : -1;
+                    }
+#pragma unroll
+                    for (int u = 0; u < CH; u++) {
+                        const int t = base + u * GS + lane;
+                        pb[u] = q[u] >= 0 ? Fc[q[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < CH; u++) {
+                        if (base + u * GS >= nitems) break;
+                        const int t = base + u * GS + lane;
+                        if (sub) {
+                            for (unsigned pm = sub; pm; pm &= pm - 1) {
+                                const int h = __ffs(pm) - 1;
+                                if (q[u] == R[h].res) pb[u] = R[h].fn[t - (t / apr) * apr];
+                            }
+                        }
+                        const float ex = fdelta(fo0.x, pb[u].x, Ls0, Ll0), ey = fdelta(fo0.y, pb[u].y, Ls1, Ll1),
+                                    ez = fdelta(fo0.z, pb[u].z, Ls2, Ll2);
+                        const bool keep = q[u] >= 0 && ex * ex + ey * ey + ez * ez <= G.skip2;
+                        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                        if (keep) ring[(head + __popc(bal & lt_mask)) & (RING - 1)] = make_float4(ex, ey, ez, __uint_as_float(pb[u].w));
+                        head += __popc(bal);
+                        if (head - tail >= 32) {
+                            __syncwarp();
+                            eval(ring[(tail + lane) & (RING - 1)]);
+                            tail += 32;
+                            __syncwarp();
+                        }
                     }
                 }
-                npairs += np;
+                __syncwarp();
+                if (lane < head - tail) eval(ring[(tail + lane) & (RING - 1)]);
+                __syncwarp();
             }
-            // float-float warp reduction (TwoSum); a group's warps are consecutive
+            // float-float warp reduction (TwoSum) of the warp's share of its move's dE
             float hi = acc, lo = 0.0f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -552,74 +625,115 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 hi = sm;
                 lo = lo + ol + e;
             }
-            if (lane == 0) s_red[warp] = make_float2(hi, lo);
+            if (lane == 0) s_red[buf][warp] = make_float2(hi, lo);
             __syncthreads();
-            if (warp == 0) {
-                // lane g < ng: dE of move g from its group's warp partials, in warp order
-                const int wpg = GS / 32;
-                double de = 0.0;
-                bool accept = false;
-                if (lane < ng) {
-                    float h = 0.0f, l = 0.0f;
-                    for (int w = 0; w < wpg; w++) {
-                        const float2 v = s_red[lane * wpg + w];
-                        float sm, e;
-                        two_sum(h, v.x, sm, e);
-                        h = sm;
-                        l = l + v.y + e;
-                    }
-                    de = (double)h + (double)l;
-                    // Metropolis test alpha < exp(-beta dE) (MC_metropolis.cpp:175-204), decided in
-                    // FP32 when the margin is clear and in FP64 otherwise
-                    const Proposal& Q = P[lane];
-                    if (de <= 2.220446049250313e-16) accept = true;
-                    else {
-                        const double tt = C.beta * de;
-                        const float tf = (float)tt;
-                        if (tf < Q.lna - 1e-4f * fmaxf(1.0f, Q.lna)) accept = true;
-                        else if (tf > Q.lna + 1e-4f * fmaxf(1.0f, Q.lna)) accept = false;
-                        else accept = Q.alpha < exp(-tt);
-                    }
+            // ---- decisions, identical in every warp: lane g < kk holds move g
+            const MoveRec* Q = P[buf];
+            float deh = 0.0f, del = 0.0f;           // dE of move `lane` as a float-float pair
+            bool acc_raw = false;
+            unsigned cm = 0;                        // earlier moves of the iteration move g may interact with
+            {
+                // lane = g * WPG + w holds warp w's partial of move g; segmented butterfly over w
+                float2 v = lane < NW ? s_red[buf][lane] : make_float2(0.0f, 0.0f);
+                for (int o = 1; o < WPG; o <<= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, v.x, o), ol = __shfl_xor_sync(0xffffffffu, v.y, o);
+                    float sm, e;
+                    two_sum(v.x, oh, sm, e);
+                    v.x = sm;
+                    v.y = v.y + ol + e;
                 }
-                const unsigned accmask = __ballot_sync(0xffffffffu, accept);
-                // commits: lane = g * apr + k
-                const int g = lane / apr, k = lane - g * apr;
-                bool far = false;
-                if (g < ng) {
-                    const Proposal& Q = P[g];
-                    if ((accmask >> g) & 1u) {
-                        const int a = Q.res * apr + k;
-                        Mc[a] = make_ulonglong4(Q.mn[k][0], Q.mn[k][1], Q.mn[k][2], 0ull);
-                        Fc[a] = Q.fn[k];
-                        const float ex = fdelta(Q.fb[k].x, Q.fn[k].x, C.Ls[0], C.Lsl[0]);
-                        const float ey = fdelta(Q.fb[k].y, Q.fn[k].y, C.Ls[1], C.Lsl[1]);
-                        const float ez = fdelta(Q.fb[k].z, Q.fn[k].z, C.Ls[2], C.Lsl[2]);
-                        far = ex * ex + ey * ey + ez * ez > G.half_skin2;
-                        s_prev_fn[g][k] = Q.fn[k];
-                    }
+                const int src = (lane < kk ? lane : 0) * WPG;
+                deh = __shfl_sync(0xffffffffu, v.x, src);
+                del = __shfl_sync(0xffffffffu, v.y, src);
+            }
+            if (lane < kk) {
+                // Metropolis test (MC_metropolis.cpp:175-204): accept when dE <= DBL_EPSILON, else
+                // when alpha < exp(-beta dE).  Decided in FP32 when the margin is clear (FP32 dE and
+                // beta are within 1e-6 relative), in FP64 otherwise.
+                const float hf = deh + del;
+                bool exact = false;
+                if (hf <= 0.0f) acc_raw = true;
+                else if (hf < 1e-12f) exact = true;
+                else {
+                    const float tf = C.beta_f * hf, lna = Q[lane].lna;
+                    if (tf < lna - 1e-4f * fmaxf(1.0f, lna)) acc_raw = true;
+                    else if (tf > lna + 1e-4f * fmaxf(1.0f, lna)) acc_raw = false;
+                    else exact = true;              // also when lna is NaN
                 }
-                if (lane < KSPEC) s_prev_res[lane] = (lane < ng && ((accmask >> lane) & 1u)) ? P[lane].res : -1;
-                if (__any_sync(0xffffffffu, far) && lane == 0) s_rebuild = 1;
-                // statistics and the running energy, in move order
-                for (int gg = 0; gg < ng; gg++) {
-                    const double d = __shfl_sync(0xffffffffu, de, gg);
+                if (exact) {
+                    const double de = (double)deh + (double)del;
+                    acc_raw = de <= 2.220446049250313e-16 || u01d_open0(Q[lane].ahi, Q[lane].alo) < exp(-C.beta * de);
+                }
+                for (int h = 0; h < lane; h++) {
+                    const float dx = fdelta(Q[h].fo0.x, Q[lane].fo0.x, Ls0, Ll0);
+                    const float dy = fdelta(Q[h].fo0.y, Q[lane].fo0.y, Ls1, Ll1);
+                    const float dz = fdelta(Q[h].fo0.z, Q[lane].fo0.z, Ls2, Ll2);
+                    if (Q[h].res == Q[lane].res || dx * dx + dy * dy + dz * dz <= G.indep2) cm |= 1u << h;
+                }
+            }
+            const unsigned araw = __ballot_sync(0xffffffffu, acc_raw);
+            unsigned accmask = 0;
+            int ng = kk;
+            for (int g = 0; g < kk; g++) {
+                const unsigned cmg = __shfl_sync(0xffffffffu, cm, g);
+                if (cmg & accmask) { ng = g; break; }
+                accmask |= araw & (1u << g);
+            }
+            // far check of the accepted moves (lane = g * apr + j) and the commits
+            bool far = false;
+            {
+                const int g = lane / apr, j = lane - g * apr;
+                float e2 = 0.0f;
+                if (g < ng && ((accmask >> g) & 1u)) {
+                    const float ex = fdelta(Q[g].fb[j].x, Q[g].fn[j].x, Ls0, Ll0);
+                    const float ey = fdelta(Q[g].fb[j].y, Q[g].fn[j].y, Ls1, Ll1);
+                    const float ez = fdelta(Q[g].fb[j].z, Q[g].fn[j].z, Ls2, Ll2);
+                    e2 = ex * ex + ey * ey + ez * ez;
+                    far = e2 > G.half_skin2;
+                }
+                if (warp == 0) {
+                    for (int o = 16; o > 0; o >>= 1) e2 = fmaxf(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+                    S.maxd2 = fmaxf(S.maxd2, e2);
+                }
+            }
+            if (gw == 0 && grp < ng && ((accmask >> grp) & 1u) && lane < apr) {   // commit: atom = lane
+                const int a = Q[grp].res * apr + lane;
+                Mc[a] = make_ulonglong4(Q[grp].mn[lane][0], Q[grp].mn[lane][1], Q[grp].mn[lane][2], 0ull);
+                Fc[a] = Q[grp].fn[lane];
+            }
+            if (grp < ng) npairs += np;
+            if (warp == 0) {   // statistics and the sweep's energy change, in move order
+                for (int g = 0; g < ng; g++) {
+                    const float dh = __shfl_sync(0xffffffffu, deh, g), dl = __shfl_sync(0xffffffffu, del, g);
                     if (lane == 0) {
                         S.trials++;
-                        if ((accmask >> gg) & 1u) { S.accepted++; S.etot += d; }
+                        if ((accmask >> g) & 1u) {
+                            S.accepted++;
+                            float sm, e;
+                            two_sum(eh, dh, sm, e);
+                            eh = sm;
+                            el = el + dl + e;
+                        }
                     }
                 }
             }
             mv += ng;
+            prev_acc = accmask;
+            buf ^= 1;
+            if (__any_sync(0xffffffffu, far)) {   // identical in every warp
+                __syncthreads();                  // the commits have landed
+                chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err,
+                                   reinterpret_cast<uint4*>(ring));
+                if (tid == 0) { S.rebuilds++; S.maxd2 = 0.0f; }
+                prev_acc = 0;
+            }
         }
         __syncthreads();
-        if (s_rebuild) {
-            chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err);
-            if (tid == 0) S.rebuilds++;
-        }
         for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
         if (lane == 0) atomicAdd(&s_pairs, (unsigned long long)npairs);
         __syncthreads();
         if (tid == 0) {
+            S.etot += (double)eh + (double)el;
             S.pairs += (long long)s_pairs;
             S.moves += (unsigned long long)nmoves;
             if (s_err) S.err = s_err;
@@ -812,7 +926,9 @@ struct mcg_batch {
     uint4 *d_F = nullptr, *d_FB = nullptr;
     uint16_t* d_LST = nullptr;
     int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr, *d_gstarts = nullptr, *d_res_chain = nullptr;
-    uint4* d_gpos = nullptr;      // first-atom positions in cell order (list builds)
+    uint4* d_gpos = nullptr;      // first-atom positions in cell order, w = residue (list builds)
+    int *d_item_chain = nullptr, *d_chain_item0 = nullptr, *d_build = nullptr;
+    int nitems = 0;               // list-build work items (home cells, or 32-residue chunks) of all chains
     double* d_prm = nullptr;
     int* d_tile_chain = nullptr;
     int* d_tile_first = nullptr;
@@ -836,27 +952,33 @@ struct mcg_batch {
         if (tgraph) cudaGraphExecDestroy(tgraph);
         for (cudaEvent_t e : tev) if (e) cudaEventDestroy(e);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
-                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos};
+                     d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos, d_item_chain,
+                     d_chain_item0, d_build};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
     }
-    // list rebuild of every chain: per-chain binning, then one warp per residue over the GPU
-    int launch_build(cudaStream_t st) {
-        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, d_gpos, nchains);
-        const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
+    // list build: per-chain binning (every chain when force, else the chains that moved enough),
+    // then one warp per home cell of the binned chains over the GPU
+    int launch_build(cudaStream_t st, int force) {
+        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, d_gpos, d_state, d_build,
+                                             G.pre2, force, nchains);
+        const int blocks = (int)std::min<int64_t>((nitems + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_lists<3><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
+            k_batch_lists<3><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_item_chain, d_chain_item0, d_gstarts, d_gorder, d_gpos,
+                                                     d_LST, d_NL, d_state, d_build, nitems);
         else if (apr_all == 1)
-            k_batch_lists<1><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
+            k_batch_lists<1><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_item_chain, d_chain_item0, d_gstarts, d_gorder, d_gpos,
+                                                     d_LST, d_NL, d_state, d_build, nitems);
         else
-            k_batch_lists<0><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_res_chain, d_gstarts, d_gorder, d_gpos, d_LST, d_NL, d_state, nres);
+            k_batch_lists<0><<<blocks, 256, 0, st>>>(d_chains, G, d_F, d_item_chain, d_chain_item0, d_gstarts, d_gorder, d_gpos,
+                                                     d_LST, d_NL, d_state, d_build, nitems);
         BK(cudaGetLastError());
         launches += 2;
         return MCG_OK;
     }
-    int launch_build() { return launch_build(stream); }
+    int launch_build() { return launch_build(stream, 1); }
     int launch_energy_list() {
         int r;
         if (!d_eres && (r = balloc_d(&d_eres, (size_t)nres))) return r;
@@ -879,7 +1001,7 @@ struct mcg_batch {
         BK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t er = cudaSuccess;
         if (timed) er = cudaEventRecordWithFlags(tev[0], stream, cudaEventRecordExternal);
-        int r = er == cudaSuccess ? launch_build(stream) : MCG_ECUDA;
+        int r = er == cudaSuccess ? launch_build(stream, 0) : MCG_ECUDA;
         if (!r && timed) er = cudaEventRecordWithFlags(tev[1], stream, cudaEventRecordExternal);
         if (!r && er == cudaSuccess) r = launch_sweep(stream);
         if (!r && timed) er = cudaEventRecordWithFlags(tev[2], stream, cudaEventRecordExternal);
@@ -945,7 +1067,12 @@ struct mcg_batch {
     }
     // Speculation width of every chain: the box-size heuristic (cap 0) or min(cap, geometric limit).
     void set_speculation(int cap) {
-        for (int c = 0; c < nchains; c++) chains[c].kspec = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
+        for (int c = 0; c < nchains; c++) {
+            int k = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
+            // a group is whole warps, and one warp holds the atoms of all moves of an iteration
+            while (k > 1 && (k > threads / 32 || k * chains[c].apr > 32)) k >>= 1;
+            chains[c].kspec = k;
+        }
         spec_cap = cap;
     }
     // Launch shape of the sweep; takes effect at the next sweep (the graphs are captured again).
@@ -1050,6 +1177,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         }
         C.beta = 1.0 / ((RBOLTZUI / KCALTOIU) * hs.temp);
         if (opts->acceptance_units == MCG_ACCEPT_PHYSICAL) C.beta /= KCALTOIU;
+        C.beta_f = (float)C.beta;
         C.dmax_trn = (float)opts->dmax_trn;
         C.dmax_rot = (float)opts->dmax_rot;
         C.ntypes_move = apr > 1 ? 2 : 1;
@@ -1108,6 +1236,11 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
     const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
     G.indep2 = (float)(rind * rind);
+    G.pre2 = (float)((0.55 * 0.5 * skin) * (0.55 * 0.5 * skin));
+    {
+        const double rs = rlist + 2 * rext + skin + 0.01;
+        G.subst2 = (float)(rs * rs);
+    }
     for (auto& C : B->chains) {
         for (int k = 0; k < 3; k++) {
             if (rc + mmax > 0.5 * C.L[k])
@@ -1122,8 +1255,18 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
             const double vol = C.L[0] * C.L[1] * C.L[2];
             const double frac = 4.0 / 3.0 * PI * rind * rind * rind / vol;
             const bool any_half = rind > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]));
-            B->kgeom.push_back(any_half ? 1 : 4);
-            B->kheur.push_back((any_half || frac > 0.35) ? 1 : (frac > 0.12 ? 2 : 4));
+            // a move is re-proposed when an earlier accepted move of its group may interact with
+            // it (probability ~ frac * acceptance, ~0.45 assumed); take the widest group whose
+            // expected number of standing moves is >= 0.7 of its width
+            const double pc = std::min(1.0, frac * 0.45);
+            int kh = 1;
+            for (int kw : {2, 4, 8}) {
+                double e = 0.0, surv = 1.0;
+                for (int g = 0; g < kw; g++) { e += surv; surv *= std::pow(1.0 - pc, g + 1); }
+                if (e >= 0.7 * kw) kh = kw;
+            }
+            B->kgeom.push_back(any_half ? 1 : KMAX);
+            B->kheur.push_back(any_half ? 1 : kh);
         }
         if (!C.use_cells) C.nc[0] = C.nc[1] = C.nc[2] = 1;
     }
@@ -1140,8 +1283,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     B->threads = opts->threads_per_chain > 0 ? opts->threads_per_chain : 512;
     if (B->threads != 128 && B->threads != 256 && B->threads != 512)
         return fail(MCG_EINVAL, "threads_per_chain must be 128, 256 or 512");
-    if (opts->speculation < 0 || opts->speculation == 3 || opts->speculation > 4)
-        return fail(MCG_EINVAL, "speculation must be 0, 1, 2 or 4");
+    if (opts->speculation < 0 || (opts->speculation & (opts->speculation - 1)) || opts->speculation > KMAX)
+        return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4 or 8");
     if (opts->ctas_per_sm < 0 || opts->ctas_per_sm > 8) return fail(MCG_EINVAL, "ctas_per_sm must be in [0, 8]");
     B->set_speculation(opts->speculation);
     int dev = 0;
@@ -1198,6 +1341,20 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if ((r = balloc(&B->d_tile_chain, tc.size())) || (r = balloc(&B->d_tile_first, tf.size())) || (r = balloc(&B->d_part, tc.size())))
         return r;
     BK(cudaMemcpyAsync(B->d_tile_chain, tc.data(), sizeof(int) * tc.size(), cudaMemcpyHostToDevice, B->stream));
+    {
+        std::vector<int> ic, i0(nchains);
+        for (int c = 0; c < nchains; c++) {
+            const ChainDev& C = B->chains[c];
+            const int n = C.use_cells ? C.nc[0] * C.nc[1] * C.nc[2] : (C.nres + 31) / 32;
+            i0[c] = (int)ic.size();
+            ic.insert(ic.end(), n, c);
+        }
+        B->nitems = (int)ic.size();
+        if ((r = balloc(&B->d_item_chain, ic.size())) || (r = balloc(&B->d_chain_item0, nchains)) || (r = balloc(&B->d_build, nchains)))
+            return r;
+        BK(cudaMemcpy(B->d_item_chain, ic.data(), sizeof(int) * ic.size(), cudaMemcpyHostToDevice));
+        BK(cudaMemcpy(B->d_chain_item0, i0.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice));
+    }
     BK(cudaMemcpyAsync(B->d_tile_first, tf.data(), sizeof(int) * tf.size(), cudaMemcpyHostToDevice, B->stream));
     B->cut64.mode = 1;
     B->cut64.c2 = rc * rc; B->cut64.n2 = ron * ron;
@@ -1320,7 +1477,7 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     }
     static const int kThreads[] = {256, 512};
     static const int kCtas[] = {1, 2};
-    static const int kSpec[] = {1, 2, 4, 0};
+    static const int kSpec[] = {1, 2, 4, 8, 0};
     best.ms_per_sweep = 3.0e38f;
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
     for (int th : kThreads)
@@ -1473,6 +1630,14 @@ int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double*
     BK(cudaMemcpyAsync(b->d_state + chain, &st[chain], sizeof(ChainState), cudaMemcpyHostToDevice, b->stream));
     BK(cudaStreamSynchronize(b->stream));
     return MCG_OK;
+}
+
+int mcg_batch_update_lists(mcg_batch* b) {
+    if (!b) return fail(MCG_EINVAL, "null handle");
+    int r = b->launch_build();
+    if (r) return r;
+    BK(cudaStreamSynchronize(b->stream));
+    return mcg_batch_stats(b, nullptr, nullptr, nullptr);
 }
 
 int64_t mcg_batch_natoms(mcg_batch* b) { return b ? b->natoms : 0; }

@@ -147,18 +147,17 @@ namespace mcg {
 //   S_b - S_a = sw2 du' [2 A_a^2 - (A_a + A_b) B_b],  A = c2 - u, B = c2 + 2u - 3 n2
 // on the switch polynomial (u clamped to [n2, c2]).  LJ is small at these distances and is
 // differenced directly.  Pairs crossing the cutoff fall back to the direct difference.
-// npair counts pair interactions (inside the cutoff before or after the move).  Branch-free
-// apart from the early exit for a pair outside the cutoff both before and after, so a warp whose
-// lanes hold pairs in different regions (inner, switch, crossing the cutoff) does not execute
-// every region's code in turn.
+// npair counts pair interactions (inside the cutoff before or after the move).  Straight-line
+// code: a pair outside the cutoff before and after gets switch factors 0 and contributes +-0, so
+// a warp whose lanes hold pairs in different regions (inner, switch, outside, crossing the cutoff)
+// executes one path, and independent calls interleave.  Needs r > 0 (distinct atoms).
 __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float doz, float mx, float my, float mz,
                                                   float qk, float e4, float ss, const CutDev& c, int& npair) {
     const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
     const float uo = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
     const float un = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
     const bool io = uo <= c.c2f, in = un <= c.c2f;
-    if (!io && !in) return 0.0f;
-    npair++;
+    npair += (io || in) ? 1 : 0;
     const float ro = rsqrtf(uo), rn = rsqrtf(un);
     // switch S(u) = (c2-u)^2 (c2+2u-3n2) sw2 above n2, 1 below; evaluated on u clamped to [n2, c2]
     const float ua = fmaxf(uo, c.n2f), ub = fmaxf(un, c.n2f);

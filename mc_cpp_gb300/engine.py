@@ -215,6 +215,9 @@ class BatchChains:
         native.check(native.lib().mcg_batch_pairs(self.h, p.ctypes.data_as(native._i64)))
         return p
 
+    def update_lists(self) -> None:
+        native.check(native.lib().mcg_batch_update_lists(self.h))
+
     def energy_fp64(self) -> np.ndarray:
         e = np.zeros(self.nchains)
         native.check(native.lib().mcg_batch_energy_fp64(self.h, native.pd(e)))

@@ -121,6 +121,7 @@ def lib():
         "mcg_batch_run_host": (C.c_int, [P, _d, C.c_int, _d, _i64, _d]),
         "mcg_batch_energy_mixed": (C.c_int, [P, _d]),
         "mcg_batch_pairs": (C.c_int, [P, _i64]),
+        "mcg_batch_update_lists": (C.c_int, [P]),
         "mcg_probe_fp32_tflops": (C.c_int, [_d]),
         "mcg_energy_switch_fp64_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                      C.c_int, _d, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),

@@ -58,6 +58,7 @@ def test_sweeps_keep_running_energy_and_geometry():
     e = B.energy_fp64()
     rel = np.abs(etot - e) / np.abs(e)
     assert rel.max() <= 1e-6, rel
+    assert (np.abs(B.energy_mixed() - e) / np.abs(e)).max() <= 1e-6
     for k, s in enumerate(ch):
         xyz = B.coords(k)
         want = _oracle_nonbonded(s, xyz)
@@ -95,10 +96,32 @@ def test_list_rebuilds_keep_energy_exact():
     B = BatchChains(ch, seed=12)
     B.sweep(3)
     rb, _ = B.counters()
-    assert rb > 0
+    assert rb >= 10           # list builds of both chains, most of them inside the sweeps
     _, _, etot = B.stats()
     e = B.energy_fp64()
     assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+    # the lists in place after the sweeps still hold every pair inside the cutoff
+    assert (np.abs(B.energy_mixed() - e) / np.abs(e)).max() <= 1e-6
+
+
+def test_lists_kept_between_sweeps_stay_complete():
+    """Chains keep their lists across sweeps until their atoms have moved enough; the lists in
+    place after every sweep must still hold every pair inside the cutoff."""
+    ch = _waters((900, 2600, 5000), seed=47)
+    B = BatchChains(ch, seed=19)
+    e0 = B.energy_fp64()
+    rb0, _ = B.counters()
+    for k in range(6):
+        B.sweep(1)
+        kept = B.energy_mixed()           # over the lists in place
+        rb, _ = B.counters()
+        B.update_lists()
+        fresh = B.energy_mixed()          # over lists built from the current coordinates
+        # the same pairs in another order: equal to the last bits of a float-float sum; a missing
+        # pair would change the total by 10-10^4 iu
+        assert np.all(np.abs(kept - fresh) <= 1e-9 * np.abs(fresh) + 1e-3), (k, kept, fresh)
+    assert rb - rb0 < 3 * 6 + 5        # fewer builds than one per chain and sweep (plus the forced ones)
+    assert not np.allclose(B.energy_fp64(), e0)
 
 
 def test_argon_chains_and_mixed_residue_sizes():
@@ -178,7 +201,8 @@ def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch)
     assert t["speculation"] in (0, 1, 2, 4) and t["ms_per_sweep"] > 0 and not t["from_cache"]
     assert {k: t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")} == B.tuning()
     tr, a, etot = B.stats()
-    assert np.all(tr == 16 * 2 * (B.sizes // 3))      # 16 shapes x (1 warm-up + 1 timed sweep)
+    sweeps = tr // (B.sizes // 3)                      # every shape: 1 warm-up + 1 timed sweep
+    assert np.all(tr == sweeps * (B.sizes // 3)) and np.all(sweeps == sweeps[0]) and sweeps[0] >= 8
     B.sweep(2)
     _, _, etot = B.stats()
     e = B.energy_fp64()
