@@ -49,10 +49,18 @@ enum mcg_acceptance {
     MCG_ACCEPT_PHYSICAL = 1   /* beta applied to dE in kcal/mol */
 };
 
+enum mcg_units {
+    MCG_UNITS_FILE = 0,       /* forcefield-file units, converted here as IO_MDBAS::read_ff does */
+    MCG_UNITS_INTERNAL = 1    /* already converted (AtomList / Bond / Angle / Dihedral after IO_MDBAS):
+                                 eps = sqrt(eps_file * 418.4), k in iu, theta0 and phi0 in radians */
+};
+
 /* One system: what the reference's Parser_XML + IO_MDBAS build (AtomList, PerConditions,
  * Ens_NVT, FField cut settings and the bonded lists).  Per-atom arrays have natom entries; topology
  * arrays hold 0-based atom indices; parameters are in forcefield-file units (kcal/mol, Angstrom,
- * degrees) and are converted exactly as IO_MDBAS::read_ff does (src/IO_MDBAS.cpp:186-467). */
+ * degrees) and are converted exactly as IO_MDBAS::read_ff does (src/IO_MDBAS.cpp:186-467), unless
+ * param_units says they are converted already.  Zero-initialise the struct: new fields default
+ * to 0. */
 typedef struct mcg_system_desc {
     int natom;
     const double *x, *y, *z;
@@ -73,6 +81,7 @@ typedef struct mcg_system_desc {
     int nangle; const int *angle_atoms; const int *angle_type; const double *angle_k, *angle_theta0;
     int ndihe;  const int *dihe_atoms;  const int *dihe_type, *dihe_order; const double *dihe_k, *dihe_phi0, *dihe_mult;
     int nimpr;  const int *impr_atoms;  const int *impr_type, *impr_order; const double *impr_k, *impr_phi0, *impr_mult;
+    int param_units;                /* enum mcg_units: how eps/eps14, force constants and angles are given */
 } mcg_system_desc;
 
 typedef struct mcg_system mcg_system;
@@ -212,6 +221,18 @@ int64_t mcg_batch_natoms(mcg_batch* b);
 int mcg_batch_chain_natoms(mcg_batch* b, int chain);
 /* Counters of the last sweeps: list rebuilds done, kernel launches issued by this handle. */
 int mcg_batch_counters(mcg_batch* b, int64_t* list_rebuilds, int64_t* kernel_launches);
+
+/* --- MDBAS input files ---------------------------------------------------------------------
+ * IO_MDBAS::read_coord + read_ff (src/IO_MDBAS.cpp:77-505) on the host: a .cor coordinate file
+ * and an MDBAS forcefield file read into library-owned arrays, in file units. */
+typedef struct mcg_mdbas mcg_mdbas;
+int mcg_mdbas_read(const char* cor_path, const char* ff_path, mcg_mdbas** out);
+int mcg_mdbas_natom(const mcg_mdbas* m);
+/* Point desc's atom and topology fields (natom .. impr_mult, param_units = MCG_UNITS_FILE) at m's
+ * arrays, valid until mcg_mdbas_free; the run settings (pbc, box, cut, temp, precision) are left
+ * as they are. */
+int mcg_mdbas_fill(const mcg_mdbas* m, mcg_system_desc* desc);
+int mcg_mdbas_free(mcg_mdbas* m);
 
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by an FFMA-chain kernel
  * (the denominator of the pair kernels' roofline). */

@@ -18,6 +18,8 @@ SRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libmcgpu.so")
+SHIM_SRC = os.path.join(HERE, "shim", "charmmene_gpu.cpp")
+SHIM = os.path.join(LIBDIR, "libcharmmene_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -62,16 +64,31 @@ def build(verbose: bool = False) -> str:
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, cuda), srcs))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [os.path.join(cuda, "bin", "nvcc")] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
-    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stdout))
-    os.replace(LIB + ".tmp", LIB)
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [os.path.join(cuda, "bin", "nvcc")] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + \
+              ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stdout))
+        os.replace(LIB + ".tmp", LIB)
+    _build_shim()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+def _build_shim() -> str:
+    """libcharmmene_gpu.so: the reference's Fortran/C energy interface on top of libmcgpu.so."""
+    deps = [SHIM_SRC, LIB, os.path.join(ROOT, "include", "charmmene_gpu.h"), os.path.join(ROOT, "include", "mcg.h")]
+    if os.path.exists(SHIM) and os.path.getmtime(SHIM) >= max(os.path.getmtime(d) for d in deps):
+        return SHIM
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", SHIM_SRC, "-I" + os.path.join(ROOT, "include"),
+           "-L" + LIBDIR, "-lmcgpu", "-Wl,-rpath,$ORIGIN", "-o", SHIM + ".tmp"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("shim build failed: %s\n%s" % (" ".join(cmd), r.stdout))
+    os.replace(SHIM + ".tmp", SHIM)
+    return SHIM
 
 
 if __name__ == "__main__":

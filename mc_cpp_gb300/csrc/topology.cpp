@@ -48,12 +48,15 @@ int build_host_system(const mcg_system_desc* d, HostSystem& hs) {
     };
     cp(d->x, hs.x, 0); cp(d->y, hs.y, 0); cp(d->z, hs.z, 0); cp(d->q, hs.q, 0);
     cp(d->sig, hs.sig, 0); cp(d->sig14, hs.sig14, 0); cp(d->mass, hs.mass, 1.0);
+    if (d->param_units != MCG_UNITS_FILE && d->param_units != MCG_UNITS_INTERNAL) return fail(MCG_EINVAL, "bad param_units");
+    const bool internal = d->param_units == MCG_UNITS_INTERNAL;
+    const double kscale = internal ? 1.0 : KCALTOIU;   // x * 1.0 is exact: internal values pass unchanged
     hs.eps.resize(n); hs.eps14.resize(n);
     for (int i = 0; i < n; i++) {
         // IO_MDBAS.cpp:460,464: epsilon stored as sqrt(eps_file * kcaltoiu)
         if (d->eps[i] < 0 || (d->eps14 && d->eps14[i] < 0)) return fail(MCG_EINVAL, "negative epsilon");
-        hs.eps[i] = std::sqrt(d->eps[i] * KCALTOIU);
-        hs.eps14[i] = std::sqrt((d->eps14 ? d->eps14[i] : 0.0) * KCALTOIU);
+        hs.eps[i] = internal ? d->eps[i] : std::sqrt(d->eps[i] * KCALTOIU);
+        hs.eps14[i] = internal ? (d->eps14 ? d->eps14[i] : 0.0) : std::sqrt((d->eps14 ? d->eps14[i] : 0.0) * KCALTOIU);
         if (!std::isfinite(hs.x[i]) || !std::isfinite(hs.y[i]) || !std::isfinite(hs.z[i]))
             return fail(MCG_EINVAL, "non-finite coordinate at atom " + std::to_string(i));
     }
@@ -66,27 +69,27 @@ int build_host_system(const mcg_system_desc* d, HostSystem& hs) {
     for (int k = 0; k < d->nbond; k++) {
         int a = d->bond_atoms[2 * k], b = d->bond_atoms[2 * k + 1];
         if (!inrange(a) || !inrange(b)) return fail(MCG_EINVAL, "bond atom out of range");
-        hs.bonds.push_back({a, b, d->bond_type ? d->bond_type[k] : 0, d->bond_k[k] * KCALTOIU, d->bond_r0[k],
+        hs.bonds.push_back({a, b, d->bond_type ? d->bond_type[k] : 0, d->bond_k[k] * kscale, d->bond_r0[k],
                             d->bond_beta ? d->bond_beta[k] : 0.0});
     }
     for (int k = 0; k < d->nub; k++) {
         int a = d->ub_atoms[2 * k], b = d->ub_atoms[2 * k + 1];
         if (!inrange(a) || !inrange(b)) return fail(MCG_EINVAL, "Urey-Bradley atom out of range");
-        hs.ubs.push_back({a, b, 0, d->ub_k[k] * KCALTOIU, d->ub_r0[k], 0.0});
+        hs.ubs.push_back({a, b, 0, d->ub_k[k] * kscale, d->ub_r0[k], 0.0});
     }
     for (int k = 0; k < d->nangle; k++) {
         const int* t = d->angle_atoms + 3 * k;
         if (!inrange(t[0]) || !inrange(t[1]) || !inrange(t[2])) return fail(MCG_EINVAL, "angle atom out of range");
-        hs.angles.push_back({t[0], t[1], t[2], d->angle_type ? d->angle_type[k] : 0, d->angle_k[k] * KCALTOIU,
-                             d->angle_theta0[k] * PI / 180.});
+        hs.angles.push_back({t[0], t[1], t[2], d->angle_type ? d->angle_type[k] : 0, d->angle_k[k] * kscale,
+                             internal ? d->angle_theta0[k] : d->angle_theta0[k] * PI / 180.});
     }
     auto tors = [&](int cnt, const int* at, const int* ty, const int* ord, const double* kk, const double* ph,
                     const double* mu, std::vector<TorsT>& out) -> int {
         for (int k = 0; k < cnt; k++) {
             const int* t = at + 4 * k;
             for (int j = 0; j < 4; j++) if (!inrange(t[j])) return fail(MCG_EINVAL, "torsion atom out of range");
-            out.push_back({t[0], t[1], t[2], t[3], ty ? ty[k] : 1, ord ? ord[k] : 1, kk[k] * KCALTOIU,
-                           ph[k] * PI / 180., mu ? mu[k] : 1.0});
+            out.push_back({t[0], t[1], t[2], t[3], ty ? ty[k] : 1, ord ? ord[k] : 1, kk[k] * kscale,
+                           internal ? ph[k] : ph[k] * PI / 180., mu ? mu[k] : 1.0});
         }
         return MCG_OK;
     };

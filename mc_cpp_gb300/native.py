@@ -52,6 +52,7 @@ class SystemDesc(C.Structure):
         ("dihe_phi0", _d), ("dihe_mult", _d),
         ("nimpr", C.c_int), ("impr_atoms", _i), ("impr_type", _i), ("impr_order", _i), ("impr_k", _d),
         ("impr_phi0", _d), ("impr_mult", _d),
+        ("param_units", C.c_int),
     ]
 
 
@@ -122,6 +123,10 @@ def lib():
         "mcg_batch_energy_mixed": (C.c_int, [P, _d]),
         "mcg_batch_pairs": (C.c_int, [P, _i64]),
         "mcg_batch_update_lists": (C.c_int, [P]),
+        "mcg_mdbas_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P)]),
+        "mcg_mdbas_natom": (C.c_int, [P]),
+        "mcg_mdbas_fill": (C.c_int, [P, C.POINTER(SystemDesc)]),
+        "mcg_mdbas_free": (C.c_int, [P]),
         "mcg_probe_fp32_tflops": (C.c_int, [_d]),
         "mcg_energy_switch_fp64_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                      C.c_int, _d, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),

@@ -64,7 +64,19 @@ $(OUT)/libcharmmene.so: $(OBJS) $(OUT)/obj/FORTRAN_interface.o
 $(OUT)/ref_probe: oracle/ref_probe.cpp $(OBJS)
 	$(CXX) $(CXXFLAGS) oracle/ref_probe.cpp $(OBJS) -o $@
 
+# FField_CUDA (mc_cpp_gb300/adapter/) compiled with the reference's headers and flags and linked
+# with the reference objects and libmcgpu.so: the drop-in as a maintainer would build it.
+LIBDIR   := mc_cpp_gb300/_lib
+$(OUT)/adapter_check: oracle/adapter_check.cpp mc_cpp_gb300/adapter/FField_CUDA.cpp mc_cpp_gb300/adapter/FField_CUDA.hpp \
+                      include/mcg.h $(OBJS) $(LIBDIR)/libmcgpu.so
+	$(CXX) $(CXXFLAGS) -Wall -Imc_cpp_gb300/adapter -Iinclude oracle/adapter_check.cpp mc_cpp_gb300/adapter/FField_CUDA.cpp \
+	    $(OBJS) -L$(LIBDIR) -lmcgpu -Wl,-rpath,$(abspath $(LIBDIR)) -o $@
+
+# exit status 0 when the reference sources are where REF points
+ref-present:
+	@test -f $(REF)/src/FField_MDBAS.cpp
+
 clean:
 	rm -rf $(OUT)
 
-.PHONY: all clean
+.PHONY: all clean ref-present
