@@ -289,6 +289,9 @@ def run_ours(args):
         rate, desc, cores = cpu_sample(chains, args.cpu_budget, host_threads())
         cpu = {"value": rate, "unit": "moves/s", "cores": cores, "kind": "port", "sample": desc}
     rb, nl = B.counters()
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = config_extras(tf.value)
     if rank == 0:
         line = {
             "metric": "accepted MC moves/s", "value": value, "unit": "moves/s", "n_gpus": world, "steps": args.steps,
@@ -316,12 +319,101 @@ def run_ours(args):
             "plain_fp64": plain,
             "batched_vs_plain_accepted": (value / plain["accepted_moves_per_s"]) if plain else None,
             "cpu_baseline": cpu,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     B.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ------------------------------------------------------------------ the other configurations
+def config_extras(tf_peak: float):
+    """The reference's other configurations, each bounded to a few seconds: the argon replay in
+    plain FP64 (the small CPU-runnable case), the solvated peptide in mixed precision with its
+    error against FP64, the 100,002-atom water box (full recomputes/s and dE/s in FP64 and mixed,
+    and the FP32 roofline of the mixed pair kernel), and 1024 batched argon chains."""
+    from mc_cpp_gb300 import systems
+    from mc_cpp_gb300.engine import BatchChains, FFieldCUDA
+    KCAL = 418.4
+    out = {}
+    # argon, 864 atoms, FP64, single-atom moves <= 0.2 A at 120 K, reference acceptance units
+    ff = FFieldCUDA(systems.argon_fcc(), "fp64")
+    ff.metropolis(200, 1, trace=False)
+    t = time.perf_counter()
+    _, _, nacc, _ = ff.metropolis(20000, 7, trace=False)
+    dt = time.perf_counter() - t
+    out["argon864_plain_fp64"] = {"moves_per_s": 20000 / dt, "accepted_moves_per_s": nacc / dt, "steps": 20000}
+    ff.close()
+    # solvated flexible peptide (40 atoms + 6000 waters): mixed precision against FP64
+    s = systems.peptide_in_water()
+    f64, fmx = FFieldCUDA(s, "fp64", moves=False), FFieldCUDA(s, "mixed", moves=False)
+    e64, emx = f64.getE(), fmx.getE()
+    rng = np.random.default_rng(5)
+    xyz = s.coords()
+    L = s.box[0]
+    errs = []
+    t_mx = 0.0
+    for k in range(300):
+        if k % 3 == 0:
+            idx = np.array([int(rng.integers(0, 40))])                         # a peptide atom
+        else:
+            r = int(rng.integers(2, s.resid.max() + 1))                          # a water residue
+            idx = np.nonzero(s.resid == r)[0]
+        new = xyz[idx] + rng.uniform(-0.15, 0.15, 3)
+        new -= L * np.round(new / L)
+        d64 = f64.delta_e(idx, new)
+        t = time.perf_counter()
+        dmx = fmx.delta_e(idx, new)
+        t_mx += time.perf_counter() - t
+        errs.append(abs(dmx - d64) / KCAL)
+    out["peptide_water_mixed"] = {"atoms": s.natom, "max_abs_dE_err_kcal_mol": float(max(errs)),
+                                  "rel_total_E_err": abs(emx - e64) / abs(e64), "dE_per_s_mixed": 300 / t_mx,
+                                  "moves": "300 random single-atom peptide and rigid-water displacements"}
+    f64.close(); fmx.close()
+    # 100,002-atom water box (33,334 molecules, 0.0334 mol/A^3), switch 10-12 A
+    w = systems.water_box(33334, seed=11)
+    res5 = {"atoms": w.natom}
+    for prec in ("fp64", "mixed"):
+        ff = FFieldCUDA(w, prec, moves=False)
+        ff.getE()
+        t = time.perf_counter()
+        for _ in range(10):
+            ff.getE()
+        rec = 10 / (time.perf_counter() - t)
+        rng = np.random.default_rng(9)
+        xyz = w.coords()
+        t = time.perf_counter()
+        for _ in range(1000):
+            r = int(rng.integers(1, w.resid.max() + 1))
+            idx = np.arange(3 * (r - 1), 3 * r)
+            ff.delta_e(idx, xyz[idx] + rng.uniform(-0.15, 0.15, 3))
+        des = 1000 / (time.perf_counter() - t)
+        lp, inc = ff.pair_count()
+        res5[prec] = {"recomputes_per_s": rec, "dE_per_s": des, "pair_interactions_per_s": inc * rec}
+        if prec == "mixed" and tf_peak:
+            res5[prec]["fp32_frac_of_probe"] = inc * rec * FLOPS_PER_PAIR / 1e12 / tf_peak
+        res5["list_pairs"], res5["pairs_in_cutoff"] = lp, inc
+        ff.close()
+    out["water100k"] = res5
+    # 1024 independent argon chains (500-2000 atoms, 0.015-0.025 atoms/A^3, 90-150 K), one batch
+    B = BatchChains(systems.argon_chains(), dmax_trn=0.2, dmax_rot=0.0, acceptance="physical", seed=3)
+    tune = B.autotune(trial_sweeps=1)
+    B.sweep(3)
+    t0, a0, _ = B.stats()
+    p0 = B.pairs()
+    tot, li, sw = B.time_phases(5)
+    t1, a1, _ = B.stats()
+    p1 = B.pairs()
+    out["argon1024_batched"] = {"accepted_moves_per_s": float((a1 - a0).sum()) / (tot * 1e-3),
+                                "trials_per_s": float((t1 - t0).sum()) / (tot * 1e-3),
+                                "pair_interactions_per_s": float((p1 - p0).sum()) / (tot * 1e-3),
+                                "fp32_frac_of_probe": (float((p1 - p0).sum()) * FLOPS_PER_PAIR / (sw * 1e-3) / 1e12 / tf_peak)
+                                if tf_peak else None,
+                                "atoms": int(B.natoms), "tuning": tune}
+    B.close()
+    return out
 
 
 def main():
@@ -338,6 +430,7 @@ def main():
     ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' figures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

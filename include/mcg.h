@@ -125,6 +125,10 @@ int mcg_commit(mcg_system* s);
  * getNeighPair/getNeighList).  counts[natom] always filled; entries (row-concatenated, each row
  * sorted ascending) filled when cap is large enough; *total = sum(counts). */
 int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);
+/* Pair counts of the current build.  Switch: the Verlet-list entries, and those within the cutoff
+ * at the current coordinates (FP64 minimum-image distances).  Full: both are the number of pairs
+ * the full energy sums (every pair i < j outside the exclusion rows). */
+int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
 /* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
  * exclList[i]) and the 1-4 pair list (getNeighList14). */
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);

@@ -5,6 +5,7 @@
 // operation order as Move.hpp, so the coordinates the device sees are the reference's.
 #include <cfloat>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -95,6 +96,45 @@ int mcg_commit(mcg_system* s) {
 int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {
     if (!s || !counts) return fail(MCG_EINVAL, "null argument");
     return s->eng.get_pairlist(counts, entries, cap, total);
+}
+
+int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff) {
+    if (!s || !list_pairs || !in_cutoff) return fail(MCG_EINVAL, "null argument");
+    const HostSystem& h = s->eng.hs;
+    const int n = h.n;
+    std::vector<double> x(n), y(n), z(n);
+    int r = s->eng.get_coords(x.data(), y.data(), z.data());
+    if (r) return r;
+    const double c2 = h.rc * h.rc;
+    auto mic = [&](double d, int k) {
+        // PerConditions::applyPBC: d -= L * rint(d / L), rint rounding half away from zero
+        if (h.pbc == MCG_PBC_NONE) return d;
+        const double t = d * h.rL[k];
+        return d - h.L[k] * (double)(int64_t)(t + (t >= 0 ? 0.5 : -0.5));
+    };
+    auto within = [&](int i, int j) {
+        const double dx = mic(x[j] - x[i], 0), dy = mic(y[j] - y[i], 1), dz = mic(z[j] - z[i], 2);
+        return dx * dx + dy * dy + dz * dz <= c2;
+    };
+    int64_t tot = 0, inc = 0;
+    if (h.cut == MCG_CUT_SWITCH) {
+        std::vector<int> counts(n);
+        int64_t total = 0;
+        if ((r = s->eng.get_pairlist(counts.data(), nullptr, 0, &total))) return r;
+        std::vector<int> ent((size_t)std::max<int64_t>(1, total));
+        if ((r = s->eng.get_pairlist(counts.data(), ent.data(), total, &total))) return r;
+        int64_t o = 0;
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < counts[i]; k++, o++) inc += within(i, ent[o]) ? 1 : 0;
+        tot = total;
+    } else {
+        // every non-excluded pair (the full energy has no cutoff)
+        tot = (int64_t)n * (n - 1) / 2 - (int64_t)h.fexclData.size();
+        inc = tot;
+    }
+    *list_pairs = tot;
+    *in_cutoff = inc;
+    return MCG_OK;
 }
 
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {

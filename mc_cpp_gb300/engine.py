@@ -93,6 +93,12 @@ class FFieldCUDA:
                                               native.pd(z), native.pd(de)))
         return float(de[0])
 
+    def pair_count(self):
+        """(list pairs, pairs within the cutoff at the current coordinates)."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        native.check(native.lib().mcg_pair_count(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def commit(self) -> None:
         native.check(native.lib().mcg_commit(self.h))
 
