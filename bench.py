@@ -46,9 +46,43 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_chains(rank: int, nchains: int):
+def make_chains(rank: int, nchains: int, **kw):
+    """Rank r's own chains (weak scaling: every rank runs nchains independent chains, seeded by r)."""
     from mc_cpp_gb300 import systems
-    return systems.water_chains(nchains=nchains, seed=3 + 7919 * rank)
+    return systems.water_chains(nchains=nchains, seed=3 + 7919 * rank, **kw)
+
+
+class Reducer:
+    """Max and sum of one float over the ranks (no-op for one rank).  Timing and statistics only:
+    the chains never exchange data."""
+
+    def __init__(self, world: int, device: str):
+        self.world, self.device = world, device
+
+    def _all(self, x, op):
+        if self.world == 1:
+            return float(x)
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x):
+        import torch.distributed as dist
+        return self._all(x, dist.ReduceOp.MAX if self.world > 1 else None)
+
+    def sum(self, x):
+        import torch.distributed as dist
+        return self._all(x, dist.ReduceOp.SUM if self.world > 1 else None)
+
+
+def aggregate(red: Reducer, accepted: float, trials: float, pairs: float, ms: float):
+    """Whole-job rates: units of all ranks over the slowest rank's time."""
+    ms_max = red.max(ms)
+    sec = ms_max * 1e-3
+    return {"ms_max": ms_max, "accepted_per_s": red.sum(accepted) / sec, "trials_per_s": red.sum(trials) / sec,
+            "pairs_per_s": red.sum(pairs) / sec}
 
 
 # ------------------------------------------------------------------ clocks during the timed region
@@ -212,19 +246,8 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def allmax(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    def allsum(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        return float(t.item())
+    red = Reducer(world, "cuda")
+    allmax, allsum = red.max, red.sum
 
     chains = make_chains(rank, args.chains)
     B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank,
@@ -244,9 +267,9 @@ def run_ours(args):
     acc = float((a1 - a0).sum())
     trials = float((t1 - t0).sum())
     pairs = float((p1 - p0).sum())
-    ms_max = allmax(ms)
-    acc_all = allsum(acc)
-    value = acc_all / (ms_max * 1e-3)
+    agg = aggregate(red, acc, trials, pairs, ms)
+    ms_max = agg["ms_max"]
+    value = agg["accepted_per_s"]
     # roofline of the sweep kernel (the only kernel in the timed region)
     peak = native.lib()
     import ctypes as C
@@ -304,9 +327,9 @@ def run_ours(args):
                        "acceptance": "physical", "parallelism": "independent chains, weak scaling over GPUs",
                        "tuning": tuning},
             "phase_ms_per_step": {"list_rebuild": ms_lists / args.steps, "sweep_kernel": ms_sweep / args.steps},
-            "trials_per_s": allsum(trials) / (ms_max * 1e-3),
+            "trials_per_s": agg["trials_per_s"],
             "acceptance_ratio": acc / max(1.0, trials),
-            "pair_interactions_per_s": allsum(pairs) / (ms_max * 1e-3),
+            "pair_interactions_per_s": agg["pairs_per_s"],
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": tf.value, "unit": "TFLOP/s",
                          "frac": achieved / tf.value if tf.value > 0 else None, "traffic": traffic,
                          "peak_source": "FFMA-chain probe kernel measured in this run (no FP32 figure in MEASURED_PEAKS.json)",
