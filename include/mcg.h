@@ -168,6 +168,8 @@ typedef struct mcg_batch_opts {
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
     int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4, 8 */
+    int clusters;             /* 0 = automatic (on with 512-thread CTAs): the largest chains each run on a
+                                 cluster of two CTAs (two SMs); -1 = off */
 } mcg_batch_opts;
 
 /* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */
@@ -194,12 +196,14 @@ int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_
 typedef struct mcg_batch_tuning {
     int threads_per_chain;    /* 256 or 512 */
     int ctas_per_sm;          /* persistent CTAs per SM (1 or 2) */
-    int speculation;          /* cap on moves evaluated together (0 = box-size heuristic) */
+    int speculation;          /* cap on moves evaluated together per CTA (0 = box-size heuristic) */
     float ms_per_sweep;       /* device time of one sweep at that shape (0 if not measured) */
     int from_cache;           /* 1 when taken from the cache without trial sweeps */
+    int clusters;             /* 1: the largest chains run on two-CTA clusters */
 } mcg_batch_tuning;
 /* Autotuner: times trial_sweeps sweeps (1..64) of every candidate launch shape (threads per chain
- * x CTAs per SM x speculation cap) on this batch and keeps the fastest.  The trial sweeps are
+ * x CTAs per SM x speculation cap x two-CTA clusters for the largest chains) on this batch and
+ * keeps the fastest.  The trial sweeps are
  * ordinary Metropolis sweeps: they advance the chains and count in their statistics.  With
  * use_cache != 0 a shape already tuned for the same workload signature (chain sizes and boxes,
  * cutoffs, move sizes, device name) in this process, or in the file named by the environment

@@ -41,6 +41,7 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "engine.hpp"
@@ -402,16 +403,23 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // (old and new pair terms, mixed_pair_delta).  Commits are written by the first warp of each group
 // after the barrier; positions that a warp may read before they land come from the previous
 // iteration's move records instead.
-template <int APR, int NT>
+//
+// CL = 2: the chain runs on a cluster of two CTAs (two SMs).  Its K moves per iteration are split
+// K/2 per CTA; each warp writes its partial dE and each group its move record to both CTAs'
+// shared memory (distributed shared memory), and the iteration's barrier is the cluster barrier.
+// In-sweep list rebuilds are done by CTA 0 while CTA 1 waits at the cluster barrier.
+template <int APR, int NT, int CL>
 __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
                                                        const int* __restrict__ cta_chains, int nchains) {
+    namespace cg = cooperative_groups;
     constexpr int NW = NT / 32;
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
+    static_assert(CL == 1 || CL == 2, "clusters of one or two CTAs");
     __shared__ MoveRec P[2][KMAX];
-    __shared__ float2 s_red[2][NW];
+    __shared__ float2 s_red[2][CL * NW];
     __shared__ float4 s_ring[NW][RING];
     __shared__ int s_cell[MAX_CELLS + 1];
     __shared__ int s_err;
@@ -421,11 +429,20 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     float4* ring = s_ring[warp];
-    for (int slot = cta_start[blockIdx.x]; slot < cta_start[blockIdx.x + 1]; slot++) {
+    const int rank = CL > 1 ? (int)cg::this_cluster().block_rank() : 0;
+    const int unit = blockIdx.x / CL;                 // the CTA (or cluster) in the chain packing
+    // the iteration barrier: the CTA, or both CTAs of the cluster (memory visible across them)
+    auto unit_sync = [&]() {
+        if (CL > 1) cg::this_cluster().sync();
+        else __syncthreads();
+    };
+    // the other CTA's copy of a shared-memory object (CL = 2)
+    auto peer = [&](auto* p) { return CL > 1 ? cg::this_cluster().map_shared_rank(p, rank ^ 1) : p; };
+    for (int slot = cta_start[unit]; slot < cta_start[unit + 1]; slot++) {
         const int c = cta_chains[slot];
         if (c >= nchains) continue;
         if (APR && chains[c].apr != APR) continue;
-        __syncthreads();   // the previous chain's last reads of shared state are done
+        unit_sync();   // the previous chain's last reads of shared state are done (in both CTAs)
         {
             static_assert(sizeof(ChainDev) % 4 == 0, "ChainDev copied as words");
             const int* src = reinterpret_cast<const int*>(&chains[c]);
@@ -435,10 +452,11 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
         __syncthreads();
         const ChainDev& C = s_chain;
         const int apr = APR ? APR : C.apr;
-        const int K = C.kspec;                 // 1, 2, 4 or 8; K * apr <= 32 and NT / K >= 32
-        const int GS = NT / K;                 // threads per move
+        const int K = C.kspec;                 // 1, 2, 4 or 8; K * apr <= 32 and CL * NT / K >= 32
+        const int KL = K / CL;                 // moves of this CTA
+        const int GS = NT / KL;                // threads per move
         const int WPG = GS >> 5;               // warps per move
-        const int grp = tid / GS, gw = (tid - grp * GS) >> 5;
+        const int grp = rank * KL + tid / GS, gw = ((tid % GS) >> 5);
         const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
         for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
             s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
@@ -525,20 +543,24 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 const float ofx = fdelta(fo0.x, fo.x, Ls0, Ll0), ofy = fdelta(fo0.y, fo.y, Ls1, Ll1),
                             ofz = fdelta(fo0.z, fo.z, Ls2, Ll2);
                 if (gw == 0) {
-                    MoveRec& Q = P[buf][grp];
-                    if (lane < apr) {
-                        Q.fn[lane] = fn;
-                        Q.mn[lane][0] = nx; Q.mn[lane][1] = ny; Q.mn[lane][2] = nz;
-                        Q.fb[lane] = fb;
-                    }
-                    if (lane == 0) {
-                        Q.fo0 = fo0;
-                        Q.res = res;
-                        Q.ahi = q1.z;
-                        Q.alo = q1.w;
-                        // alpha >= ahi / 2^32 and below it by < 2^-32: for ahi >= 2^16 the FP32
-                        // -ln(alpha) is within 2e-5 of the exact one, inside the decision margin
-                        Q.lna = q1.z >= 65536u ? -__logf(__uint2float_rn(q1.z) * 2.3283064365386963e-10f) : __int_as_float(0x7fc00000);
+                    // alpha >= ahi / 2^32 and below it by < 2^-32: for ahi >= 2^16 the FP32
+                    // -ln(alpha) is within 2e-5 of the exact one, inside the decision margin
+                    const float lna = q1.z >= 65536u ? -__logf(__uint2float_rn(q1.z) * 2.3283064365386963e-10f)
+                                                     : __int_as_float(0x7fc00000);
+                    for (int cp = 0; cp < CL; cp++) {
+                        MoveRec& Q = cp ? *peer(&P[buf][grp]) : P[buf][grp];
+                        if (lane < apr) {
+                            Q.fn[lane] = fn;
+                            Q.mn[lane][0] = nx; Q.mn[lane][1] = ny; Q.mn[lane][2] = nz;
+                            Q.fb[lane] = fb;
+                        }
+                        if (lane == 0) {
+                            Q.fo0 = fo0;
+                            Q.res = res;
+                            Q.ahi = q1.z;
+                            Q.alo = q1.w;
+                            Q.lna = lna;
+                        }
                     }
                 }
                 float m[A][3], off[A][3];
@@ -625,8 +647,11 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 hi = sm;
                 lo = lo + ol + e;
             }
-            if (lane == 0) s_red[buf][warp] = make_float2(hi, lo);
-            __syncthreads();
+            if (lane == 0) {
+                s_red[buf][rank * NW + warp] = make_float2(hi, lo);
+                if (CL > 1) *peer(&s_red[buf][rank * NW + warp]) = make_float2(hi, lo);
+            }
+            unit_sync();
             // ---- decisions, identical in every warp: lane g < kk holds move g
             const MoveRec* Q = P[buf];
             float deh = 0.0f, del = 0.0f;           // dE of move `lane` as a float-float pair
@@ -634,7 +659,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
             unsigned cm = 0;                        // earlier moves of the iteration move g may interact with
             {
                 // lane = g * WPG + w holds warp w's partial of move g; segmented butterfly over w
-                float2 v = lane < NW ? s_red[buf][lane] : make_float2(0.0f, 0.0f);
+                float2 v = lane < CL * NW ? s_red[buf][lane] : make_float2(0.0f, 0.0f);
                 for (int o = 1; o < WPG; o <<= 1) {
                     const float oh = __shfl_xor_sync(0xffffffffu, v.x, o), ol = __shfl_xor_sync(0xffffffffu, v.y, o);
                     float sm, e;
@@ -721,18 +746,20 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
             prev_acc = accmask;
             buf ^= 1;
             if (__any_sync(0xffffffffu, far)) {   // identical in every warp
-                __syncthreads();                  // the commits have landed
-                chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0, &s_err,
-                                   reinterpret_cast<uint4*>(ring));
+                unit_sync();                      // the commits have landed
+                if (rank == 0)
+                    chain_rebuild<APR>(C, G, F, FB, LST, NL, s_cell, g_order + C.res0, g_cell + C.res0, g_pos + C.res0,
+                                       &s_err, reinterpret_cast<uint4*>(ring));
+                if (CL > 1) unit_sync();          // CTA 1 waits for CTA 0's lists
                 if (tid == 0) { S.rebuilds++; S.maxd2 = 0.0f; }
                 prev_acc = 0;
             }
         }
         __syncthreads();
         for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
-        if (lane == 0) atomicAdd(&s_pairs, (unsigned long long)npairs);
-        __syncthreads();
-        if (tid == 0) {
+        if (lane == 0) atomicAdd(rank == 0 ? &s_pairs : peer(&s_pairs), (unsigned long long)npairs);
+        unit_sync();
+        if (rank == 0 && tid == 0) {
             S.etot += (double)eh + (double)el;
             S.pairs += (long long)s_pairs;
             S.moves += (unsigned long long)nmoves;
@@ -940,7 +967,13 @@ struct mcg_batch {
     cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
     std::vector<double> cost;     // LPT cost of each chain's sweep
     std::vector<int> kgeom, kheur; // speculation: geometric maximum and the box-size heuristic per chain
-    int nsm = 152, ctas_per_sm = 1, spec_cap = 0;
+    std::vector<char> clustered;   // chains run by a cluster of two CTAs
+    int nsm = 152, ctas_per_sm = 1, spec_cap = 0, clusters = 0;
+    int ncl = 0;                   // clusters (one chain each)
+    int* d_cl_order = nullptr;     // their chains
+    int* d_cl_start = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string signature;        // workload + device key of the autotuner cache
     double* d_xyz = nullptr;      // staging for host-buffer runs (3 x natoms)
     double* d_eres = nullptr;     // per-residue energy shares (mixed recompute)
@@ -951,6 +984,11 @@ struct mcg_batch {
         if (graph) cudaGraphExecDestroy(graph);
         if (tgraph) cudaGraphExecDestroy(tgraph);
         for (cudaEvent_t e : tev) if (e) cudaEventDestroy(e);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (stream2) cudaStreamDestroy(stream2);
+        if (d_cl_order) cudaFree(d_cl_order);
+        if (d_cl_start) cudaFree(d_cl_start);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
                      d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos, d_item_chain,
                      d_chain_item0, d_build};
@@ -1033,14 +1071,36 @@ struct mcg_batch {
     // Longest-processing-time packing of chains onto ctas_per_sm persistent CTAs per SM: the cost
     // of a chain's sweep is its move count times the pairs one move touches.  The largest chains
     // get a CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
-    int pack(int per_sm) {
-        ncta = std::min(nchains, std::max(1, nsm * std::max(1, per_sm)));
+    // With clusters on (512-thread CTAs), the largest chains whose sweep would outlast the average
+    // SM load get a cluster of two CTAs (two SMs) each; the others are packed onto the remaining
+    // persistent CTAs.
+    int pack(int per_sm, int cl) {
         std::vector<int> idx(nchains);
         std::iota(idx.begin(), idx.end(), 0);
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-        std::vector<double> load(ncta, 0.0);
-        std::vector<std::vector<int>> per(ncta);
+        clustered.assign(nchains, 0);
+        std::vector<int> cl_chains;
+        if (cl && threads == 512) {
+            double reg = 0.0, clc = 0.0;
+            for (double v : cost) reg += v;
+            for (int c : idx) {
+                // a two-SM chain runs ~1.6x faster at ~1.25x the SM time
+                const double avg = (reg + 1.25 * clc) / nsm;
+                if (!(cost[c] > 1.1 * avg) || kgeom[c] < 2 || 2 * ((int)cl_chains.size() + 1) > nsm / 2) break;
+                clustered[c] = 1;
+                cl_chains.push_back(c);
+                reg -= cost[c];
+                clc += cost[c];
+            }
+        }
+        ncl = (int)cl_chains.size();
+        clusters = cl;
+        const int nreg = nchains - ncl;
+        ncta = nreg ? std::min(nreg, std::max(1, nsm * std::max(1, per_sm) - 2 * ncl)) : 0;
+        std::vector<double> load(std::max(1, ncta), 0.0);
+        std::vector<std::vector<int>> per(std::max(1, ncta));
         for (int c : idx) {
+            if (clustered[c]) continue;
             int best = 0;
             for (int k = 1; k < ncta; k++) if (load[k] < load[best]) best = k;
             load[best] += cost[c];
@@ -1061,27 +1121,42 @@ struct mcg_batch {
         if (d_cta_start) { cudaFree(d_cta_start); d_cta_start = nullptr; }
         cudaError_t e = cudaMalloc((void**)&d_cta_start, sizeof(int) * (ncta + 1));
         if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        BK(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, stream));
+        if (!order.empty())
+            BK(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, stream));
         BK(cudaMemcpyAsync(d_cta_start, cta_start.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, stream));
+        if (ncl) {
+            std::vector<int> st(ncl + 1);
+            std::iota(st.begin(), st.end(), 0);
+            if (d_cl_order) { cudaFree(d_cl_order); d_cl_order = nullptr; }
+            if (d_cl_start) { cudaFree(d_cl_start); d_cl_start = nullptr; }
+            if (cudaMalloc((void**)&d_cl_order, sizeof(int) * ncl) != cudaSuccess ||
+                cudaMalloc((void**)&d_cl_start, sizeof(int) * (ncl + 1)) != cudaSuccess)
+                return fail(MCG_ECUDA, "cudaMalloc of the cluster packing");
+            BK(cudaMemcpyAsync(d_cl_order, cl_chains.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, stream));
+            BK(cudaMemcpyAsync(d_cl_start, st.data(), sizeof(int) * (ncl + 1), cudaMemcpyHostToDevice, stream));
+            if (!stream2) BK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+            if (!ev_fork) { BK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)); BK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)); }
+        }
         return MCG_OK;
     }
     // Speculation width of every chain: the box-size heuristic (cap 0) or min(cap, geometric limit).
     void set_speculation(int cap) {
         for (int c = 0; c < nchains; c++) {
-            int k = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
+            const int cl = (c < (int)clustered.size() && clustered[c]) ? 2 : 1;
+            int k = cap <= 0 ? (cl > 1 ? kgeom[c] : kheur[c]) : std::min(cl * cap, kgeom[c]);
             // a group is whole warps, and one warp holds the atoms of all moves of an iteration
-            while (k > 1 && (k > threads / 32 || k * chains[c].apr > 32)) k >>= 1;
-            chains[c].kspec = k;
+            while (k > 1 && (k > cl * threads / 32 || k * chains[c].apr > 32)) k >>= 1;
+            chains[c].kspec = std::max(k, cl);
         }
         spec_cap = cap;
     }
     // Launch shape of the sweep; takes effect at the next sweep (the graphs are captured again).
-    int reconfigure(int nthreads, int per_sm, int spec) {
+    int reconfigure(int nthreads, int per_sm, int spec, int cl) {
         BK(cudaStreamSynchronize(stream));
         threads = nthreads;
-        set_speculation(spec);
-        int r = pack(per_sm);
+        int r = pack(per_sm, cl);
         if (r) return r;
+        set_speculation(spec);
         BK(cudaMemcpyAsync(d_chains, chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, stream));
         BK(cudaStreamSynchronize(stream));
         drop_graphs();
@@ -1089,21 +1164,50 @@ struct mcg_batch {
     }
     template <int APR>
     void sweep_kernel(cudaStream_t st) {
+        if (!ncta) return;
         if (threads == 512)
-            k_batch_sweep<APR, 512><<<ncta, 512, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
-                                                          d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<APR, 512, 1><<<ncta, 512, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
         else if (threads == 128)
-            k_batch_sweep<APR, 128><<<ncta, 128, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
-                                                          d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<APR, 128, 1><<<ncta, 128, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
         else
-            k_batch_sweep<APR, 256><<<ncta, 256, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_gpos,
-                                                          d_state, d_cta_start, d_order, nchains);
+            k_batch_sweep<APR, 256, 1><<<ncta, 256, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
     }
+    template <int APR>
+    cudaError_t cluster_kernel(cudaStream_t st) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * ncl);
+        cfg.blockDim = dim3(512);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_batch_sweep<APR, 512, 2>, (const ChainDev*)d_chains, G, d_M, d_F, d_FB, d_LST,
+                                  d_NL, d_gorder, d_gcell, d_gpos, d_state, (const int*)d_cl_start, (const int*)d_cl_order,
+                                  nchains);
+    }
+    // The cluster chains on a second stream branch, concurrently with the regular CTAs.
     int launch_sweep(cudaStream_t st) {
+        if (ncl) {
+            BK(cudaEventRecord(ev_fork, st));
+            BK(cudaStreamWaitEvent(stream2, ev_fork, 0));
+            if (apr_all == 3) BK(cluster_kernel<3>(stream2));
+            else if (apr_all == 1) BK(cluster_kernel<1>(stream2));
+            else BK(cluster_kernel<0>(stream2));
+            BK(cudaEventRecord(ev_join, stream2));
+        }
         if (apr_all == 3) sweep_kernel<3>(st);
         else if (apr_all == 1) sweep_kernel<1>(st);
         else sweep_kernel<0>(st);
-    BK(cudaGetLastError());
+        BK(cudaGetLastError());
+        if (ncl) BK(cudaStreamWaitEvent(st, ev_join, 0));
         return MCG_OK;
     }
 };
@@ -1286,7 +1390,6 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if (opts->speculation < 0 || (opts->speculation & (opts->speculation - 1)) || opts->speculation > KMAX)
         return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4 or 8");
     if (opts->ctas_per_sm < 0 || opts->ctas_per_sm > 8) return fail(MCG_EINVAL, "ctas_per_sm must be in [0, 8]");
-    B->set_speculation(opts->speculation);
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1313,7 +1416,9 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     }
     BK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
     int r;
-    if ((r = B->pack(opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 1))) return r;
+    if (opts->clusters < -1 || opts->clusters > 1) return fail(MCG_EINVAL, "clusters must be -1, 0 or 1");
+    if ((r = B->pack(opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 1, opts->clusters >= 0 ? 1 : 0))) return r;
+    B->set_speculation(opts->speculation);
     if ((r = balloc(&B->d_chains, nchains)) || (r = balloc(&B->d_state, nchains)) ||
         (r = balloc(&B->d_M, atom0)) || (r = balloc(&B->d_F, atom0)) || (r = balloc(&B->d_FB, atom0)) ||
         (r = balloc(&B->d_LST, (size_t)res0 * G.cap)) || (r = balloc(&B->d_NL, res0)) || (r = balloc(&B->d_gorder, res0)) ||
@@ -1447,7 +1552,8 @@ static bool tune_lookup(const std::string& sig, mcg_batch_tuning* t) {
     char key[256];
     mcg_batch_tuning v{};
     bool found = false;
-    while (fscanf(f, "%255s %d %d %d %f", key, &v.threads_per_chain, &v.ctas_per_sm, &v.speculation, &v.ms_per_sweep) == 5)
+    while (fscanf(f, "%255s %d %d %d %d %f", key, &v.threads_per_chain, &v.ctas_per_sm, &v.speculation, &v.clusters,
+                  &v.ms_per_sweep) == 6)
         if (sig == key) { *t = v; found = true; }
     fclose(f);
     if (found) g_tune_cache[sig] = *t;
@@ -1461,7 +1567,8 @@ static void tune_store(const std::string& sig, const mcg_batch_tuning& t) {
     if (!path || !*path) return;
     FILE* f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%s %d %d %d %.4f\n", sig.c_str(), t.threads_per_chain, t.ctas_per_sm, t.speculation, t.ms_per_sweep);
+    fprintf(f, "%s %d %d %d %d %.4f\n", sig.c_str(), t.threads_per_chain, t.ctas_per_sm, t.speculation, t.clusters,
+            t.ms_per_sweep);
     fclose(f);
 }
 
@@ -1469,7 +1576,7 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     if (!b || trial_sweeps < 1 || trial_sweeps > 64) return fail(MCG_EINVAL, "trial_sweeps must be in [1, 64]");
     mcg_batch_tuning best{};
     if (use_cache && tune_lookup(b->signature, &best)) {
-        int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation);
+        int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation, best.clusters);
         if (r) return r;
         best.from_cache = 1;
         if (out) *out = best;
@@ -1482,8 +1589,9 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
     for (int th : kThreads)
         for (int cp : kCtas)
-            for (int sp : kSpec) {
-                int r = b->reconfigure(th, cp, sp);
+            for (int sp : kSpec)
+                for (int cl = 0; cl < (th == 512 ? 2 : 1); cl++) {
+                int r = b->reconfigure(th, cp, sp, cl);
                 if (r) return r;
                 if ((r = b->ensure_graph())) return r;
                 BK(cudaGraphLaunch(b->graph, b->stream));      // upload + warm
@@ -1495,9 +1603,12 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
                 BK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
                 b->launches += 3 * (int64_t)(trial_sweeps + 1);
                 ms /= (float)trial_sweeps;
-                if (ms < best.ms_per_sweep) { best.threads_per_chain = th; best.ctas_per_sm = cp; best.speculation = sp; best.ms_per_sweep = ms; }
-            }
-    int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation);
+                if (ms < best.ms_per_sweep) {
+                    best.threads_per_chain = th; best.ctas_per_sm = cp; best.speculation = sp; best.clusters = cl;
+                    best.ms_per_sweep = ms;
+                }
+                }
+    int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation, best.clusters);
     if (r) return r;
     best.from_cache = 0;
     tune_store(b->signature, best);
@@ -1510,6 +1621,7 @@ int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out) {
     out->threads_per_chain = b->threads;
     out->ctas_per_sm = b->ctas_per_sm;
     out->speculation = b->spec_cap;
+    out->clusters = b->clusters;
     out->ms_per_sweep = 0.f;
     out->from_cache = 0;
     return MCG_OK;

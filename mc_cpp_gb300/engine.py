@@ -154,7 +154,7 @@ class BatchChains:
 
     def __init__(self, chains, dmax_trn: float = 0.15, dmax_rot: float = 15.0, acceptance: str = "physical",
                  seed: int = 1, threads_per_chain: int = 0, list_capacity: int = 0, ctas_per_sm: int = 0,
-                 speculation: int = 0):
+                 speculation: int = 0, clusters: int = 0):
         L = native.lib()
         self.nchains = len(chains)
         arr = (native.SystemDesc * self.nchains)()
@@ -164,7 +164,7 @@ class BatchChains:
             arr[k] = d
             self._keep.append(keep)
         opts = native.BatchOpts(dmax_trn, dmax_rot, native.ACCEPT[acceptance], threads_per_chain, list_capacity, seed,
-                                ctas_per_sm, speculation)
+                                ctas_per_sm, speculation, clusters)
         h = C.c_void_p()
         native.check(L.mcg_batch_create(arr, self.nchains, C.byref(opts), C.byref(h)))
         self.h = h
@@ -201,12 +201,13 @@ class BatchChains:
         t = native.BatchTuning()
         native.check(native.lib().mcg_batch_autotune(self.h, trial_sweeps, int(use_cache), C.byref(t)))
         return {"threads_per_chain": t.threads_per_chain, "ctas_per_sm": t.ctas_per_sm, "speculation": t.speculation,
-                "ms_per_sweep": t.ms_per_sweep, "from_cache": bool(t.from_cache)}
+                "clusters": t.clusters, "ms_per_sweep": t.ms_per_sweep, "from_cache": bool(t.from_cache)}
 
     def tuning(self) -> dict:
         t = native.BatchTuning()
         native.check(native.lib().mcg_batch_get_tuning(self.h, C.byref(t)))
-        return {"threads_per_chain": t.threads_per_chain, "ctas_per_sm": t.ctas_per_sm, "speculation": t.speculation}
+        return {"threads_per_chain": t.threads_per_chain, "ctas_per_sm": t.ctas_per_sm, "speculation": t.speculation,
+                "clusters": t.clusters}
 
     def stats(self):
         t = np.zeros(self.nchains, np.int64)

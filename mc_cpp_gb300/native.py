@@ -59,12 +59,12 @@ class SystemDesc(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("dmax_trn", C.c_double), ("dmax_rot", C.c_double), ("acceptance_units", C.c_int),
                 ("threads_per_chain", C.c_int), ("list_capacity", C.c_int), ("seed", C.c_uint64),
-                ("ctas_per_sm", C.c_int), ("speculation", C.c_int)]
+                ("ctas_per_sm", C.c_int), ("speculation", C.c_int), ("clusters", C.c_int)]
 
 
 class BatchTuning(C.Structure):
     _fields_ = [("threads_per_chain", C.c_int), ("ctas_per_sm", C.c_int), ("speculation", C.c_int),
-                ("ms_per_sweep", C.c_float), ("from_cache", C.c_int)]
+                ("ms_per_sweep", C.c_float), ("from_cache", C.c_int), ("clusters", C.c_int)]
 
 
 _lib = None

@@ -173,13 +173,16 @@ def test_invalid_batches_rejected():
     assert ei.value.code == native.MCG_EINVAL
 
 
-def test_speculative_sweep_reproduces_sequential_chain():
-    """Moves evaluated together (speculation 4) must give the sequential chain: same random
-    numbers, same decisions, same coordinates.  dE sums differ only in float summation order, so
-    a decision could flip only at an exact tie (probability ~1e-7 per move)."""
+@pytest.mark.parametrize("speculation,clusters", [(4, -1), (4, 0), (8, 0), (2, 0)])
+def test_speculative_sweep_reproduces_sequential_chain(speculation, clusters):
+    """Moves evaluated together (up to 8, on one CTA or a two-CTA cluster) must give the
+    sequential chain: same random numbers, same decisions, same coordinates.  dE sums differ only
+    in float summation order, so a decision could flip only at an exact tie (~1e-7 per move)."""
     ch = _waters((4000, 2600, 1500), seed=31)
-    seq = BatchChains(ch, seed=17, speculation=1)
-    spec = BatchChains(ch, seed=17, speculation=4)
+    seq = BatchChains(ch, seed=17, speculation=1, clusters=-1)
+    spec = BatchChains(ch, seed=17, speculation=speculation, clusters=clusters)
+    if clusters == 0:
+        assert spec.tuning()["clusters"] == 1
     seq.sweep(2)
     spec.sweep(2)
     t1, a1, e1 = seq.stats()
@@ -197,9 +200,9 @@ def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch)
     ch = _waters((512, 1500, 3000), seed=41)
     B = BatchChains(ch, seed=8)
     t = B.autotune(trial_sweeps=1, use_cache=False)
-    assert t["threads_per_chain"] in (256, 512) and t["ctas_per_sm"] in (1, 2)
+    assert t["threads_per_chain"] in (256, 512) and t["ctas_per_sm"] in (1, 2) and t["clusters"] in (0, 1)
     assert t["speculation"] in (0, 1, 2, 4) and t["ms_per_sweep"] > 0 and not t["from_cache"]
-    assert {k: t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")} == B.tuning()
+    assert {k: t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation", "clusters")} == B.tuning()
     tr, a, etot = B.stats()
     sweeps = tr // (B.sizes // 3)                      # every shape: 1 warm-up + 1 timed sweep
     assert np.all(tr == sweeps * (B.sizes // 3)) and np.all(sweeps == sweeps[0]) and sweeps[0] >= 8
@@ -211,8 +214,8 @@ def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch)
     B2 = BatchChains(ch, seed=8)
     t2 = B2.autotune(trial_sweeps=1, use_cache=True)
     assert t2["from_cache"]
-    assert [t2[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")] == \
-           [t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation")]
+    assert [t2[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation", "clusters")] == \
+           [t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation", "clusters")]
     assert np.all(B2.stats()[0] == 0)
     assert (tmp_path / "tune.txt").read_text().count("\n") == 1
 
