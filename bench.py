@@ -414,9 +414,12 @@ def config_extras(tf_peak: float):
             ff.delta_e(idx, xyz[idx] + rng.uniform(-0.15, 0.15, 3))
         des = 1000 / (time.perf_counter() - t)
         lp, inc = ff.pair_count()
-        res5[prec] = {"recomputes_per_s": rec, "dE_per_s": des, "pair_interactions_per_s": inc * rec}
+        kms = ff.time_nonbonded(20) / 20                 # the pair kernel alone, CUDA events
+        res5[prec] = {"recomputes_per_s": rec, "dE_per_s": des, "pair_interactions_per_s": inc * rec,
+                      "pair_kernel_ms": kms, "pair_kernel_pairs_per_s": inc / (kms * 1e-3)}
         if prec == "mixed" and tf_peak:
-            res5[prec]["fp32_frac_of_probe"] = inc * rec * FLOPS_PER_PAIR / 1e12 / tf_peak
+            res5[prec]["pair_kernel_fp32_tflops"] = inc * FLOPS_PER_PAIR / (kms * 1e-3) / 1e12
+            res5[prec]["pair_kernel_fp32_frac_of_probe"] = res5[prec]["pair_kernel_fp32_tflops"] / tf_peak
         res5["list_pairs"], res5["pairs_in_cutoff"] = lp, inc
         ff.close()
     out["water100k"] = res5

@@ -129,6 +129,9 @@ int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int6
  * at the current coordinates (FP64 minimum-image distances).  Full: both are the number of pairs
  * the full energy sums (every pair i < j outside the exclusion rows). */
 int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
+/* Device time (ms, CUDA events on the handle's stream) of reps launches of the switched
+ * nonbonded pair kernel alone over the current list (switch mode). */
+int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);
 /* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
  * exclList[i]) and the 1-4 pair list (getNeighList14). */
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);

@@ -42,7 +42,9 @@ def _compile(src: str, cuda: str) -> str:
     obj = os.path.join(BUILD, src + ".o")
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + SRC]
     if src.endswith(".cu"):
-        cmd = [os.path.join(cuda, "bin", "nvcc")] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        # -ftz=true: FP32 subnormals flush to zero (no pair term, displacement or partial sum is
+        # subnormal); the FP64 plain path is unaffected
+        cmd = [os.path.join(cuda, "bin", "nvcc")] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler", "-fPIC",
                                                              "-diag-suppress", "1444", "-c", path, "-o", obj] + inc
     else:
         cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c", path, "-o", obj,

@@ -137,6 +137,11 @@ int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff) {
     return MCG_OK;
 }
 
+int mcg_time_nonbonded(mcg_system* s, int reps, float* ms) {
+    if (!s || !ms || reps < 1) return fail(MCG_EINVAL, "bad arguments");
+    return s->eng.time_nonbonded(reps, ms);
+}
+
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {
     if (!s || !counts) return fail(MCG_EINVAL, "null argument");
     const HostSystem& h = s->eng.hs;

@@ -329,6 +329,77 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
     block_reduce2(sel, svd, part + 2 * blockIdx.x);
 }
 
+// Mixed-precision switched energy over the half list for periodic boxes: the pair kernel.  A warp
+// per row i, lanes over its j > i entries.  One 16-byte load per list entry (the fixed-point
+// position: exact minimum-image displacement by 32-bit wrap-around, scaled by a float-float box
+// length) and one 16-byte load per pair inside the cutoff (charge as float-float, eps, sig).
+// Coulomb is summed per lane as a float-float pair (TwoSum), LJ in FP32 per row and FP64 across
+// rows; the block sums in FP64.  Same terms as mixed_pair (unscaled, k_finalize scales).
+// U list entries in flight per lane; MINB resident CTAs per SM requested from the register
+// allocator (occupancy against registers); the engine times the variants once and keeps the fastest.
+template <int U, int MINB>
+__global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint4* __restrict__ fx, const float4* __restrict__ prm,
+                                                                      int n, float Ls0, float Ls1, float Ls2, float Ll0,
+                                                                      float Ll1, float Ll2, CutDev cut, const int* __restrict__ nbr,
+                                                                      const int* __restrict__ nup, int cap, double* part) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const float c2 = cut.c2f, n2 = cut.n2f, sw2 = cut.sw2f, k3 = c2 - 3.0f * n2;
+    float eh = 0.0f, elo = 0.0f;   // Coulomb of this lane, float-float
+    double svd = 0.0;
+    for (int i = warp; i < n; i += nwarps) {
+        const uint4 fi = fx[i];
+        const float4 pi = prm[i];
+        const int* row = nbr + (size_t)i * cap;
+        const int m = nup[i];
+        float vrow = 0.0f;
+        for (int k0 = 0; k0 < m; k0 += 32 * U) {
+            int j[U];
+            uint4 fj[U];
+            float4 pj[U];
+            float r2[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int k = k0 + u * 32 + lane;
+                j[u] = k < m ? row[k] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) fj[u] = j[u] >= 0 ? fx[j[u]] : fi;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
+                            dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
+                r2[u] = j[u] >= 0 ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 2.0f * c2;
+                pj[u] = r2[u] <= c2 ? prm[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (r2[u] <= c2) {
+                    const float qh = pi.x * pj[u].x;
+                    const float ql = fmaf(pi.x, pj[u].x, -qh) + fmaf(pi.x, pj[u].y, pi.y * pj[u].x);
+                    float rinv = rsqrtf(r2[u]);
+                    rinv = rinv * fmaf(-0.5f * r2[u] * rinv, rinv, 1.5f);   // one Newton step
+                    const float ri2 = rinv * rinv;
+                    const float sg = pi.w + pj[u].w;
+                    const float x2 = sg * sg * ri2;
+                    const float x6 = x2 * x2 * x2;
+                    const float a = c2 - r2[u];
+                    const float f = r2[u] > n2 ? a * a * fmaf(2.0f, r2[u], k3) * sw2 : 1.0f;
+                    const float e = fmaf(qh, rinv, ql * rinv) * f;
+                    vrow = fmaf(pi.z * pj[u].z * fmaf(x6, x6, -x6), f, vrow);
+                    float sm, er;
+                    two_sum(eh, e, sm, er);
+                    eh = sm;
+                    elo += er;
+                }
+            }
+        }
+        svd += (double)vrow;
+    }
+    block_reduce2((double)eh + (double)elo, svd, part + 2 * blockIdx.x);
+}
+
 // Full energy: all pairs j > i not in the full-mode exclusion row of i, no cutoff.  Triangular
 // grid of TILE x TILE blocks; each thread owns one i and walks a shared-memory j tile with the
 // reference's sorted-row cursor (FField_MDBAS.cpp:227-234).
@@ -769,7 +840,7 @@ static int dupload(T** p, const std::vector<T>& v, cudaStream_t st) {
 SingleEngine::~SingleEngine() { release(); }
 
 void SingleEngine::release() {
-    void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
+    void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_prmf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
                     d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
                     d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_out, d_maxrow,
                     d_stage};
@@ -796,6 +867,7 @@ int SingleEngine::init(const HostSystem& h) {
     std::vector<double4> pq(n);
     std::vector<double2> es(n), es14(n);
     std::vector<float2> esf(n), esf14(n), qf(n);
+    std::vector<float4> prmf(n);
     for (int i = 0; i < n; i++) {
         pq[i] = make_double4(hs.x[i], hs.y[i], hs.z[i], hs.q[i]);
         es[i] = make_double2(hs.eps[i], hs.sig[i]);
@@ -804,10 +876,12 @@ int SingleEngine::init(const HostSystem& h) {
         esf14[i] = make_float2((float)hs.eps14[i], (float)hs.sig14[i]);
         float qh = (float)hs.q[i];
         qf[i] = make_float2(qh, (float)(hs.q[i] - (double)qh));
+        prmf[i] = make_float4(qf[i].x, qf[i].y, esf[i].x, esf[i].y);
     }
     int rc;
     if ((rc = dupload(&d_pq, pq, stream)) || (rc = dupload(&d_es, es, stream)) || (rc = dupload(&d_es14, es14, stream)) ||
         (rc = dupload(&d_esf, esf, stream)) || (rc = dupload(&d_esf14, esf14, stream)) || (rc = dupload(&d_qf, qf, stream)) ||
+        (rc = dupload(&d_prmf, prmf, stream)) ||
         (rc = dupload(&d_frozen, hs.frozen, stream)) || (rc = dupload(&d_xs, hs.exclStart, stream)) ||
         (rc = dupload(&d_xd, hs.exclData, stream)) || (rc = dupload(&d_fxs, hs.fexclStart, stream)) ||
         (rc = dupload(&d_fxd, hs.fexclData, stream)))
@@ -845,7 +919,7 @@ int SingleEngine::init(const HostSystem& h) {
     term_start[n] = (int)term_data.size() / 2;
     // scratch: partial sums and the ΔE ticket
     ntile = (n + TILE - 1) / TILE;
-    size_t nparts = std::max<size_t>({(size_t)NB_BLOCKS, (size_t)ntile * (ntile + 1) / 2, (size_t)MAX_MOVED + 1});
+    size_t nparts = std::max<size_t>({(size_t)152 * 8, (size_t)ntile * (ntile + 1) / 2, (size_t)MAX_MOVED + 1});
     part_cap = nparts * 3 + 2 * 64 + 5 * 64 + 16;
     if ((rc = dalloc(&d_part, part_cap)) || (rc = dalloc(&d_ticket, 1)) || (rc = dalloc(&d_out, 16)) ||
         (rc = dalloc(&d_maxrow, 1)))
@@ -862,6 +936,77 @@ int SingleEngine::init(const HostSystem& h) {
         if ((rc = build_list())) return rc;
     }
     CK(cudaStreamSynchronize(stream));
+    return MCG_OK;
+}
+
+// The switched nonbonded kernel over the half list (FP64, or mixed: the dedicated pair kernel for
+// periodic boxes).
+int SingleEngine::launch_nonbonded(double* nbp) {
+    AtomsDev A = atoms();
+    if (hs.prec == MCG_PREC_FP64)
+        k_energy_list<PREC_F64><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
+    else if (pbc.type != 0) {
+        if (pair_variant < 0) tune_pair_kernel();
+        return launch_pair_variant(pair_variant, nbp);
+    } else
+        k_energy_list<PREC_MIX><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
+    return NB_BLOCKS;
+}
+
+static const int kPairVariants = 4;
+
+int SingleEngine::launch_pair_variant(int v, double* nbp) {
+    AtomsDev A = atoms();
+    // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
+    switch (v) {
+    case 0: k_energy_list_mix<4, 4><<<152 * 4, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
+                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+    case 1: k_energy_list_mix<4, 6><<<152 * 6, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
+                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+    case 2: k_energy_list_mix<2, 8><<<152 * 8, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
+                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+    default: k_energy_list_mix<8, 3><<<152 * 3, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
+                                                                        A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+    }
+    static const int kBlocks[kPairVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
+    return kBlocks[v < 0 || v >= kPairVariants ? kPairVariants - 1 : v];
+}
+
+// Times every pair-kernel variant on the current system (3 launches each) and keeps the fastest.
+void SingleEngine::tune_pair_kernel() {
+    cudaEvent_t a, b;
+    pair_variant = 0;
+    if (cudaEventCreate(&a) != cudaSuccess) return;
+    if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return; }
+    float best = 3.0e38f;
+    for (int v = 0; v < kPairVariants; v++) {
+        launch_pair_variant(v, d_part);
+        cudaEventRecord(a, stream);
+        for (int r = 0; r < 3; r++) launch_pair_variant(v, d_part);
+        cudaEventRecord(b, stream);
+        float ms = 0.f;
+        if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) continue;
+        if (ms < best) { best = ms; pair_variant = v; }
+    }
+    launches += 4 * kPairVariants;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+}
+
+int SingleEngine::time_nonbonded(int reps, float* ms) {
+    if (hs.cut != MCG_CUT_SWITCH) return fail(MCG_ENOTSUP, "the pair-kernel timing covers the switch mode");
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    launch_nonbonded(d_part);                       // warm
+    CK(cudaEventRecord(a, stream));
+    for (int r = 0; r < reps; r++) launch_nonbonded(d_part);
+    CK(cudaEventRecord(b, stream));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    launches += reps + 1;
     return MCG_OK;
 }
 
@@ -954,11 +1099,7 @@ int SingleEngine::energy(double ener[10]) {
     double* nbp = d_part;
     int nnb = 0;
     if (hs.cut == MCG_CUT_SWITCH) {
-        nnb = NB_BLOCKS;
-        if (hs.prec == MCG_PREC_FP64)
-            k_energy_list<PREC_F64><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
-        else
-            k_energy_list<PREC_MIX><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
+        nnb = launch_nonbonded(nbp);
     } else {
         nnb = ntile * (ntile + 1) / 2;
         if (hs.prec == MCG_PREC_FP64)

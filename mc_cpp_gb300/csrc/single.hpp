@@ -24,6 +24,7 @@ public:
     int delta_e(int m, const int* atoms, const double* nx, const double* ny, const double* nz, double* de);
     int commit();
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
+    int time_nonbonded(int reps, float* ms);
 
     HostSystem hs;
     int n = 0;
@@ -37,6 +38,10 @@ private:
     int build_list();
     void release();
     AtomsDev atoms() const;
+    int launch_nonbonded(double* nbp);     // returns the CTAs launched (partial sums written)
+    int launch_pair_variant(int v, double* nbp);
+    void tune_pair_kernel();
+    int pair_variant = -1;        // mixed pair-kernel variant, chosen by timing at the first use
     BondedDev bonded() const;
 
     cudaStream_t stream = nullptr;
@@ -47,6 +52,7 @@ private:
     double2 *d_es = nullptr, *d_es14 = nullptr;
     uint4* d_fx = nullptr;
     float2 *d_esf = nullptr, *d_esf14 = nullptr, *d_qf = nullptr;
+    float4* d_prmf = nullptr;     // (q as float-float, eps, sig) per atom for the mixed pair kernel
     uint8_t* d_frozen = nullptr;
     int *d_xs = nullptr, *d_xd = nullptr, *d_fxs = nullptr, *d_fxd = nullptr;
     int2* d_p14 = nullptr;

@@ -93,6 +93,12 @@ class FFieldCUDA:
                                               native.pd(z), native.pd(de)))
         return float(de[0])
 
+    def time_nonbonded(self, reps: int) -> float:
+        """Device ms of reps launches of the switched pair kernel alone."""
+        ms = C.c_float(0)
+        native.check(native.lib().mcg_time_nonbonded(self.h, reps, C.byref(ms)))
+        return ms.value
+
     def pair_count(self):
         """(list pairs, pairs within the cutoff at the current coordinates)."""
         a, b = C.c_int64(0), C.c_int64(0)
