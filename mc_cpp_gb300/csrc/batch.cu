@@ -490,6 +490,17 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                 const int piv = (int)(((uint64_t)q0.z * (uint64_t)apr) >> 32);
                 const int k = lane < apr ? lane : 0;
                 const int a = res * apr + k;
+                // the first neighbour indices of the list row, loaded before the move is formed so
+                // their latency overlaps the moved residue's loads and the move arithmetic
+                constexpr int CH = 4;
+                const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
+                const int nitems = NL[C.res0 + res] * apr;
+                int q_first[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const int e = (gw * 32 + u * GS + lane) / apr;
+                    q_first[u] = e < G.cap ? row[e] : 0;
+                }
                 uint4 fo = Fc[a];
                 ulonglong4 mo = Mc[a];
                 const uint4 fb = FB[C.atom0 + a];
@@ -592,17 +603,14 @@ __global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restric
                         acc += mixed_pair_delta(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, cut, np);
                     }
                 };
-                const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
-                const int nitems = NL[C.res0 + res] * apr;
                 int head = 0, tail = 0;
-                constexpr int CH = 4;
                 for (int base = gw * 32; base < nitems; base += CH * GS) {
                     int q[CH];
                     uint4 pb[CH];
 #pragma unroll
                     for (int u = 0; u < CH; u++) {
                         const int t = base + u * GS + lane;
-                        q[u] = t < nitems ? row[t / apr] : -1;
+                        q[u] = t < nitems ? (base == gw * 32 ? q_first[u] : (int)row[t / apr]) : -1;
                     }
 #pragma unroll
                     for (int u = 0; u < CH; u++) {
@@ -1143,7 +1151,7 @@ struct mcg_batch {
     void set_speculation(int cap) {
         for (int c = 0; c < nchains; c++) {
             const int cl = (c < (int)clustered.size() && clustered[c]) ? 2 : 1;
-            int k = cap <= 0 ? (cl > 1 ? kgeom[c] : kheur[c]) : std::min(cl * cap, kgeom[c]);
+            int k = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
             // a group is whole warps, and one warp holds the atoms of all moves of an iteration
             while (k > 1 && (k > cl * threads / 32 || k * chains[c].apr > 32)) k >>= 1;
             chains[c].kspec = std::max(k, cl);
