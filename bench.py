@@ -352,16 +352,32 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------------ the other configurations
-def config_extras(tf_peak: float):
+def config_extras(tf_peak: float, only=None):
     """The reference's other configurations, each bounded to a few seconds: the argon replay in
     plain FP64 (the small CPU-runnable case), the solvated peptide in mixed precision with its
     error against FP64, the 100,002-atom water box (full recomputes/s and dE/s in FP64 and mixed,
     and the FP32 roofline of the mixed pair kernel), and 1024 batched argon chains."""
-    from mc_cpp_gb300 import systems
-    from mc_cpp_gb300.engine import BatchChains, FFieldCUDA
     KCAL = 418.4
     out = {}
-    # argon, 864 atoms, FP64, single-atom moves <= 0.2 A at 120 K, reference acceptance units
+
+    def want(name):
+        return only is None or only == name
+    if want("argon864"):
+        out.update(_argon864())
+    if want("peptide"):
+        out.update(_peptide(KCAL))
+    if want("water100k"):
+        out.update(_water100k(tf_peak))
+    if want("argon1024"):
+        out.update(_argon1024(tf_peak))
+    return out
+
+
+def _argon864():
+    """Argon, 864 atoms, FP64, single-atom moves <= 0.2 A at 120 K, reference acceptance units."""
+    from mc_cpp_gb300 import systems
+    from mc_cpp_gb300.engine import FFieldCUDA
+    out = {}
     ff = FFieldCUDA(systems.argon_fcc(), "fp64")
     ff.metropolis(200, 1, trace=False)
     t = time.perf_counter()
@@ -369,7 +385,14 @@ def config_extras(tf_peak: float):
     dt = time.perf_counter() - t
     out["argon864_plain_fp64"] = {"moves_per_s": 20000 / dt, "accepted_moves_per_s": nacc / dt, "steps": 20000}
     ff.close()
-    # solvated flexible peptide (40 atoms + 6000 waters): mixed precision against FP64
+    return out
+
+
+def _peptide(KCAL):
+    """Solvated flexible peptide (40 atoms + 6000 waters): mixed precision against FP64."""
+    from mc_cpp_gb300 import systems
+    from mc_cpp_gb300.engine import FFieldCUDA
+    out = {}
     s = systems.peptide_in_water()
     f64, fmx = FFieldCUDA(s, "fp64", moves=False), FFieldCUDA(s, "mixed", moves=False)
     e64, emx = f64.getE(), fmx.getE()
@@ -395,7 +418,14 @@ def config_extras(tf_peak: float):
                                   "rel_total_E_err": abs(emx - e64) / abs(e64), "dE_per_s_mixed": 300 / t_mx,
                                   "moves": "300 random single-atom peptide and rigid-water displacements"}
     f64.close(); fmx.close()
-    # 100,002-atom water box (33,334 molecules, 0.0334 mol/A^3), switch 10-12 A
+    return out
+
+
+def _water100k(tf_peak):
+    """100,002-atom water box (33,334 molecules, 0.0334 mol/A^3), switch 10-12 A."""
+    from mc_cpp_gb300 import systems
+    from mc_cpp_gb300.engine import FFieldCUDA
+    out = {}
     w = systems.water_box(33334, seed=11)
     res5 = {"atoms": w.natom}
     for prec in ("fp64", "mixed"):
@@ -423,7 +453,14 @@ def config_extras(tf_peak: float):
         res5["list_pairs"], res5["pairs_in_cutoff"] = lp, inc
         ff.close()
     out["water100k"] = res5
-    # 1024 independent argon chains (500-2000 atoms, 0.015-0.025 atoms/A^3, 90-150 K), one batch
+    return out
+
+
+def _argon1024(tf_peak):
+    """1024 independent argon chains (500-2000 atoms, 0.015-0.025 atoms/A^3, 90-150 K), one batch."""
+    from mc_cpp_gb300 import systems
+    from mc_cpp_gb300.engine import BatchChains
+    out = {}
     B = BatchChains(systems.argon_chains(), dmax_trn=0.2, dmax_rot=0.0, acceptance="physical", seed=3)
     tune = B.autotune(trial_sweeps=1)
     B.sweep(3)
@@ -457,7 +494,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' figures")
+    ap.add_argument("--config-only", choices=["argon864", "peptide", "water100k", "argon1024"],
+                    help="print only that configuration's figures (one JSON line) and exit")
     args = ap.parse_args()
+    if args.config_only:
+        import ctypes as C
+        from mc_cpp_gb300 import native
+        tf = C.c_double(0)
+        native.check(native.lib().mcg_probe_fp32_tflops(C.byref(tf)))
+        print(json.dumps(config_extras(tf.value, args.config_only)), flush=True)
+        return 0
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -409,7 +409,7 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // shared memory (distributed shared memory), and the iteration's barrier is the cluster barrier.
 // In-sweep list rebuilds are done by CTA 0 while CTA 1 waits at the cluster barrier.
 template <int APR, int NT, int CL>
-__global__ void __launch_bounds__(NT, 1) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
+__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
@@ -1079,7 +1079,7 @@ struct mcg_batch {
     // Longest-processing-time packing of chains onto ctas_per_sm persistent CTAs per SM: the cost
     // of a chain's sweep is its move count times the pairs one move touches.  The largest chains
     // get a CTA, and so an SM, of their own; smaller ones fill the least-loaded CTAs.
-    // With clusters on (512-thread CTAs), the largest chains whose sweep would outlast the average
+    // With clusters on (their CTAs have 512 threads), the largest chains whose sweep would outlast the average
     // SM load get a cluster of two CTAs (two SMs) each; the others are packed onto the remaining
     // persistent CTAs.
     int pack(int per_sm, int cl) {
@@ -1088,7 +1088,7 @@ struct mcg_batch {
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
         clustered.assign(nchains, 0);
         std::vector<int> cl_chains;
-        if (cl && threads == 512) {
+        if (cl) {
             double reg = 0.0, clc = 0.0;
             for (double v : cost) reg += v;
             for (int c : idx) {
@@ -1104,6 +1104,8 @@ struct mcg_batch {
         ncl = (int)cl_chains.size();
         clusters = cl;
         const int nreg = nchains - ncl;
+        // per_sm CTAs per SM less the cluster CTAs: with per_sm above the CTAs an SM holds, the
+        // extra CTAs start as others finish (dynamic balancing of the longest-first packing)
         ncta = nreg ? std::min(nreg, std::max(1, nsm * std::max(1, per_sm) - 2 * ncl)) : 0;
         std::vector<double> load(std::max(1, ncta), 0.0);
         std::vector<std::vector<int>> per(std::max(1, ncta));
@@ -1590,15 +1592,16 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
         if (out) *out = best;
         return MCG_OK;
     }
-    static const int kThreads[] = {256, 512};
-    static const int kCtas[] = {1, 2};
+    // (threads per CTA, CTAs per SM): one chain per SM at 512 threads (also as two waves), two
+    // co-resident chains at 256, four at 128
+    static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}};
     static const int kSpec[] = {1, 2, 4, 8, 0};
     best.ms_per_sweep = 3.0e38f;
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
-    for (int th : kThreads)
-        for (int cp : kCtas)
+    for (const auto& shp : kShape)
             for (int sp : kSpec)
-                for (int cl = 0; cl < (th == 512 ? 2 : 1); cl++) {
+                for (int cl = 0; cl < 2; cl++) {
+                const int th = shp[0], cp = shp[1];
                 int r = b->reconfigure(th, cp, sp, cl);
                 if (r) return r;
                 if ((r = b->ensure_graph())) return r;
