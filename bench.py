@@ -11,7 +11,8 @@ synthetic (seeded), the working set (2.1 M atoms, 1.5 GB of neighbour lists) exc
 flush is needed between steps.
 
 Before the warm-up the autotuner picks the sweep's launch shape (threads per chain, CTAs per SM,
-speculation width) from two trial sweeps per candidate; those sweeps are untimed.
+speculation width, two-CTA clusters for the largest chains) from trial sweeps; those sweeps are
+untimed.
 
 Reported: `value` = accepted moves/s over all GPUs (device time of whole sweeps, list rebuild
 included, CUDA events on the library's stream, max over ranks); `e2e` = the same through the
@@ -253,7 +254,7 @@ def run_ours(args):
     B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank,
                     threads_per_chain=args.threads, ctas_per_sm=args.ctas_per_sm)
     natoms = B.natoms
-    tuning = B.autotune(trial_sweeps=2) if not (args.threads or args.ctas_per_sm) else dict(B.tuning(), from_cache=False)
+    tuning = B.autotune(trial_sweeps=1) if not (args.threads or args.ctas_per_sm) else dict(B.tuning(), from_cache=False)
     B.sweep(args.warmup)
     barrier()
     t0, a0, _ = B.stats()

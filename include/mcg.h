@@ -205,8 +205,9 @@ typedef struct mcg_batch_tuning {
     int clusters;             /* 1: the largest chains run on two-CTA clusters */
 } mcg_batch_tuning;
 /* Autotuner: times trial_sweeps sweeps (1..64) of every candidate launch shape (threads per chain
- * x CTAs per SM x speculation cap x two-CTA clusters for the largest chains) on this batch and
- * keeps the fastest.  The trial sweeps are
+ * x CTAs per SM x speculation cap x two-CTA clusters for the largest chains) on this batch, times
+ * the six fastest again in three interleaved rounds of one sweep each (the chains drift while
+ * shapes are timed) and keeps the fastest.  The trial sweeps are
  * ordinary Metropolis sweeps: they advance the chains and count in their statistics.  With
  * use_cache != 0 a shape already tuned for the same workload signature (chain sizes and boxes,
  * cutoffs, move sizes, device name) in this process, or in the file named by the environment

@@ -1596,29 +1596,51 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     // co-resident chains at 256, four at 128
     static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}};
     static const int kSpec[] = {1, 2, 4, 8, 0};
-    best.ms_per_sweep = 3.0e38f;
+    struct Cand { int th, cp, sp, cl; float ms; };
+    std::vector<Cand> cand;
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
+    // ms per sweep of the current shape over `n` sweeps, after one warm-up sweep (graph upload)
+    auto time_shape = [&](const Cand& c, int n, float* ms) -> int {
+        int r = b->reconfigure(c.th, c.cp, c.sp, c.cl);
+        if (r) return r;
+        if ((r = b->ensure_graph())) return r;
+        BK(cudaGraphLaunch(b->graph, b->stream));
+        BK(cudaEventRecord(b->ev0, b->stream));
+        for (int s = 0; s < n; s++) BK(cudaGraphLaunch(b->graph, b->stream));
+        BK(cudaEventRecord(b->ev1, b->stream));
+        BK(cudaEventSynchronize(b->ev1));
+        BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+        *ms /= (float)n;
+        b->launches += 3 * (int64_t)(n + 1);
+        return MCG_OK;
+    };
+    // stage 1: every shape
     for (const auto& shp : kShape)
-            for (int sp : kSpec)
-                for (int cl = 0; cl < 2; cl++) {
-                const int th = shp[0], cp = shp[1];
-                int r = b->reconfigure(th, cp, sp, cl);
+        for (int sp : kSpec)
+            for (int cl = 0; cl < 2; cl++) {
+                Cand c{shp[0], shp[1], sp, cl, 0.f};
+                int r = time_shape(c, trial_sweeps, &c.ms);
                 if (r) return r;
-                if ((r = b->ensure_graph())) return r;
-                BK(cudaGraphLaunch(b->graph, b->stream));      // upload + warm
-                BK(cudaEventRecord(b->ev0, b->stream));
-                for (int s = 0; s < trial_sweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
-                BK(cudaEventRecord(b->ev1, b->stream));
-                BK(cudaEventSynchronize(b->ev1));
-                float ms = 0.f;
-                BK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-                b->launches += 3 * (int64_t)(trial_sweeps + 1);
-                ms /= (float)trial_sweeps;
-                if (ms < best.ms_per_sweep) {
-                    best.threads_per_chain = th; best.ctas_per_sm = cp; best.speculation = sp; best.clusters = cl;
-                    best.ms_per_sweep = ms;
-                }
-                }
+                cand.push_back(c);
+            }
+    // stage 2: the six fastest again, in interleaved rounds (the chains drift while they are timed)
+    std::stable_sort(cand.begin(), cand.end(), [](const Cand& x, const Cand& y) { return x.ms < y.ms; });
+    cand.resize(std::min<size_t>(6, cand.size()));
+    std::vector<float> sum(cand.size(), 0.f);
+    for (int round = 0; round < 3; round++)
+        for (size_t k = 0; k < cand.size(); k++) {
+            float ms = 0.f;
+            int r = time_shape(cand[k], 1, &ms);
+            if (r) return r;
+            sum[k] += ms;
+        }
+    size_t bi = 0;
+    for (size_t k = 1; k < cand.size(); k++) if (sum[k] < sum[bi]) bi = k;
+    best.threads_per_chain = cand[bi].th;
+    best.ctas_per_sm = cand[bi].cp;
+    best.speculation = cand[bi].sp;
+    best.clusters = cand[bi].cl;
+    best.ms_per_sweep = sum[bi] / 3.0f;
     int r = b->reconfigure(best.threads_per_chain, best.ctas_per_sm, best.speculation, best.clusters);
     if (r) return r;
     best.from_cache = 0;
