@@ -74,8 +74,8 @@ def test_metropolis_trace_bitwise(name, steps):
     assert np.array_equal(tr, want), np.argwhere(tr != want)[:5]
 
 
-def test_survey_acceptance_counts_nma():
-    # survey record: NMA switch, 500 steps, seed 1234 -> TRN 245/75, ROT 255/100
+def test_reference_acceptance_counts_nma():
+    # the reference's own run: NMA switch, 500 steps, seed 1234 -> TRN 245/75, ROT 255/100
     g = goldens.golden()["mc"]["nma_switch"]
     assert g["trials"] == [245, 255]
     assert g["accepted"] == [75, 100]
