@@ -225,6 +225,9 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
 int mcg_batch_energy_mixed(mcg_batch* b, double* e);
 /* Pair interactions evaluated so far by each chain (pairs inside the cutoff before or after a move). */
 int mcg_batch_pairs(mcg_batch* b, int64_t* pairs);
+/* The residue neighbour lists of one chain as they are now: counts[nres] always; entries (the
+ * rows concatenated, residue indices within the chain) when cap >= *total. */
+int mcg_batch_get_lists(mcg_batch* b, int chain, int* counts, int* entries, int64_t cap, int64_t* total);
 /* Rebuild every chain's neighbour lists now (the batched counterpart of FField::askListUpdate,
  * FField.cpp:222-235).  Sweeps rebuild lists by themselves when atoms have moved enough. */
 int mcg_batch_update_lists(mcg_batch* b);

@@ -832,9 +832,14 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
                                                           const uint4* __restrict__ F, const int* __restrict__ res_chain,
                                                           const uint16_t* __restrict__ LST, const int* __restrict__ NL,
                                                           double* e_res, int64_t nres_total) {
+    // A warp per residue r, lanes over its list entries q > r, all atom pairs of (r, q), with r's
+    // atoms in registers.  Coulomb and LJ are summed per lane as float-float pairs (TwoSum), so the
+    // result does not depend on the list order beyond ~1e-14; the warp sums in FP64.
+    constexpr int A = APR ? APR : MAX_APR;
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
     cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
+    const float c2 = G.c2f;
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
@@ -846,27 +851,46 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
         const uint4* Fc = F + C.atom0;
         const uint16_t* row = LST + (size_t)gr * G.cap;
         const int nl = NL[gr];
-        F32Acc acc;
-        for (int e = lane; e < nl; e += 32) {
-            const int q = row[e];
+        const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
+        uint4 pa[A];
+#pragma unroll
+        for (int k = 0; k < A; k++) pa[k] = k < apr ? Fc[r * apr + k] : make_uint4(0, 0, 0, 0);
+        float eh = 0.0f, elo = 0.0f, vh = 0.0f, vlo = 0.0f;
+        for (int e0 = 0; e0 < nl; e0 += 32) {
+            const int e = e0 + lane;
+            const int q = e < nl ? (int)row[e] : -1;
             if (q <= r) continue;
-            for (int k = 0; k < apr; k++) {
-                const uint4 pa = Fc[r * apr + k];
-                for (int b = 0; b < apr; b++) {
-                    const uint4 pb = Fc[q * apr + b];
-                    const float dx = fdelta(pa.x, pb.x, C.Ls[0], C.Lsl[0]), dy = fdelta(pa.y, pb.y, C.Ls[1], C.Lsl[1]),
-                                dz = fdelta(pa.z, pb.z, C.Ls[2], C.Lsl[2]);
-                    const float u = dx * dx + dy * dy + dz * dz;
-                    if (u > cut.c2f) continue;
+            uint4 pb[A];
+#pragma unroll
+            for (int b = 0; b < A; b++) pb[b] = b < apr ? Fc[q * apr + b] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (int k = 0; k < A; k++) {
+                if (k >= apr) break;
+#pragma unroll
+                for (int b = 0; b < A; b++) {
+                    if (b >= apr) break;
+                    const float dx = fdelta(pa[k].x, pb[b].x, Ls0, Ll0), dy = fdelta(pa[k].y, pb[b].y, Ls1, Ll1),
+                                dz = fdelta(pa[k].z, pb[b].z, Ls2, Ll2);
+                    const float u = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (u > c2) continue;
+                    // slot k of r against slot b of q (F.w holds the slot)
+                    // slot k of r against slot b of q (F.w holds the slot); float-float charge and
+                    // LJ constants: per-type roundings of the products are systematic biases that
+                    // the cancellation in the total would amplify
                     float el, vd;
-                    mixed_pair(u, C.tab[pa.w][pb.w][0], C.tab[pa.w][pb.w][3], C.tab[pa.w][pb.w][1], C.tab[pa.w][pb.w][2],
-                               true, cut, el, vd, C.tablo[pa.w][pb.w][0], C.tablo[pa.w][pb.w][1]);
-                    acc.add(el);
-                    acc.add(vd);
+                    mixed_pair(u, C.tab[k][b][0], C.tab[k][b][3], C.tab[k][b][1], C.tab[k][b][2], true, cut, el, vd,
+                               C.tablo[k][b][0], C.tablo[k][b][1]);
+                    float sm, er;
+                    two_sum(eh, el, sm, er);
+                    eh = sm;
+                    elo += er;
+                    two_sum(vh, vd, sm, er);
+                    vh = sm;
+                    vlo += er;
                 }
             }
         }
-        const double v = warp_sum(acc.value());
+        const double v = warp_sum(((double)eh + (double)elo) + ((double)vh + (double)vlo));
         if (lane == 0) e_res[gr] = v;
     }
 }
@@ -1774,6 +1798,27 @@ int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double*
     st[chain].etot = e[chain];
     BK(cudaMemcpyAsync(b->d_state + chain, &st[chain], sizeof(ChainState), cudaMemcpyHostToDevice, b->stream));
     BK(cudaStreamSynchronize(b->stream));
+    return MCG_OK;
+}
+
+int mcg_batch_get_lists(mcg_batch* b, int chain, int* counts, int* entries, int64_t cap, int64_t* total) {
+    if (!b || chain < 0 || chain >= b->nchains || !counts || !total) return fail(MCG_EINVAL, "bad arguments");
+    const ChainDev& C = b->chains[chain];
+    std::vector<int> nl(C.nres);
+    BK(cudaMemcpyAsync(nl.data(), b->d_NL + C.res0, sizeof(int) * C.nres, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    int64_t tot = 0;
+    for (int r = 0; r < C.nres; r++) { counts[r] = nl[r]; tot += nl[r]; }
+    *total = tot;
+    if (entries && cap >= tot) {
+        std::vector<uint16_t> rows((size_t)C.nres * b->G.cap);
+        BK(cudaMemcpyAsync(rows.data(), b->d_LST + (size_t)C.res0 * b->G.cap, sizeof(uint16_t) * rows.size(),
+                           cudaMemcpyDeviceToHost, b->stream));
+        BK(cudaStreamSynchronize(b->stream));
+        int64_t o = 0;
+        for (int r = 0; r < C.nres; r++)
+            for (int k = 0; k < nl[r]; k++) entries[o++] = rows[(size_t)r * b->G.cap + k];
+    }
     return MCG_OK;
 }
 

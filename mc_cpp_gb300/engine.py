@@ -176,6 +176,8 @@ class BatchChains:
         self.h = h
         self.natoms = int(L.mcg_batch_natoms(h))
         self.sizes = np.array([L.mcg_batch_chain_natoms(h, k) for k in range(self.nchains)])
+        # atoms per residue of each chain (rigid residues of one size per chain)
+        self._apr_of = [int(np.count_nonzero(s.resid == s.resid[0])) for s in chains]
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -227,6 +229,20 @@ class BatchChains:
         p = np.zeros(self.nchains, np.int64)
         native.check(native.lib().mcg_batch_pairs(self.h, p.ctypes.data_as(native._i64)))
         return p
+
+    def lists(self, chain: int):
+        """The chain's residue neighbour lists as they are now (one array per residue)."""
+        nres = int(self.sizes[chain]) // self._apr(chain)
+        counts = np.zeros(nres, np.int32)
+        total = C.c_int64(0)
+        L = native.lib()
+        native.check(L.mcg_batch_get_lists(self.h, chain, native.pi(counts), None, 0, C.byref(total)))
+        ent = np.zeros(max(1, total.value), np.int32)
+        native.check(L.mcg_batch_get_lists(self.h, chain, native.pi(counts), native.pi(ent), total.value, C.byref(total)))
+        return np.split(ent[:total.value], np.cumsum(counts)[:-1])
+
+    def _apr(self, chain: int) -> int:
+        return self._apr_of[chain]
 
     def update_lists(self) -> None:
         native.check(native.lib().mcg_batch_update_lists(self.h))

@@ -123,6 +123,7 @@ def lib():
         "mcg_batch_energy_mixed": (C.c_int, [P, _d]),
         "mcg_batch_pairs": (C.c_int, [P, _i64]),
         "mcg_batch_update_lists": (C.c_int, [P]),
+        "mcg_batch_get_lists": (C.c_int, [P, C.c_int, _i, _i, C.c_int64, _i64]),
         "mcg_pair_count": (C.c_int, [P, _i64, _i64]),
         "mcg_time_nonbonded": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
         "mcg_mdbas_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P)]),
