@@ -15,7 +15,7 @@
 // the cutoff is ever missed.
 //
 // HBM layout (pools over all chains, chain c owns a contiguous slice):
-//   M[atoms]      ulonglong4  master coordinates as 64-bit fixed-point box fractions (x, y, z):
+//   M[atoms]      ulonglong4_32a  master coordinates as 64-bit fixed-point box fractions (x, y, z):
 //                 exact, wrap-free integer updates, resolution L/2^64 (finer than FP64 anywhere in
 //                 the box); FP64 views (x = int64 * L/2^64) are formed only for output and checks
 //   F[atoms]      uint4    32-bit mirror = the high words of M (w = residue slot type)
@@ -409,7 +409,7 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // shared memory (distributed shared memory), and the iteration's barrier is the cluster barrier.
 // In-sweep list rebuilds are done by CTA 0 while CTA 1 waits at the cluster barrier.
 template <int APR, int NT, int CL>
-__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4* M,
+__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4_32a* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         const int nmoves = C.nres;
         long long npairs = 0;
         uint4* Fc = F + C.atom0;
-        ulonglong4* Mc = M + C.atom0;
+        ulonglong4_32a* Mc = M + C.atom0;
         int mv = 0, buf = 0;
         unsigned prev_acc = 0;                 // accepted moves of the previous iteration (records P[buf ^ 1])
         float eh = 0.0f, el = 0.0f;            // accepted dE of this sweep (float-float, warp 0 lane 0)
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     q_first[u] = e < G.cap ? row[e] : 0;
                 }
                 uint4 fo = Fc[a];
-                ulonglong4 mo = Mc[a];
+                ulonglong4_32a mo = Mc[a];
                 const uint4 fb = FB[C.atom0 + a];
                 // records of the previous iteration: accepted moves whose commits may not have landed
                 unsigned sub = 0;
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     const int h = __ffs(pm) - 1;
                     if (R[h].res == res) {
                         fo = R[h].fn[k];
-                        mo = make_ulonglong4(R[h].mn[k][0], R[h].mn[k][1], R[h].mn[k][2], 0ull);
+                        mo = make_ulonglong4_32a(R[h].mn[k][0], R[h].mn[k][1], R[h].mn[k][2], 0ull);
                     }
                 }
                 const uint4 fo0 = make_uint4(__shfl_sync(0xffffffffu, fo.x, 0), __shfl_sync(0xffffffffu, fo.y, 0),
@@ -731,7 +731,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             }
             if (gw == 0 && grp < ng && ((accmask >> grp) & 1u) && lane < apr) {   // commit: atom = lane
                 const int a = Q[grp].res * apr + lane;
-                Mc[a] = make_ulonglong4(Q[grp].mn[lane][0], Q[grp].mn[lane][1], Q[grp].mn[lane][2], 0ull);
+                Mc[a] = make_ulonglong4_32a(Q[grp].mn[lane][0], Q[grp].mn[lane][1], Q[grp].mn[lane][2], 0ull);
                 Fc[a] = Q[grp].fn[lane];
             }
             if (grp < ng) npairs += np;
@@ -785,7 +785,7 @@ __device__ __forceinline__ double master_to_f64(unsigned long long v, double L) 
 // ---- fresh FP64 energy of every chain (reference arithmetic, all pairs, cutoff + switch)
 constexpr int ETILE = 128;
 __global__ void k_batch_energy64(const ChainDev* __restrict__ chains, const int* __restrict__ tile_chain,
-                                 const int* __restrict__ tile_first, const ulonglong4* __restrict__ M,
+                                 const int* __restrict__ tile_first, const ulonglong4_32a* __restrict__ M,
                                  const double* __restrict__ prm, CutDev cut, double* part) {
     const int t = blockIdx.x;
     const int c = tile_chain[t];
@@ -797,13 +797,13 @@ __global__ void k_batch_energy64(const ChainDev* __restrict__ chains, const int*
         PbcDev pbc;
         pbc.type = 2;
         for (int k = 0; k < 3; k++) { pbc.L[k] = C.L[k]; pbc.rL[k] = C.rL[k]; }
-        const ulonglong4 ma = M[C.atom0 + i];
+        const ulonglong4_32a ma = M[C.atom0 + i];
         const double ax = master_to_f64(ma.x, C.L[0]), ay = master_to_f64(ma.y, C.L[1]), az = master_to_f64(ma.z, C.L[2]);
         const int ri = i / C.apr;
         const double* pa = prm + 3 * (size_t)(C.atom0 + i);
         for (int j = i + 1; j < n; j++) {
             if (j / C.apr == ri) continue;  // intra-residue pairs are excluded
-            const ulonglong4 mb = M[C.atom0 + j];
+            const ulonglong4_32a mb = M[C.atom0 + j];
             const double r2 = ref64_dist2(ax, ay, az, master_to_f64(mb.x, C.L[0]), master_to_f64(mb.y, C.L[1]),
                                           master_to_f64(mb.z, C.L[2]), pbc);
             if (r2 > cut.c2) continue;
@@ -914,7 +914,7 @@ __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const do
 
 // FP64 coordinates (all chains concatenated) -> 64-bit masters and 32-bit mirrors
 __global__ void k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz, int64_t natoms,
-                               ulonglong4* M, uint4* F, int nchains) {
+                               ulonglong4_32a* M, uint4* F, int nchains) {
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
@@ -928,12 +928,12 @@ __global__ void k_batch_import(const ChainDev* __restrict__ chains, const double
             if (u >= 0.5) u -= 1.0;
             m[k] = (unsigned long long)__double2ll_rn(u * TWO64);
         }
-        M[a] = make_ulonglong4(m[0], m[1], m[2], 0ull);
+        M[a] = make_ulonglong4_32a(m[0], m[1], m[2], 0ull);
         F[a] = make_uint4((uint32_t)(m[0] >> 32), (uint32_t)(m[1] >> 32), (uint32_t)(m[2] >> 32), (uint32_t)(i % C.apr));
     }
 }
 
-__global__ void k_batch_export(const ChainDev* __restrict__ chains, const ulonglong4* __restrict__ M, int64_t natoms,
+__global__ void k_batch_export(const ChainDev* __restrict__ chains, const ulonglong4_32a* __restrict__ M, int64_t natoms,
                                double* xyz, int nchains) {
     const int c = blockIdx.x;
     if (c >= nchains) return;
@@ -941,7 +941,7 @@ __global__ void k_batch_export(const ChainDev* __restrict__ chains, const ulongl
     const int n = C.nres * C.apr;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int64_t a = C.atom0 + i;
-        const ulonglong4 m = M[a];
+        const ulonglong4_32a m = M[a];
         xyz[a] = master_to_f64(m.x, C.L[0]);
         xyz[natoms + a] = master_to_f64(m.y, C.L[1]);
         xyz[2 * natoms + a] = master_to_f64(m.z, C.L[2]);
@@ -981,7 +981,7 @@ struct mcg_batch {
     int* d_order = nullptr;       // chains of each CTA, CTA after CTA (d_cta_start: CSR offsets)
     int* d_cta_start = nullptr;
     int ncta = 0;
-    ulonglong4* d_M = nullptr;
+    ulonglong4_32a* d_M = nullptr;
     uint4 *d_F = nullptr, *d_FB = nullptr;
     uint16_t* d_LST = nullptr;
     int *d_NL = nullptr, *d_gorder = nullptr, *d_gcell = nullptr, *d_gstarts = nullptr, *d_res_chain = nullptr;
@@ -1266,7 +1266,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     B->nchains = nchains;
     const mcg_system_desc& d0 = descs[0];
     const double rc = d0.cutoff, ron = d0.cuton, skin = d0.dcut > 0 ? d0.dcut : 2.0;
-    std::vector<ulonglong4> M;
+    std::vector<ulonglong4_32a> M;
     std::vector<uint4> F;
     std::vector<double> prm;
     double rext = 0.0;       // largest distance from a residue's first atom to its other atoms
@@ -1335,7 +1335,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
                 C.tablo[a][b][1] = (float)(s * s - (double)(float)(s * s));
             }
         for (int i = 0; i < hs.n; i++) {
-            ulonglong4 m;
+            ulonglong4_32a m;
             m.x = host_master(hs.x[i], hs.rL[0]); m.y = host_master(hs.y[i], hs.rL[1]); m.z = host_master(hs.z[i], hs.rL[2]); m.w = 0;
             M.push_back(m);
             F.push_back(make_uint4((uint32_t)(m.x >> 32), (uint32_t)(m.y >> 32), (uint32_t)(m.z >> 32), (uint32_t)(i % apr)));
@@ -1467,7 +1467,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         BK(cudaMemcpy(B->d_res_chain, rcn.data(), sizeof(int) * res0, cudaMemcpyHostToDevice));
     }
     BK(cudaMemcpyAsync(B->d_chains, B->chains.data(), sizeof(ChainDev) * nchains, cudaMemcpyHostToDevice, B->stream));
-    BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4) * atom0, cudaMemcpyHostToDevice, B->stream));
+    BK(cudaMemcpyAsync(B->d_M, M.data(), sizeof(ulonglong4_32a) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_F, F.data(), sizeof(uint4) * atom0, cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemcpyAsync(B->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice, B->stream));
     BK(cudaMemsetAsync(B->d_state, 0, sizeof(ChainState) * nchains, B->stream));
@@ -1767,8 +1767,8 @@ int mcg_batch_get_coords(mcg_batch* b, int chain, double* x, double* y, double* 
     if (!b || chain < 0 || chain >= b->nchains || !x || !y || !z) return fail(MCG_EINVAL, "bad arguments");
     const ChainDev& C = b->chains[chain];
     int n = C.nres * C.apr;
-    std::vector<ulonglong4> M(n);
-    BK(cudaMemcpyAsync(M.data(), b->d_M + C.atom0, sizeof(ulonglong4) * n, cudaMemcpyDeviceToHost, b->stream));
+    std::vector<ulonglong4_32a> M(n);
+    BK(cudaMemcpyAsync(M.data(), b->d_M + C.atom0, sizeof(ulonglong4_32a) * n, cudaMemcpyDeviceToHost, b->stream));
     BK(cudaStreamSynchronize(b->stream));
     for (int i = 0; i < n; i++) { x[i] = host_view(M[i].x, C.L[0]); y[i] = host_view(M[i].y, C.L[1]); z[i] = host_view(M[i].z, C.L[2]); }
     return MCG_OK;
@@ -1778,14 +1778,14 @@ int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double*
     if (!b || chain < 0 || chain >= b->nchains || !x || !y || !z) return fail(MCG_EINVAL, "bad arguments");
     const ChainDev& C = b->chains[chain];
     int n = C.nres * C.apr;
-    std::vector<ulonglong4> M(n);
+    std::vector<ulonglong4_32a> M(n);
     std::vector<uint4> F(n);
     for (int i = 0; i < n; i++) {
         if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i])) return fail(MCG_EINVAL, "non-finite coordinate");
         M[i].x = host_master(x[i], C.rL[0]); M[i].y = host_master(y[i], C.rL[1]); M[i].z = host_master(z[i], C.rL[2]); M[i].w = 0;
         F[i] = make_uint4((uint32_t)(M[i].x >> 32), (uint32_t)(M[i].y >> 32), (uint32_t)(M[i].z >> 32), (uint32_t)(i % C.apr));
     }
-    BK(cudaMemcpyAsync(b->d_M + C.atom0, M.data(), sizeof(ulonglong4) * n, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_M + C.atom0, M.data(), sizeof(ulonglong4_32a) * n, cudaMemcpyHostToDevice, b->stream));
     BK(cudaMemcpyAsync(b->d_F + C.atom0, F.data(), sizeof(uint4) * n, cudaMemcpyHostToDevice, b->stream));
     int r = b->launch_build();
     if (r) return r;

@@ -30,20 +30,20 @@ static __device__ __align__(256) double g_noalloc_partials[2 * NOALLOC_MAX_BLOCK
 
 // Each block sums the switched pair terms of its 8 rows (a warp per row, lanes over the row's
 // j > i entries) and writes (elec, vdw) unscaled to its own slot of the static scratch.
-__global__ void __launch_bounds__(256) k_noalloc_energy(const double4* __restrict__ pq, const double2* __restrict__ es,
+__global__ void __launch_bounds__(256) k_noalloc_energy(const double4_32a* __restrict__ pq, const double2* __restrict__ es,
                                                         const int* __restrict__ nbr, const int* __restrict__ nup, int n,
                                                         int cap, PbcDev pbc, CutDev cut, double* partials) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * NOALLOC_ROWS_PER_BLOCK + w;
     double sel = 0.0, svd = 0.0;
     if (i < n) {
-        const double4 pi = pq[i];
+        const double4_32a pi = pq[i];
         const double2 ai = es[i];
         const int* row = nbr + (size_t)i * cap;
         const int m = nup[i];
         for (int k = lane; k < m; k += 32) {
             const int j = row[k];
-            const double4 pj = pq[j];
+            const double4_32a pj = pq[j];
             const double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
             if (r2 > cut.c2) continue;
             const double2 aj = es[j];
@@ -139,7 +139,7 @@ extern "C" int mcg_energy_switch_fp64_noalloc(int natom, const double* pq, const
     cut.c2f = (float)cut.c2; cut.n2f = (float)cut.n2; cut.sw2f = (float)cut.sw2;
     cudaStream_t st = (cudaStream_t)stream;
     const int nblocks = (natom + NOALLOC_ROWS_PER_BLOCK - 1) / NOALLOC_ROWS_PER_BLOCK;
-    k_noalloc_energy<<<nblocks, 256, 0, st>>>((const double4*)pq, (const double2*)es, nbr, nup, natom, cap, pbc, cut, scratch);
+    k_noalloc_energy<<<nblocks, 256, 0, st>>>((const double4_32a*)pq, (const double2*)es, nbr, nup, natom, cap, pbc, cut, scratch);
     k_noalloc_finalize<<<1, 256, 0, st>>>(scratch, nblocks, out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("launch: ") + cudaGetErrorString(e));

@@ -1,7 +1,7 @@
 // Single-system engine: the device side of FField_CUDA.
 //
 // Data layout in HBM (one system, n atoms):
-//   pq[n]        double4 (x, y, z, q)      FP64 master coordinates + charge (32 B, aligned loads)
+//   pq[n]        double4_32a (x, y, z, q)      FP64 master coordinates + charge (32 B, aligned loads)
 //   es[n]        double2 (eps, sig)        sqrt(eps*418.4) and MDBAS half-sigma
 //   es14[n]      double2 (eps14, sig14)
 //   fx[n]        uint4 (fx, fy, fz, q as float bits)  fixed-point mirror for the mixed kernels
@@ -58,11 +58,11 @@ struct Grid {
     int periodic;
 };
 
-__global__ void k_cell_assign(const double4* __restrict__ pq, int n, PbcDev pbc, Grid g, int* cell_of,
+__global__ void k_cell_assign(const double4_32a* __restrict__ pq, int n, PbcDev pbc, Grid g, int* cell_of,
                               int* cell_count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double4 p = pq[i];
+    double4_32a p = pq[i];
     double c[3] = {p.x, p.y, p.z};
     int idx[3];
     for (int k = 0; k < 3; k++) {
@@ -161,7 +161,7 @@ __device__ __forceinline__ bool stored_excluded(int lo, int hi, const int* __res
 }
 
 // One warp per atom i; lanes walk the candidates of the stencil cells 32 at a time.
-__global__ void __launch_bounds__(256) k_build_rows(const double4* __restrict__ pq, const uint8_t* __restrict__ frozen,
+__global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restrict__ pq, const uint8_t* __restrict__ frozen,
                                                     int n, PbcDev pbc, Grid g, ListParams lp,
                                                     const int* __restrict__ cell_of, const int* __restrict__ cell_start,
                                                     const int* __restrict__ cell_atoms, const int* __restrict__ xs,
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4* __restrict__ 
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int i = warp; i < n; i += nwarps) {
-        double4 pi = pq[i];
+        double4_32a pi = pq[i];
         bool fi = frozen[i] != 0;
         int c = cell_of[i];
         int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4* __restrict__ 
                         if (t < e) {
                             j = cell_atoms[t];
                             if (j != i) {
-                                double4 pj = pq[j];
+                                double4_32a pj = pq[j];
                                 double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
                                 if (r2 <= lp.cutnb2 && !(fi && frozen[j])) {
                                     int a = min(i, j), bb = max(i, j);
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4* __restrict__ 
 // ------------------------------------------------------------------------------------------
 // Energies.
 struct AtomsDev {
-    const double4* pq;
+    const double4_32a* pq;
     const double2* es;
     const double2* es14;
     const uint4* fx;
@@ -251,7 +251,7 @@ struct AtomsDev {
 
 template <int P>
 __device__ __forceinline__ void pair_energy(const AtomsDev& A, const PbcDev& pbc, const CutDev& cut, bool fourteen,
-                                            double4 pi, uint4 fi, int i, double4 pj, uint4 fj, int j,
+                                            double4_32a pi, uint4 fi, int i, double4_32a pj, uint4 fj, int j,
                                             bool apply_cut, double& el, double& vd) {
     if (P == PREC_F64) {
         double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
@@ -309,14 +309,14 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     double sel = 0.0, svd = 0.0;
     for (int i = warp; i < n; i += nwarps) {
-        double4 pi = A.pq[i];
+        double4_32a pi = A.pq[i];
         uint4 fi = P == PREC_MIX ? A.fx[i] : make_uint4(0, 0, 0, 0);
         const int* row = nbr + (size_t)i * cap;
         int m = nup[i];
         F32Acc fe, fv;
         for (int k = lane; k < m; k += 32) {
             int j = row[k];
-            double4 pj = P == PREC_F64 ? A.pq[j] : make_double4(0, 0, 0, 0);
+            double4_32a pj = P == PREC_F64 ? A.pq[j] : make_double4_32a(0, 0, 0, 0);
             uint4 fj = P == PREC_MIX ? A.fx[j] : make_uint4(0, 0, 0, 0);
             if (P == PREC_MIX && pbc.type == 0) pj = A.pq[j];
             double el, vd;
@@ -409,7 +409,7 @@ template <int P>
 __global__ void __launch_bounds__(TILE) k_energy_all(AtomsDev A, int n, PbcDev pbc, CutDev cut,
                                                      const int* __restrict__ fxs, const int* __restrict__ fxd,
                                                      int ntile, double* part) {
-    __shared__ double4 spq[TILE];
+    __shared__ double4_32a spq[TILE];
     __shared__ uint4 sfx[TILE];
     // block -> (I, J) with I <= J, row-major over the upper triangle
     int b = blockIdx.x;
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(TILE) k_energy_all(AtomsDev A, int n, PbcDev p
     __syncthreads();
     double sel = 0.0, svd = 0.0;
     if (i < n) {
-        double4 pi = A.pq[i];
+        double4_32a pi = A.pq[i];
         uint4 fi = P == PREC_MIX ? A.fx[i] : make_uint4(0, 0, 0, 0);
         int xb = fxs[i], xe = fxs[i + 1];
         int cur = xb;
@@ -470,8 +470,8 @@ struct BondedDev {
     const TorsT* imprs; int ni;
 };
 
-__device__ __forceinline__ void crd(const double4* pq, int i, double c[3]) {
-    double4 p = pq[i]; c[0] = p.x; c[1] = p.y; c[2] = p.z;
+__device__ __forceinline__ void crd(const double4_32a* pq, int i, double c[3]) {
+    double4_32a p = pq[i]; c[0] = p.x; c[1] = p.y; c[2] = p.z;
 }
 __device__ __forceinline__ void apply_pbc(double d[3], const PbcDev& p) {
     if (p.type != 0) for (int k = 0; k < 3; k++) d[k] = ref64_mic(d[k], p.L[k], p.rL[k]);
@@ -479,7 +479,7 @@ __device__ __forceinline__ void apply_pbc(double d[3], const PbcDev& p) {
 
 // crd_of: coordinates of atom i, with moved atoms taken from the proposal.
 struct CrdSrc {
-    const double4* pq;
+    const double4_32a* pq;
     const int* mv_idx; const double* mv_xyz; int m;   // sorted moved atoms (may be m = 0)
     __device__ __forceinline__ void get(int i, double c[3]) const {
         int lo = 0, hi = m - 1;
@@ -540,7 +540,7 @@ __device__ double tors_e(const TorsT& t, const CrdSrc& S, const PbcDev& pbc) {
 }
 
 // part layout: 5 doubles per block (bond, ang, ub, dihe, impr)
-__global__ void k_bonded(BondedDev B, PbcDev pbc, const double4* __restrict__ pq, double* part) {
+__global__ void k_bonded(BondedDev B, PbcDev pbc, const double4_32a* __restrict__ pq, double* part) {
     double e[5] = {0, 0, 0, 0, 0};
     CrdSrc S{pq, nullptr, nullptr, 0};
     int total = B.nb + B.na + B.nu + B.nd + B.ni;
@@ -648,8 +648,8 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
     if ((int)blockIdx.x < m) {
         const int ka = blockIdx.x;
         const int a = s_idx[ka];
-        const double4 ao = A.pq[a];
-        const double4 an = make_double4(s_xyz[3 * ka], s_xyz[3 * ka + 1], s_xyz[3 * ka + 2], ao.w);
+        const double4_32a ao = A.pq[a];
+        const double4_32a an = make_double4_32a(s_xyz[3 * ka], s_xyz[3 * ka + 1], s_xyz[3 * ka + 2], ao.w);
         const uint4 fo = P == PREC_MIX ? A.fx[a] : make_uint4(0, 0, 0, 0);
         const uint4 fn = P == PREC_MIX ? s_fx[ka] : make_uint4(0, 0, 0, 0);
         CutDev cutx = cut;   // full mode: no cutoff and no switch
@@ -667,9 +667,9 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         auto visit = [&](int j, bool fourteen, bool apply_cut) {
             int sj = slot(j);
             if (sj >= 0 && j < a) return;       // counted by the lower index's block
-            double4 jo = A.pq[j];
+            double4_32a jo = A.pq[j];
             uint4 gjo = P == PREC_MIX ? A.fx[j] : make_uint4(0, 0, 0, 0);
-            double4 jn = jo;
+            double4_32a jn = jo;
             uint4 gjn = gjo;
             if (sj >= 0) { jn.x = s_xyz[3 * sj]; jn.y = s_xyz[3 * sj + 1]; jn.z = s_xyz[3 * sj + 2]; if (P == PREC_MIX) gjn = s_fx[sj]; }
             if (P == PREC_F64) {
@@ -792,12 +792,12 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
 }
 
 template <int P>
-__global__ void k_commit(int m, const int* __restrict__ idx, const double* __restrict__ xyz, double4* pq, uint4* fx,
+__global__ void k_commit(int m, const int* __restrict__ idx, const double* __restrict__ xyz, double4_32a* pq, uint4* fx,
                          PbcDev pbc) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     int a = idx[k];
-    double4 p = pq[a];
+    double4_32a p = pq[a];
     p.x = xyz[3 * k]; p.y = xyz[3 * k + 1]; p.z = xyz[3 * k + 2];
     pq[a] = p;
     if (pbc.type != 0) {
@@ -807,10 +807,10 @@ __global__ void k_commit(int m, const int* __restrict__ idx, const double* __res
     }
 }
 
-__global__ void k_fix_all(int n, const double4* __restrict__ pq, uint4* fx, PbcDev pbc) {
+__global__ void k_fix_all(int n, const double4_32a* __restrict__ pq, uint4* fx, PbcDev pbc) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double4 p = pq[i];
+    double4_32a p = pq[i];
     uint4 f;
     if (pbc.type != 0) { f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]); }
     else { f.x = f.y = f.z = 0; }
@@ -864,12 +864,12 @@ int SingleEngine::init(const HostSystem& h) {
         cut.sw2 = 1. / (d * d * d);
     }
     cut.c2f = (float)cut.c2; cut.n2f = (float)cut.n2; cut.sw2f = (float)cut.sw2;
-    std::vector<double4> pq(n);
+    std::vector<double4_32a> pq(n);
     std::vector<double2> es(n), es14(n);
     std::vector<float2> esf(n), esf14(n), qf(n);
     std::vector<float4> prmf(n);
     for (int i = 0; i < n; i++) {
-        pq[i] = make_double4(hs.x[i], hs.y[i], hs.z[i], hs.q[i]);
+        pq[i] = make_double4_32a(hs.x[i], hs.y[i], hs.z[i], hs.q[i]);
         es[i] = make_double2(hs.eps[i], hs.sig[i]);
         es14[i] = make_double2(hs.eps14[i], hs.sig14[i]);
         esf[i] = make_float2((float)hs.eps[i], (float)hs.sig[i]);
@@ -1132,14 +1132,14 @@ int SingleEngine::energy(double ener[10]) {
 }
 
 int SingleEngine::set_coords(const double* x, const double* y, const double* z) {
-    std::vector<double4> pq(n);
+    std::vector<double4_32a> pq(n);
     for (int i = 0; i < n; i++) {
         if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i]))
             return fail(MCG_EINVAL, "non-finite coordinate at atom " + std::to_string(i));
-        pq[i] = make_double4(x[i], y[i], z[i], hs.q[i]);
+        pq[i] = make_double4_32a(x[i], y[i], z[i], hs.q[i]);
         host_x[i] = x[i]; host_y[i] = y[i]; host_z[i] = z[i];
     }
-    CK(cudaMemcpyAsync(d_pq, pq.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_pq, pq.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
     k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
@@ -1147,8 +1147,8 @@ int SingleEngine::set_coords(const double* x, const double* y, const double* z) 
 }
 
 int SingleEngine::get_coords(double* x, double* y, double* z) {
-    std::vector<double4> pq(n);
-    CK(cudaMemcpyAsync(pq.data(), d_pq, sizeof(double4) * n, cudaMemcpyDeviceToHost, stream));
+    std::vector<double4_32a> pq(n);
+    CK(cudaMemcpyAsync(pq.data(), d_pq, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     for (int i = 0; i < n; i++) { x[i] = pq[i].x; y[i] = pq[i].y; z[i] = pq[i].z; }
     return MCG_OK;

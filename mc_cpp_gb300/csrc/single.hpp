@@ -48,7 +48,7 @@ private:
     PbcDev pbc{};
     CutDev cut{};
     int n14 = 0, ntile = 0;
-    double4* d_pq = nullptr;
+    double4_32a* d_pq = nullptr;
     double2 *d_es = nullptr, *d_es14 = nullptr;
     uint4* d_fx = nullptr;
     float2 *d_esf = nullptr, *d_esf14 = nullptr, *d_qf = nullptr;
