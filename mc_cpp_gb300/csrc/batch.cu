@@ -856,13 +856,25 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
 #pragma unroll
         for (int k = 0; k < A; k++) pa[k] = k < apr ? Fc[r * apr + k] : make_uint4(0, 0, 0, 0);
         float eh = 0.0f, elo = 0.0f, vh = 0.0f, vlo = 0.0f;
-        for (int e0 = 0; e0 < nl; e0 += 32) {
-            const int e = e0 + lane;
-            const int q = e < nl ? (int)row[e] : -1;
-            if (q <= r) continue;
-            uint4 pb[A];
+        // two list entries in flight per lane: both entries' neighbour atoms are loaded before
+        // either is evaluated
+        constexpr int U = APR ? 2 : 1;
+        for (int e0 = 0; e0 < nl; e0 += 32 * U) {
+          int qq[U];
+          uint4 pbb[U][A];
 #pragma unroll
-            for (int b = 0; b < A; b++) pb[b] = b < apr ? Fc[q * apr + b] : make_uint4(0, 0, 0, 0);
+          for (int v = 0; v < U; v++) {
+            const int e = e0 + v * 32 + lane;
+            qq[v] = e < nl ? (int)row[e] : -1;
+          }
+#pragma unroll
+          for (int v = 0; v < U; v++)
+#pragma unroll
+            for (int b = 0; b < A; b++) pbb[v][b] = (qq[v] > r && b < apr) ? Fc[qq[v] * apr + b] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+          for (int v = 0; v < U; v++) {
+            if (qq[v] <= r) continue;
+            const uint4* pb = pbb[v];
 #pragma unroll
             for (int k = 0; k < A; k++) {
                 if (k >= apr) break;
@@ -889,6 +901,7 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
                     vlo += er;
                 }
             }
+          }
         }
         const double v = warp_sum(((double)eh + (double)elo) + ((double)vh + (double)vlo));
         if (lane == 0) e_res[gr] = v;
