@@ -259,10 +259,12 @@ def run_ours(args):
     barrier()
     t0, a0, _ = B.stats()
     p0 = B.pairs()
+    _, nl0 = B.counters()
     with ClockSampler(local) as clk:
         barrier()
         ms, ms_lists, ms_sweep = B.time_phases(args.steps)
         barrier()
+    _, nl1 = B.counters()
     t1, a1, e1 = B.stats()
     p1 = B.pairs()
     acc = float((a1 - a0).sum())
@@ -337,7 +339,7 @@ def run_ours(args):
                          "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
             "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(3 * natoms * 8),
                     "d2h_bytes_per_step": int(3 * natoms * 8 + args.chains * 16)},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": int(nl1 - nl0),
             "list_rebuilds_total": int(rb),
             "clocks": clk.summary(),
             "plain_fp64": plain,

@@ -124,6 +124,7 @@ struct BatchGeom {
     float indep2;      // (rc + 2 extents + 2 largest moves)^2: two moves cannot interact beyond it
     float subst2;      // (list centre radius + skin)^2: a residue farther than this is in no list of the other
     float pre2;        // a chain whose atoms moved less than this (squared) since the build keeps its lists
+    float pair2;       // (rc + 2 extents)^2: residues whose first atoms are farther share no atom pair within rc
     int cap;
 };
 
@@ -867,6 +868,16 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
             const int e = e0 + v * 32 + lane;
             qq[v] = e < nl ? (int)row[e] : -1;
           }
+          // first atoms farther than rc + 2 extents: no atom pair of the two residues is within rc
+#pragma unroll
+          for (int v = 0; v < U; v++) {
+            if (qq[v] > r) {
+              const uint4 q0 = Fc[qq[v] * apr];
+              const float dx = fdelta(pa[0].x, q0.x, Ls0, Ll0), dy = fdelta(pa[0].y, q0.y, Ls1, Ll1),
+                          dz = fdelta(pa[0].z, q0.z, Ls2, Ll2);
+              if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > G.pair2) qq[v] = -1;
+            }
+          }
 #pragma unroll
           for (int v = 0; v < U; v++)
 #pragma unroll
@@ -1102,6 +1113,8 @@ struct mcg_batch {
         return MCG_OK;
     }
     int ensure_graph() { return graph ? MCG_OK : capture(&graph, false); }
+    // kernels one replay of the sweep graph launches: bin, lists, and the one-CTA and/or cluster sweep
+    int kernels_per_sweep() const { return 2 + (ncta > 0 ? 1 : 0) + (ncl > 0 ? 1 : 0); }
     int ensure_timed_graph() {
         if (tgraph) return MCG_OK;
         for (cudaEvent_t& e : tev)
@@ -1388,6 +1401,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
     G.indep2 = (float)(rind * rind);
     G.pre2 = (float)((0.55 * 0.5 * skin) * (0.55 * 0.5 * skin));
+    G.pair2 = (float)((rc + 2.0 * rext + 1e-3) * (rc + 2.0 * rext + 1e-3));
     {
         const double rs = rlist + 2 * rext + skin + 0.01;
         G.subst2 = (float)(rs * rs);
@@ -1538,7 +1552,7 @@ int mcg_batch_sweep(mcg_batch* b, int nsweeps) {
     int r = b->ensure_graph();
     if (r) return r;
     for (int s = 0; s < nsweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
-    b->launches += 3 * (int64_t)nsweeps;
+    b->launches += b->kernels_per_sweep() * (int64_t)nsweeps;
     return MCG_OK;
 }
 
@@ -1553,7 +1567,7 @@ int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms) {
     BK(cudaEventRecord(b->ev1, b->stream));
     BK(cudaEventSynchronize(b->ev1));
     BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
-    b->launches += 3 * (int64_t)nsweeps;
+    b->launches += b->kernels_per_sweep() * (int64_t)nsweeps;
     return MCG_OK;
 }
 
@@ -1579,7 +1593,7 @@ int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_
     BK(cudaEventElapsedTime(ms_total, b->ev0, b->ev1));
     *ms_lists = (float)tl;
     *ms_sweep = (float)ts;
-    b->launches += 3 * (int64_t)nsweeps;
+    b->launches += b->kernels_per_sweep() * (int64_t)nsweeps;
     return MCG_OK;
 }
 
@@ -1648,7 +1662,7 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
         BK(cudaEventSynchronize(b->ev1));
         BK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
         *ms /= (float)n;
-        b->launches += 3 * (int64_t)(n + 1);
+        b->launches += b->kernels_per_sweep() * (int64_t)(n + 1);
         return MCG_OK;
     };
     // stage 1: every shape
