@@ -462,9 +462,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
             s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
                                                           C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
-        CutDev cut;
-        cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
-        cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
+        const float c2f = G.c2f, n2f = G.n2f, sw2f = G.sw2f, k3f = G.c2f - 3.0f * G.n2f;
         ChainState S = state[c];
         if (tid == 0) { s_err = 0; s_pairs = 0ull; }
         __syncthreads();
@@ -601,7 +599,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                             ez -= (ez > C.Lhalf[2]) ? C.Lf[2] : ((ez < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
                         }
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
-                        acc += mixed_pair_delta(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, cut, np);
+                        acc += mixed_pair_delta_clamped(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, c2f, n2f,
+                                                        k3f, sw2f, np);
                     }
                 };
                 int head = 0, tail = 0;
