@@ -431,9 +431,10 @@ def _water100k(tf_peak):
     out = {}
     w = systems.water_box(33334, seed=11)
     res5 = {"atoms": w.natom}
+    etot = {}
     for prec in ("fp64", "mixed"):
         ff = FFieldCUDA(w, prec, moves=False)
-        ff.getE()
+        etot[prec] = ff.getE()
         t = time.perf_counter()
         for _ in range(10):
             ff.getE()
@@ -453,6 +454,18 @@ def _water100k(tf_peak):
         if prec == "mixed" and tf_peak:
             res5[prec]["pair_kernel_fp32_tflops"] = inc * FLOPS_PER_PAIR / (kms * 1e-3) / 1e12
             res5[prec]["pair_kernel_fp32_frac_of_probe"] = res5[prec]["pair_kernel_fp32_tflops"] / tf_peak
+        if prec == "mixed":
+            # every variant of the mixed pair kernel (0-3 per-atom list, 4+ cluster-pair), CUDA events
+            chosen, nv = ff.pair_kernel()
+            per = {}
+            for v in range(nv):
+                ff.set_pair_kernel(v)
+                per[str(v)] = ff.time_nonbonded(20) / 20
+            ff.set_pair_kernel(chosen)
+            ncl, ncp, nbits = ff.cluster_stats()
+            res5[prec].update({"pair_kernel_variant": chosen, "variant_ms": per,
+                               "clusters": ncl, "cluster_pairs": ncp, "cluster_mask_pairs": nbits,
+                               "rel_total_E_err_vs_fp64": abs(etot["mixed"] - etot["fp64"]) / abs(etot["fp64"])})
         res5["list_pairs"], res5["pairs_in_cutoff"] = lp, inc
         ff.close()
     out["water100k"] = res5

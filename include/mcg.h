@@ -132,6 +132,18 @@ int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
 /* Device time (ms, CUDA events on the handle's stream) of reps launches of the switched
  * nonbonded pair kernel alone over the current list (switch mode). */
 int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);
+/* Kernel of the mixed-precision periodic switch energy (an addition without a reference
+ * counterpart: FField_MDBAS has one scalar loop).  variant -1 (the default) times every variant
+ * at the first energy and keeps the fastest; 0..3 are per-atom list kernels; 4 and above are
+ * cluster-pair kernels over the cluster form of the same Verlet list (MCG_ENOTSUP when it was
+ * not built).  mcg_get_pair_kernel reports the variant in use (-1 before the first energy) and
+ * the number of variants. */
+int mcg_set_pair_kernel(mcg_system* s, int variant);
+int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count);
+/* Cluster form of the current Verlet list (mixed periodic switch systems; zeros otherwise):
+ * clusters of 8 atoms, cluster pairs in the list, and the Verlet pairs their masks encode (equal
+ * to the half-list size when the cluster list is complete). */
+int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
 /* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
  * exclList[i]) and the 1-4 pair list (getNeighList14). */
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);

@@ -142,6 +142,27 @@ int mcg_time_nonbonded(mcg_system* s, int reps, float* ms) {
     return s->eng.time_nonbonded(reps, ms);
 }
 
+int mcg_set_pair_kernel(mcg_system* s, int variant) {
+    if (!s) return fail(MCG_EINVAL, "null argument");
+    return s->eng.set_pair_kernel(variant);
+}
+
+int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count) {
+    if (!s || !variant || !count) return fail(MCG_EINVAL, "null argument");
+    *variant = s->eng.pair_kernel();
+    *count = SingleEngine::pair_kernel_count();
+    return MCG_OK;
+}
+
+int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs) {
+    if (!s || !clusters || !cluster_pairs || !mask_pairs) return fail(MCG_EINVAL, "null argument");
+    const ClusterPairs& c = s->eng.clp;
+    *clusters = c.ok ? c.ncl : 0;
+    *cluster_pairs = c.ok ? c.npairs : 0;
+    *mask_pairs = c.ok ? c.nbits : 0;
+    return MCG_OK;
+}
+
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {
     if (!s || !counts) return fail(MCG_EINVAL, "null argument");
     const HostSystem& h = s->eng.hs;

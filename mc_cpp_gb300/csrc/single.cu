@@ -953,9 +953,15 @@ int SingleEngine::launch_nonbonded(double* nbp) {
     return NB_BLOCKS;
 }
 
-static const int kPairVariants = 4;
+static const int kListVariants = 4;
+
+int SingleEngine::pair_kernel_count() { return kListVariants + ClusterPairs::kVariants; }
 
 int SingleEngine::launch_pair_variant(int v, double* nbp) {
+    if (v >= kListVariants) {
+        launches += 1;   // the pack kernel in front of the cluster kernel
+        return clp.launch_energy(stream, v - kListVariants, d_fx, d_prmf, cluster_geom(), nbp);
+    }
     AtomsDev A = atoms();
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
@@ -968,18 +974,20 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     default: k_energy_list_mix<8, 3><<<152 * 3, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
                                                                         A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
     }
-    static const int kBlocks[kPairVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
-    return kBlocks[v < 0 || v >= kPairVariants ? kPairVariants - 1 : v];
+    static const int kBlocks[kListVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
+    return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
 }
 
-// Times every pair-kernel variant on the current system (3 launches each) and keeps the fastest.
+// Times every pair-kernel variant on the current system (3 launches each) and keeps the fastest;
+// the cluster-pair variants take part when the cluster list was built.
 void SingleEngine::tune_pair_kernel() {
     cudaEvent_t a, b;
     pair_variant = 0;
     if (cudaEventCreate(&a) != cudaSuccess) return;
     if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return; }
     float best = 3.0e38f;
-    for (int v = 0; v < kPairVariants; v++) {
+    const int nv = clp.ok ? pair_kernel_count() : kListVariants;
+    for (int v = 0; v < nv; v++) {
         launch_pair_variant(v, d_part);
         cudaEventRecord(a, stream);
         for (int r = 0; r < 3; r++) launch_pair_variant(v, d_part);
@@ -988,9 +996,54 @@ void SingleEngine::tune_pair_kernel() {
         if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) continue;
         if (ms < best) { best = ms; pair_variant = v; }
     }
-    launches += 4 * kPairVariants;
+    launches += 4 * nv;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+}
+
+int SingleEngine::set_pair_kernel(int v) {
+    if (v < -1 || v >= pair_kernel_count()) return fail(MCG_EINVAL, "pair-kernel variant out of range");
+    if (v >= kListVariants && !clp.ok)
+        return fail(MCG_ENOTSUP, "no cluster-pair list: the cluster kernels need a periodic box, mixed precision and switch mode");
+    if (v >= 0 && (hs.prec != MCG_PREC_MIXED || pbc.type == 0 || hs.cut != MCG_CUT_SWITCH))
+        return fail(MCG_ENOTSUP, "pair-kernel variants apply to the mixed periodic switch energy");
+    pair_variant = v;
+    return MCG_OK;
+}
+
+ClusterGeom SingleEngine::cluster_geom() const {
+    ClusterGeom G;
+    AtomsDev A = atoms();
+    for (int k = 0; k < 3; k++) {
+        G.Ls[k] = A.Ls[k];
+        G.Ll[k] = A.Lsl[k];
+        G.Lf[k] = (float)hs.L[k];
+        G.iLf[k] = (float)(1.0 / hs.L[k]);
+        G.lim[k] = (float)(hs.L[k] - hs.rc - 0.01);
+    }
+    G.c2 = cut.c2f;
+    G.n2 = cut.n2f;
+    G.k3 = cut.c2f - 3.0f * cut.n2f;
+    const float pr = (float)(hs.rc + 0.01);
+    G.prune2 = pr * pr;
+    // the FP32 switch polynomial at u = ron^2, as the kernel forms it
+    const float a = G.c2 - G.n2;
+    const float aa = a * a;
+    const float bb = std::fmaf(2.0f, G.n2, G.k3);
+    const float f1 = aa * bb;
+    G.inv_f1 = 1.0 / (double)f1;
+    return G;
+}
+
+int SingleEngine::ensure_part(size_t count) {
+    if (count <= part_cap) return MCG_OK;
+    if (d_part) cudaFree(d_part);
+    d_part = nullptr;
+    part_cap = 0;
+    int rc = dalloc(&d_part, count);
+    if (rc) return rc;
+    part_cap = count;
+    return MCG_OK;
 }
 
 int SingleEngine::time_nonbonded(int reps, float* ms) {
@@ -1084,7 +1137,22 @@ int SingleEngine::build_list() {
         CK(cudaMemcpyAsync(&maxrow, d_maxrow, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         last_max_row = maxrow;
-        if (maxrow <= cap) return MCG_OK;
+        if (maxrow <= cap) {
+            if (hs.prec == MCG_PREC_MIXED && pbc.type != 0) {
+                // the cluster-pair form of the list; without it the per-atom list kernels run
+                const int crc = clp.build(stream, d_fx, n, hs.L, d_nbr, d_nup, d_nlo, cap);
+                if (crc == MCG_ECUDA) return crc;
+                if (crc == MCG_OK) {
+                    launches += clp.build_launches;
+                    clp.build_launches = 0;
+                    if ((rc = ensure_part((size_t)2 * clp.ncl + 2 * 64 + 5 * 64 + 16))) return rc;
+                } else {
+                    set_error("");
+                    if (pair_variant >= kListVariants) pair_variant = -1;
+                }
+            }
+            return MCG_OK;
+        }
         cudaFree(d_nbr);
         d_nbr = nullptr;
         cap = ((int)(maxrow * 1.1) + 32 + 31) & ~31;

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "cluster.hpp"
 #include "dev_types.hpp"
 #include "engine.hpp"
 
@@ -25,6 +26,12 @@ public:
     int commit();
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
     int time_nonbonded(int reps, float* ms);
+    // Pair-kernel variant of the mixed periodic switch energy: -1 = chosen by timing at the first
+    // use; 0..3 per-atom list kernels; 4.. cluster-pair kernels (when the cluster list exists).
+    int set_pair_kernel(int v);
+    int pair_kernel() const { return pair_variant; }
+    static int pair_kernel_count();
+    ClusterPairs clp;
 
     HostSystem hs;
     int n = 0;
@@ -43,6 +50,8 @@ private:
     void tune_pair_kernel();
     int pair_variant = -1;        // mixed pair-kernel variant, chosen by timing at the first use
     BondedDev bonded() const;
+    ClusterGeom cluster_geom() const;
+    int ensure_part(size_t count);
 
     cudaStream_t stream = nullptr;
     PbcDev pbc{};

@@ -99,6 +99,23 @@ class FFieldCUDA:
         native.check(native.lib().mcg_time_nonbonded(self.h, reps, C.byref(ms)))
         return ms.value
 
+    def set_pair_kernel(self, variant: int) -> None:
+        """Pins the mixed periodic switch-energy kernel (-1: fastest by timing at the first use;
+        0..3 per-atom list kernels; 4.. cluster-pair kernels)."""
+        native.check(native.lib().mcg_set_pair_kernel(self.h, variant))
+
+    def pair_kernel(self):
+        """(variant in use or -1, number of variants)."""
+        v, n = C.c_int(0), C.c_int(0)
+        native.check(native.lib().mcg_get_pair_kernel(self.h, C.byref(v), C.byref(n)))
+        return v.value, n.value
+
+    def cluster_stats(self):
+        """(clusters, cluster pairs, Verlet pairs in the masks) of the cluster form of the list."""
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        native.check(native.lib().mcg_cluster_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def pair_count(self):
         """(list pairs, pairs within the cutoff at the current coordinates)."""
         a, b = C.c_int64(0), C.c_int64(0)

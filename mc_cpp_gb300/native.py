@@ -126,6 +126,9 @@ def lib():
         "mcg_batch_get_lists": (C.c_int, [P, C.c_int, _i, _i, C.c_int64, _i64]),
         "mcg_pair_count": (C.c_int, [P, _i64, _i64]),
         "mcg_time_nonbonded": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
+        "mcg_set_pair_kernel": (C.c_int, [P, C.c_int]),
+        "mcg_get_pair_kernel": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "mcg_cluster_stats": (C.c_int, [P, _i64, _i64, _i64]),
         "mcg_mdbas_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P)]),
         "mcg_mdbas_natom": (C.c_int, [P]),
         "mcg_mdbas_fill": (C.c_int, [P, C.POINTER(SystemDesc)]),
