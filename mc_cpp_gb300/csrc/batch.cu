@@ -832,15 +832,23 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
                                                           const uint4* __restrict__ F, const int* __restrict__ res_chain,
                                                           const uint16_t* __restrict__ LST, const int* __restrict__ NL,
                                                           double* e_res, int64_t nres_total) {
-    // A warp per residue r, lanes over its list entries q > r, all atom pairs of (r, q), with r's
-    // atoms in registers.  Coulomb and LJ are summed per lane as float-float pairs (TwoSum), so the
-    // result does not depend on the list order beyond ~1e-14; the warp sums in FP64.
+    // A warp per residue r.  Lanes scan r's list 32 entries at a time; the entries q > r whose
+    // first atom lies within rc + 2 extents of r's are compacted into the warp's ring in shared
+    // memory, and each time 32 are pending every lane evaluates one residue pair: all atom pairs
+    // of (r, q), with r's atoms in registers.  Atom pairs beyond rc take r^2 = rc^2, where the
+    // switch is exactly 0 (no divergent skip).  Coulomb and LJ are summed per lane as float-float
+    // pairs (TwoSum), so the result does not depend on the list order beyond ~1e-14; the warp
+    // sums in FP64.
     constexpr int A = APR ? APR : MAX_APR;
+    constexpr int ERING = 64;
+    __shared__ int s_q[8][ERING];
     CutDev cut;
     cut.mode = 1; cut.c2 = 0; cut.n2 = 0; cut.sw2 = 0;
     cut.c2f = G.c2f; cut.n2f = G.n2f; cut.sw2f = G.sw2f;
     const float c2 = G.c2f;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int* ring = s_q[wib];
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
         const int c = res_chain[gr];
@@ -856,35 +864,11 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
 #pragma unroll
         for (int k = 0; k < A; k++) pa[k] = k < apr ? Fc[r * apr + k] : make_uint4(0, 0, 0, 0);
         float eh = 0.0f, elo = 0.0f, vh = 0.0f, vlo = 0.0f;
-        // two list entries in flight per lane: both entries' neighbour atoms are loaded before
-        // either is evaluated
-        constexpr int U = APR ? 2 : 1;
-        for (int e0 = 0; e0 < nl; e0 += 32 * U) {
-          int qq[U];
-          uint4 pbb[U][A];
+        // residue q (>= 0) against r, by this lane
+        auto eval = [&](int q) {
+            uint4 pb[A];
 #pragma unroll
-          for (int v = 0; v < U; v++) {
-            const int e = e0 + v * 32 + lane;
-            qq[v] = e < nl ? (int)row[e] : -1;
-          }
-          // first atoms farther than rc + 2 extents: no atom pair of the two residues is within rc
-#pragma unroll
-          for (int v = 0; v < U; v++) {
-            if (qq[v] > r) {
-              const uint4 q0 = Fc[qq[v] * apr];
-              const float dx = fdelta(pa[0].x, q0.x, Ls0, Ll0), dy = fdelta(pa[0].y, q0.y, Ls1, Ll1),
-                          dz = fdelta(pa[0].z, q0.z, Ls2, Ll2);
-              if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > G.pair2) qq[v] = -1;
-            }
-          }
-#pragma unroll
-          for (int v = 0; v < U; v++)
-#pragma unroll
-            for (int b = 0; b < A; b++) pbb[v][b] = (qq[v] > r && b < apr) ? Fc[qq[v] * apr + b] : make_uint4(0, 0, 0, 0);
-#pragma unroll
-          for (int v = 0; v < U; v++) {
-            if (qq[v] <= r) continue;
-            const uint4* pb = pbb[v];
+            for (int b = 0; b < A; b++) pb[b] = b < apr ? Fc[q * apr + b] : make_uint4(0, 0, 0, 0);
 #pragma unroll
             for (int k = 0; k < A; k++) {
                 if (k >= apr) break;
@@ -893,9 +877,7 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
                     if (b >= apr) break;
                     const float dx = fdelta(pa[k].x, pb[b].x, Ls0, Ll0), dy = fdelta(pa[k].y, pb[b].y, Ls1, Ll1),
                                 dz = fdelta(pa[k].z, pb[b].z, Ls2, Ll2);
-                    const float u = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    if (u > c2) continue;
-                    // slot k of r against slot b of q (F.w holds the slot)
+                    const float u = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), c2);
                     // slot k of r against slot b of q (F.w holds the slot); float-float charge and
                     // LJ constants: per-type roundings of the products are systematic biases that
                     // the cancellation in the total would amplify
@@ -911,8 +893,31 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
                     vlo += er;
                 }
             }
-          }
+        };
+        int head = 0, tail = 0;
+        for (int e0 = 0; e0 < nl; e0 += 32) {
+            const int e = e0 + lane;
+            const int q = e < nl ? (int)row[e] : -1;
+            bool keep = false;
+            if (q > r) {
+                // first atoms farther than rc + 2 extents: no atom pair of the two residues is within rc
+                const uint4 q0 = Fc[q * apr];
+                const float dx = fdelta(pa[0].x, q0.x, Ls0, Ll0), dy = fdelta(pa[0].y, q0.y, Ls1, Ll1),
+                            dz = fdelta(pa[0].z, q0.z, Ls2, Ll2);
+                keep = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= G.pair2;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) ring[(head + __popc(bal & lt_mask)) & (ERING - 1)] = q;
+            head += __popc(bal);
+            if (head - tail >= 32) {
+                __syncwarp();
+                eval(ring[(tail + lane) & (ERING - 1)]);
+                tail += 32;
+            }
+            __syncwarp();
         }
+        if (lane < head - tail) eval(ring[(tail + lane) & (ERING - 1)]);
+        __syncwarp();
         const double v = warp_sum(((double)eh + (double)elo) + ((double)vh + (double)vlo));
         if (lane == 0) e_res[gr] = v;
     }
@@ -936,12 +941,18 @@ __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const do
 }
 
 // FP64 coordinates (all chains concatenated) -> 64-bit masters and 32-bit mirrors
-__global__ void k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz, int64_t natoms,
-                               ulonglong4_32a* M, uint4* F, int nchains) {
+// The chain's largest squared displacement from its list-build positions FB enters state.maxd2, so
+// the next list build (k_batch_bin) rebuilds exactly the chains whose imported atoms moved beyond
+// the rebuild threshold.  Launched with 256 threads per chain.
+__global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz,
+                                                      int64_t natoms, ulonglong4_32a* M, uint4* F,
+                                                      const uint4* __restrict__ FB, ChainState* state, int nchains) {
+    __shared__ float s_max[8];
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     const int n = C.nres * C.apr;
+    float dmax = 0.0f;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int64_t a = C.atom0 + i;
         unsigned long long m[3];
@@ -952,7 +963,19 @@ __global__ void k_batch_import(const ChainDev* __restrict__ chains, const double
             m[k] = (unsigned long long)__double2ll_rn(u * TWO64);
         }
         M[a] = make_ulonglong4_32a(m[0], m[1], m[2], 0ull);
-        F[a] = make_uint4((uint32_t)(m[0] >> 32), (uint32_t)(m[1] >> 32), (uint32_t)(m[2] >> 32), (uint32_t)(i % C.apr));
+        const uint4 f = make_uint4((uint32_t)(m[0] >> 32), (uint32_t)(m[1] >> 32), (uint32_t)(m[2] >> 32), (uint32_t)(i % C.apr));
+        F[a] = f;
+        const uint4 fb = FB[a];
+        const float ex = fdelta(fb.x, f.x, C.Ls[0], C.Lsl[0]), ey = fdelta(fb.y, f.y, C.Ls[1], C.Lsl[1]),
+                    ez = fdelta(fb.z, f.z, C.Ls[2], C.Lsl[2]);
+        dmax = fmaxf(dmax, fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
+    }
+    for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = dmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) dmax = fmaxf(dmax, s_max[w]);
+        state[c].maxd2 = fmaxf(state[c].maxd2, dmax);
     }
 }
 
@@ -1717,10 +1740,12 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
     if ((xyz_in || xyz_out) && !b->d_xyz) { if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r; }
     if (xyz_in) {
         BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
-        k_batch_import<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M, b->d_F, b->nchains);
+        k_batch_import<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M, b->d_F, b->d_FB,
+                                                          b->d_state, b->nchains);
         BK(cudaGetLastError());
         b->launches++;
-        if ((r = b->launch_build()) || (r = b->launch_energy_list())) return r;
+        // lists of the chains whose atoms moved beyond the rebuild threshold, then the energies
+        if ((r = b->launch_build(b->stream, 0)) || (r = b->launch_energy_list())) return r;
     }
     if ((r = mcg_batch_sweep(b, nsweeps))) return r;
     if (xyz_out) {

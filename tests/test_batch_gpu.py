@@ -184,6 +184,32 @@ def test_host_buffer_run_roundtrip():
     assert np.array_equal(got, out)
 
 
+def test_host_import_rebuilds_only_chains_that_moved():
+    """Importing coordinates rebuilds the lists of exactly the chains whose atoms moved beyond the
+    rebuild threshold from their list-build positions; the energies are recomputed either way."""
+    ch = _waters((600, 900), seed=33)
+    B = BatchChains(ch, seed=15)
+    out = np.zeros((3, B.natoms))
+    B.run_host(None, 0, out)
+    rb0, _ = B.counters()
+    _, e = B.run_host(out.copy(), 0, out)          # unchanged coordinates: the lists stay valid
+    rb1, _ = B.counters()
+    assert rb1 == rb0
+    ef = B.energy_fp64()
+    assert np.all(np.abs(e - ef) <= 1e-6 * _scale(B, ef))
+    xin = out.copy()
+    idx = ch[0].natom + np.arange(300)             # 100 molecules of chain 1, 2.6 A (half skin: 1 A)
+    xin[:, idx] += 1.5
+    _, e = B.run_host(xin, 0, out)
+    rb2, _ = B.counters()
+    assert rb2 == rb1 + 1
+    rows = [set(r.tolist()) for r in B.lists(1)]
+    miss = [(r, q) for r, q in _pairs_within(B.coords(1), 3, ch[1].box[0], 12.0) if q not in rows[r] or r not in rows[q]]
+    assert not miss, miss[:5]
+    ef = B.energy_fp64()
+    assert np.all(np.abs(e - ef) <= 1e-6 * _scale(B, ef))
+
+
 def test_invalid_batches_rejected():
     w = systems.water_box(512, seed=3)
     flexible = w.copy()
