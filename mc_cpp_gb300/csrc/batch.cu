@@ -491,13 +491,15 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 const int a = res * apr + k;
                 // the first neighbour indices of the list row, loaded before the move is formed so
                 // their latency overlaps the moved residue's loads and the move arithmetic
-                constexpr int CH = 4;
+                // lanes take list entries (neighbour residues), CH per lane in flight, each with all
+                // of its atoms
+                constexpr int CH = A >= 3 ? 1 : (A == 2 ? 2 : 4);
                 const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
-                const int nitems = NL[C.res0 + res] * apr;
+                const int nent = NL[C.res0 + res];
                 int q_first[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
-                    const int e = (gw * 32 + u * GS + lane) / apr;
+                    const int e = gw * 32 + u * GS + lane;
                     q_first[u] = e < G.cap ? row[e] : 0;
                 }
                 uint4 fo = Fc[a];
@@ -604,40 +606,50 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     }
                 };
                 int head = 0, tail = 0;
-                for (int base = gw * 32; base < nitems; base += CH * GS) {
+                for (int base = gw * 32; base < nent; base += CH * GS) {
                     int q[CH];
-                    uint4 pb[CH];
+                    uint4 pb[CH][A];
 #pragma unroll
                     for (int u = 0; u < CH; u++) {
-                        const int t = base + u * GS + lane;
-                        q[u] = t < nitems ? (base == gw * 32 ? q_first[u] : (int)row[t / apr]) : -1;
+                        const int e = base + u * GS + lane;
+                        q[u] = e < nent ? (base == gw * 32 ? q_first[u] : (int)row[e]) : -1;
                     }
 #pragma unroll
-                    for (int u = 0; u < CH; u++) {
-                        const int t = base + u * GS + lane;
-                        pb[u] = q[u] >= 0 ? Fc[q[u] * apr + (t - (t / apr) * apr)] : make_uint4(0, 0, 0, 0);
-                    }
+                    for (int u = 0; u < CH; u++)
+#pragma unroll
+                        for (int b = 0; b < A; b++)
+                            pb[u][b] = (q[u] >= 0 && b < apr) ? Fc[q[u] * apr + b] : make_uint4(0, 0, 0, 0);
 #pragma unroll
                     for (int u = 0; u < CH; u++) {
-                        if (base + u * GS >= nitems) break;
-                        const int t = base + u * GS + lane;
+                        if (base + u * GS >= nent) break;
                         if (sub) {
                             for (unsigned pm = sub; pm; pm &= pm - 1) {
                                 const int h = __ffs(pm) - 1;
-                                if (q[u] == R[h].res) pb[u] = R[h].fn[t - (t / apr) * apr];
+                                if (q[u] == R[h].res) {
+#pragma unroll
+                                    for (int b = 0; b < A; b++)
+                                        if (b < apr) pb[u][b] = R[h].fn[b];
+                                }
                             }
                         }
-                        const float ex = fdelta(fo0.x, pb[u].x, Ls0, Ll0), ey = fdelta(fo0.y, pb[u].y, Ls1, Ll1),
-                                    ez = fdelta(fo0.z, pb[u].z, Ls2, Ll2);
-                        const bool keep = q[u] >= 0 && ex * ex + ey * ey + ez * ez <= G.skip2;
-                        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-                        if (keep) ring[(head + __popc(bal & lt_mask)) & (RING - 1)] = make_float4(ex, ey, ez, __uint_as_float(pb[u].w));
-                        head += __popc(bal);
-                        if (head - tail >= 32) {
-                            __syncwarp();
-                            eval(ring[(tail + lane) & (RING - 1)]);
-                            tail += 32;
-                            __syncwarp();
+                        // each atom of the entry is kept on its own distance from the moved
+                        // residue's first atom
+#pragma unroll
+                        for (int b = 0; b < A; b++) {
+                            if (b >= apr) break;
+                            const float ex = fdelta(fo0.x, pb[u][b].x, Ls0, Ll0), ey = fdelta(fo0.y, pb[u][b].y, Ls1, Ll1),
+                                        ez = fdelta(fo0.z, pb[u][b].z, Ls2, Ll2);
+                            const bool keep = q[u] >= 0 && ex * ex + ey * ey + ez * ez <= G.skip2;
+                            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                            if (keep)
+                                ring[(head + __popc(bal & lt_mask)) & (RING - 1)] = make_float4(ex, ey, ez, __uint_as_float(pb[u][b].w));
+                            head += __popc(bal);
+                            if (head - tail >= 32) {
+                                __syncwarp();
+                                eval(ring[(tail + lane) & (RING - 1)]);
+                                tail += 32;
+                                __syncwarp();
+                            }
                         }
                     }
                 }
