@@ -333,27 +333,31 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
 // per row i, lanes over its j > i entries.  One 16-byte load per list entry (the fixed-point
 // position: exact minimum-image displacement by 32-bit wrap-around, scaled by a float-float box
 // length) and one 16-byte load per pair inside the cutoff (charge as float-float, eps, sig).
-// Coulomb is summed per lane as a float-float pair (TwoSum), LJ in FP32 per row and FP64 across
-// rows; the block sums in FP64.  Same terms as mixed_pair (unscaled, k_finalize scales).
+// The row's sums are factored: each lane sums q_j g (g = S(r^2)/r, float-float by TwoSum) and
+// eps_j l S (l = x^12 - x^6, FP32) over its entries of row i, and at the row's end multiplies them
+// by q_i (float-float) and eps_i into float-float totals; no FP64 arithmetic until the block sum.
+// The switch is formed unscaled as A^2 B with A = rc^2 - u, B = 2u + rc^2 - 3 ron^2 and u = r^2
+// raised to ron^2; inv_f1 = 1 / (that FP32 polynomial at ron^2) scales the block sums, so inner
+// pairs have S = 1 exactly.  Same terms as mixed_pair (unscaled, k_finalize scales).
 // U list entries in flight per lane; MINB resident CTAs per SM requested from the register
 // allocator (occupancy against registers); the engine times the variants once and keeps the fastest.
 template <int U, int MINB>
 __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint4* __restrict__ fx, const float4* __restrict__ prm,
                                                                       int n, float Ls0, float Ls1, float Ls2, float Ll0,
-                                                                      float Ll1, float Ll2, CutDev cut, const int* __restrict__ nbr,
+                                                                      float Ll1, float Ll2, CutDev cut, double inv_f1,
+                                                                      const int* __restrict__ nbr,
                                                                       const int* __restrict__ nup, int cap, double* part) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const float c2 = cut.c2f, n2 = cut.n2f, sw2 = cut.sw2f, k3 = c2 - 3.0f * n2;
-    float eh = 0.0f, elo = 0.0f;   // Coulomb of this lane, float-float
-    double svd = 0.0;
+    const float c2 = cut.c2f, n2 = cut.n2f, k3 = c2 - 3.0f * n2;
+    float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;   // this lane's totals, float-float
     for (int i = warp; i < n; i += nwarps) {
         const uint4 fi = fx[i];
-        const float4 pi = prm[i];
+        const float4 pi = prm[i];        // (q hi, q lo, eps, sig)
         const int* row = nbr + (size_t)i * cap;
         const int m = nup[i];
-        float vrow = 0.0f;
+        float ch = 0.0f, cl = 0.0f, vs = 0.0f;
         for (int k0 = 0; k0 < m; k0 += 32 * U) {
             int j[U];
             uint4 fj[U];
@@ -376,28 +380,34 @@ __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (r2[u] <= c2) {
-                    const float qh = pi.x * pj[u].x;
-                    const float ql = fmaf(pi.x, pj[u].x, -qh) + fmaf(pi.x, pj[u].y, pi.y * pj[u].x);
                     float rinv = rsqrtf(r2[u]);
                     rinv = rinv * fmaf(-0.5f * r2[u] * rinv, rinv, 1.5f);   // one Newton step
-                    const float ri2 = rinv * rinv;
-                    const float sg = pi.w + pj[u].w;
-                    const float x2 = sg * sg * ri2;
-                    const float x6 = x2 * x2 * x2;
-                    const float a = c2 - r2[u];
-                    const float f = r2[u] > n2 ? a * a * fmaf(2.0f, r2[u], k3) * sw2 : 1.0f;
-                    const float e = fmaf(qh, rinv, ql * rinv) * f;
-                    vrow = fmaf(pi.z * pj[u].z * fmaf(x6, x6, -x6), f, vrow);
+                    const float uu = fmaxf(r2[u], n2);
+                    const float a = c2 - uu;
+                    const float f = a * a * fmaf(2.0f, uu, k3);
+                    const float g = rinv * f;
                     float sm, er;
-                    two_sum(eh, e, sm, er);
-                    eh = sm;
-                    elo += er;
+                    two_sum(ch, pj[u].x * g, sm, er);
+                    ch = sm;
+                    cl = fmaf(pj[u].y, g, cl + er);
+                    const float y = (pi.w + pj[u].w) * rinv;
+                    const float x2 = y * y;
+                    const float x6 = x2 * x2 * x2;
+                    vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
                 }
             }
         }
-        svd += (double)vrow;
+        // the lane's share of row i: q_i (ch + cl) and eps_i vs, into the float-float totals
+        float ph, pl, sm, er;
+        ff_mul(pi.x, pi.y, ch, cl, ph, pl);
+        two_sum(EH, ph, sm, er);
+        EH = sm;
+        EL += er + pl;
+        two_sum(VH, pi.z * vs, sm, er);
+        VH = sm;
+        VL += er;
     }
-    block_reduce2((double)eh + (double)elo, svd, part + 2 * blockIdx.x);
+    block_reduce2(((double)EH + (double)EL) * inv_f1, ((double)VH + (double)VL) * inv_f1, part + 2 * blockIdx.x);
 }
 
 // Full energy: all pairs j > i not in the full-mode exclusion row of i, no cutoff.  Triangular
@@ -963,16 +973,17 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
         return clp.launch_energy(stream, v - kListVariants, d_fx, d_prmf, cluster_geom(), nbp);
     }
     AtomsDev A = atoms();
+    const double inv_f1 = cluster_geom().inv_f1;
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
     case 0: k_energy_list_mix<4, 4><<<152 * 4, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
     case 1: k_energy_list_mix<4, 6><<<152 * 6, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
     case 2: k_energy_list_mix<2, 8><<<152 * 8, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
     default: k_energy_list_mix<8, 3><<<152 * 3, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                        A.Lsl[1], A.Lsl[2], cut, d_nbr, d_nup, cap, nbp); break;
+                                                                        A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
     }
     static const int kBlocks[kListVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
     return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
