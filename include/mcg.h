@@ -185,6 +185,16 @@ typedef struct mcg_batch_opts {
     int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4, 8 */
     int clusters;             /* 0 = automatic (on with 512-thread CTAs): the largest chains each run on a
                                  cluster of two CTAs (two SMs); -1 = off */
+    /* dmax adjustment per move type (index 0 = TRN, 1 = ROT), as MC_metropolis::run does it
+     * (src/MC_metropolis.cpp:136-146, MC::adjust_dmax src/MC.cpp:165-173): after every
+     * dmax_each[t]-th move of a chain (0 = never), dmax[t] is multiplied by 1.1 when the moves of
+     * type t accepted since the last adjustment, divided by dmax_each[t], exceed dmax_target[t]
+     * percent, else by 0.9.  Adjusted values are capped at dmax_max[t] (0 = twice the initial
+     * value when adjusted, the initial value otherwise): the sweep sizes its neighbour radii for
+     * the largest move, so the cap is part of the geometry. */
+    int dmax_each[2];
+    double dmax_target[2];
+    double dmax_max[2];
 } mcg_batch_opts;
 
 /* chains[c] describes chain c (as for mcg_create; precision, cut_mode must be switch). */
@@ -194,6 +204,8 @@ int mcg_batch_destroy(mcg_batch* b);
 int mcg_batch_sweep(mcg_batch* b, int nsweeps);
 /* Same, host-synchronous, returning per-chain totals: trials, accepted, running E (iu). */
 int mcg_batch_stats(mcg_batch* b, int64_t* trials, int64_t* accepted, double* etot);
+/* Current dmax of every chain: translation (Angstrom) and rotation (degrees), nchains each. */
+int mcg_batch_get_dmax(mcg_batch* b, double* dmax_trn, double* dmax_rot);
 /* Fresh FP64 recompute of every chain's nonbonded energy (iu) with a freshly built list. */
 int mcg_batch_energy_fp64(mcg_batch* b, double* e);
 int mcg_batch_get_coords(mcg_batch* b, int chain, double* x, double* y, double* z);

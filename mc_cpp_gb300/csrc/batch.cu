@@ -98,6 +98,9 @@ struct ChainDev {
     float beta_f;         // beta rounded to FP32 (clear-margin Metropolis decisions)
     float dmax_trn, dmax_rot;
     int ntypes_move;      // 1: TRN only, 2: TRN + ROT
+    int each[2];          // dmax adjustment period per move type (0 = fixed), MC::adjust_dmax
+    double target[2];     // target acceptance per move type, fraction
+    double dmax_cap[2];   // largest adjusted dmax per move type
     uint32_t key0, key1;
     float tab[MAX_APR][MAX_APR][4];   // (qk, e4, ss, qk_lo) per slot pair; qk + qk_lo = K q_a q_b
     float tablo[MAX_APR][MAX_APR][2]; // (e4_lo, ss_lo): float-float parts for total-energy kernels
@@ -112,6 +115,8 @@ struct ChainState {
     int err;
     float maxd2;                // largest squared displacement of a committed atom since the last build
     int pad_;
+    double dmax[2];             // current dmax: translation (A), rotation (degrees)
+    int acc_tmp[2];             // accepted moves per type since the last dmax adjustment
 };
 
 struct BatchGeom {
@@ -373,6 +378,7 @@ struct MoveRec {
     uint4 fb[MAX_APR];                   // build positions of the moved atoms
     uint4 fo0;                           // old position of the first atom
     int res;
+    int rot;                             // move type: 0 translation, 1 rotation
     float lna;                           // -ln(alpha), FP32 estimate (NaN: decide in FP64)
     uint32_t ahi, alo;                   // Philox words of alpha in (0, 1] (u01d_open0)
 };
@@ -472,9 +478,18 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         ulonglong4_32a* Mc = M + C.atom0;
         int mv = 0, buf = 0;
         unsigned prev_acc = 0;                 // accepted moves of the previous iteration (records P[buf ^ 1])
+        // moves left before the next dmax adjustment of each type (0: the type is never adjusted)
+        const bool adjust = C.each[0] > 0 || C.each[1] > 0;
+        int to_adj[2];
+#pragma unroll
+        for (int t = 0; t < 2; t++) to_adj[t] = C.each[t] > 0 ? C.each[t] - (int)(S.moves % (unsigned long long)C.each[t]) : 0;
         float eh = 0.0f, el = 0.0f;            // accepted dE of this sweep (float-float, warp 0 lane 0)
         while (mv < nmoves) {
-            const int kk = min(K, nmoves - mv);
+            int kk = min(K, nmoves - mv);
+            if (adjust) {   // an iteration ends at the move after which dmax is adjusted
+#pragma unroll
+                for (int t = 0; t < 2; t++) if (to_adj[t] > 0) kk = min(kk, to_adj[t]);
+            }
             const bool gact = grp < kk;
             MoveRec* R = P[buf ^ 1];
             float acc = 0.0f;
@@ -529,7 +544,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 const float ux = st * cphi, uy = st * sphi, uz = ct;
                 float dx, dy, dz;
                 if (!rot) {
-                    const float rad = C.dmax_trn * cbrtf(u01f(q1.y));
+                    const float rad = (float)S.dmax[0] * cbrtf(u01f(q1.y));
                     dx = rad * ux; dy = rad * uy; dz = rad * uz;
                 } else {
                     // unit quaternion for an angle uniform in [-dmax, dmax] degrees about u;
@@ -537,7 +552,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     const uint32_t px = __shfl_sync(0xffffffffu, fo.x, piv), py = __shfl_sync(0xffffffffu, fo.y, piv),
                                    pz = __shfl_sync(0xffffffffu, fo.z, piv);
                     float sh, ch;
-                    sincospif(C.dmax_rot * (2.0f * u01f(q1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
+                    sincospif((float)S.dmax[1] * (2.0f * u01f(q1.y) - 1.0f) * (1.0f / 360.0f), &sh, &ch);
                     const float qw = ch, qx = sh * ux, qy = sh * uy, qz = sh * uz;
                     const float ox = fdelta(px, fo.x, Ls0, Ll0), oy = fdelta(py, fo.y, Ls1, Ll1),
                                 oz = fdelta(pz, fo.z, Ls2, Ll2);
@@ -569,6 +584,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                         if (lane == 0) {
                             Q.fo0 = fo0;
                             Q.res = res;
+                            Q.rot = rot ? 1 : 0;
                             Q.ahi = q1.z;
                             Q.alo = q1.w;
                             Q.lna = lna;
@@ -747,6 +763,20 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 Fc[a] = Q[grp].fn[lane];
             }
             if (grp < ng) npairs += np;
+            if (adjust) {   // dmax adjustment after the standing moves, in move order (every thread alike)
+                for (int g = 0; g < ng; g++) {
+                    if ((accmask >> g) & 1u) S.acc_tmp[Q[g].rot]++;
+#pragma unroll
+                    for (int t = 0; t < 2; t++) {
+                        if (to_adj[t] > 0 && --to_adj[t] == 0) {
+                            const double ratio = (double)S.acc_tmp[t] / (double)C.each[t];
+                            S.dmax[t] = fmin(C.dmax_cap[t], S.dmax[t] * (ratio > C.target[t] ? 1.10 : 0.9));
+                            S.acc_tmp[t] = 0;
+                            to_adj[t] = C.each[t];
+                        }
+                    }
+                }
+            }
             if (warp == 0) {   // statistics and the sweep's energy change, in move order
                 for (int g = 0; g < ng; g++) {
                     const float dh = __shfl_sync(0xffffffffu, deh, g), dl = __shfl_sync(0xffffffffu, del, g);
@@ -1320,6 +1350,20 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     *out = nullptr;
     if (!descs || nchains <= 0 || !opts) return fail(MCG_EINVAL, "need chains and options");
     if (!(opts->dmax_trn >= 0) || !(opts->dmax_rot >= 0)) return fail(MCG_EINVAL, "dmax values must be >= 0");
+    // dmax adjustment: periods, targets and the caps the sweep's geometry is sized for
+    double dmax_cap[2];
+    {
+        const double init[2] = {opts->dmax_trn, opts->dmax_rot};
+        for (int t = 0; t < 2; t++) {
+            if (opts->dmax_each[t] < 0) return fail(MCG_EINVAL, "dmax_each must be >= 0");
+            if (!(opts->dmax_target[t] >= 0.0 && opts->dmax_target[t] <= 100.0))
+                return fail(MCG_EINVAL, "dmax_target must be a percentage in [0, 100]");
+            if (!(opts->dmax_max[t] >= 0.0)) return fail(MCG_EINVAL, "dmax_max must be >= 0");
+            dmax_cap[t] = opts->dmax_max[t] > 0.0 ? opts->dmax_max[t] : (opts->dmax_each[t] > 0 ? 2.0 * init[t] : init[t]);
+            if (dmax_cap[t] < init[t]) return fail(MCG_EINVAL, "dmax_max is below the initial dmax");
+        }
+        if (dmax_cap[1] > 180.0) return fail(MCG_EINVAL, "the rotation dmax cap exceeds 180 degrees");
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) { cudaGetLastError(); return fail(MCG_ECUDA, "no CUDA device available"); }
     std::unique_ptr<mcg_batch> B(new mcg_batch);
@@ -1378,6 +1422,11 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         C.beta_f = (float)C.beta;
         C.dmax_trn = (float)opts->dmax_trn;
         C.dmax_rot = (float)opts->dmax_rot;
+        for (int t = 0; t < 2; t++) {
+            C.each[t] = opts->dmax_each[t];
+            C.target[t] = opts->dmax_target[t] / 100.0;
+            C.dmax_cap[t] = dmax_cap[t];
+        }
         C.ntypes_move = apr > 1 ? 2 : 1;
         uint64_t key = (opts->seed + 1) * 0x9E3779B97F4A7C15ull ^ ((uint64_t)c * 0xD1B54A32D192ED03ull);
         C.key0 = (uint32_t)key; C.key1 = (uint32_t)(key >> 32);
@@ -1430,7 +1479,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     // dE forms the new displacement as d_old - m; that is the minimum image for every pair inside
     // the cutoff only while rc + |m| <= L/2 (m: the largest move of one atom)
     const double span = span_max + 0.01;   // rigid residues keep their intra-residue distances
-    const double mmax = std::max((double)opts->dmax_trn, 2.0 * span * std::sin(0.5 * opts->dmax_rot * PI / 180.0)) + 1e-6;
+    const double mmax = std::max(dmax_cap[0], 2.0 * span * std::sin(0.5 * dmax_cap[1] * PI / 180.0)) + 1e-6;
     G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
     const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
     G.indep2 = (float)(rind * rind);
@@ -1502,6 +1551,10 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         }
         mix((uint64_t)llround(rc * 1000)); mix((uint64_t)llround(skin * 1000));
         mix((uint64_t)llround(opts->dmax_trn * 1e4)); mix((uint64_t)llround(opts->dmax_rot * 1e4));
+        for (int t = 0; t < 2; t++) {
+            mix((uint64_t)opts->dmax_each[t]); mix((uint64_t)llround(opts->dmax_target[t] * 1e4));
+            mix((uint64_t)llround(dmax_cap[t] * 1e4));
+        }
         cudaDeviceProp prop;
         std::string name = cudaGetDeviceProperties(&prop, dev) == cudaSuccess ? prop.name : "unknown";
         for (char& ch : name) if (ch == ' ') ch = '_';
@@ -1569,6 +1622,8 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     for (int c = 0; c < nchains; c++) {
         if (st[c].err) return fail(st[c].err, "neighbour list capacity exceeded (chain " + std::to_string(c) + ")");
         st[c].etot = e[c];
+        st[c].dmax[0] = opts->dmax_trn;
+        st[c].dmax[1] = opts->dmax_rot;
     }
     BK(cudaMemcpyAsync(B->d_state, st.data(), sizeof(ChainState) * nchains, cudaMemcpyHostToDevice, B->stream));
     BK(cudaStreamSynchronize(B->stream));
@@ -1767,6 +1822,15 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
         BK(cudaMemcpyAsync(xyz_out, b->d_xyz, bytes, cudaMemcpyDeviceToHost, b->stream));
     }
     return mcg_batch_stats(b, nullptr, accepted, etot);
+}
+
+int mcg_batch_get_dmax(mcg_batch* b, double* dmax_trn, double* dmax_rot) {
+    if (!b || !dmax_trn || !dmax_rot) return fail(MCG_EINVAL, "null argument");
+    std::vector<ChainState> st(b->nchains);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < b->nchains; c++) { dmax_trn[c] = st[c].dmax[0]; dmax_rot[c] = st[c].dmax[1]; }
+    return MCG_OK;
 }
 
 int mcg_batch_energy_mixed(mcg_batch* b, double* e) {

@@ -177,7 +177,8 @@ class BatchChains:
 
     def __init__(self, chains, dmax_trn: float = 0.15, dmax_rot: float = 15.0, acceptance: str = "physical",
                  seed: int = 1, threads_per_chain: int = 0, list_capacity: int = 0, ctas_per_sm: int = 0,
-                 speculation: int = 0, clusters: int = 0):
+                 speculation: int = 0, clusters: int = 0, dmax_each=(0, 0), dmax_target=(50.0, 50.0),
+                 dmax_max=(0.0, 0.0)):
         L = native.lib()
         self.nchains = len(chains)
         arr = (native.SystemDesc * self.nchains)()
@@ -187,7 +188,8 @@ class BatchChains:
             arr[k] = d
             self._keep.append(keep)
         opts = native.BatchOpts(dmax_trn, dmax_rot, native.ACCEPT[acceptance], threads_per_chain, list_capacity, seed,
-                                ctas_per_sm, speculation, clusters)
+                                ctas_per_sm, speculation, clusters, (C.c_int * 2)(*dmax_each),
+                                (C.c_double * 2)(*dmax_target), (C.c_double * 2)(*dmax_max))
         h = C.c_void_p()
         native.check(L.mcg_batch_create(arr, self.nchains, C.byref(opts), C.byref(h)))
         self.h = h
@@ -293,6 +295,13 @@ class BatchChains:
                                                      native.pd(xyz_out) if xyz_out is not None else None,
                                                      a.ctypes.data_as(native._i64), native.pd(e)))
         return a, e
+
+    def dmax(self):
+        """Current (translation A, rotation degrees) dmax of every chain."""
+        t = np.zeros(self.nchains)
+        r = np.zeros(self.nchains)
+        native.check(native.lib().mcg_batch_get_dmax(self.h, native.pd(t), native.pd(r)))
+        return t, r
 
     def counters(self):
         rb = C.c_int64(0)

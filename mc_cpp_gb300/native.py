@@ -59,7 +59,8 @@ class SystemDesc(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("dmax_trn", C.c_double), ("dmax_rot", C.c_double), ("acceptance_units", C.c_int),
                 ("threads_per_chain", C.c_int), ("list_capacity", C.c_int), ("seed", C.c_uint64),
-                ("ctas_per_sm", C.c_int), ("speculation", C.c_int), ("clusters", C.c_int)]
+                ("ctas_per_sm", C.c_int), ("speculation", C.c_int), ("clusters", C.c_int),
+                ("dmax_each", C.c_int * 2), ("dmax_target", C.c_double * 2), ("dmax_max", C.c_double * 2)]
 
 
 class BatchTuning(C.Structure):
@@ -123,6 +124,7 @@ def lib():
         "mcg_batch_energy_mixed": (C.c_int, [P, _d]),
         "mcg_batch_pairs": (C.c_int, [P, _i64]),
         "mcg_batch_update_lists": (C.c_int, [P]),
+        "mcg_batch_get_dmax": (C.c_int, [P, _d, _d]),
         "mcg_batch_get_lists": (C.c_int, [P, C.c_int, _i, _i, C.c_int64, _i64]),
         "mcg_pair_count": (C.c_int, [P, _i64, _i64]),
         "mcg_time_nonbonded": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),

@@ -247,6 +247,52 @@ def test_speculative_sweep_reproduces_sequential_chain(speculation, clusters):
     assert (np.abs(e2 - ef) / np.abs(ef)).max() <= 1e-6
 
 
+def test_dmax_adjustment_follows_the_reference_rule():
+    """MC::adjust_dmax (MC.cpp:165-173) after every dmax_each-th move of a chain, per move type.
+    With a 100% target no window exceeds it, so every adjustment multiplies dmax by 0.9: after n
+    moves, dmax = dmax0 * 0.9^floor(n / each), across sweep boundaries.  With a 0% target a window
+    that accepted a move of the type grows dmax by 1.1, never past the cap."""
+    ch = _waters((600, 900), seed=41)
+    B = BatchChains(ch, seed=5, dmax_each=(10, 14), dmax_target=(100.0, 100.0))
+    B.sweep(2)
+    t, r = B.dmax()
+    n = np.array([600, 900]) * 2
+    assert np.allclose(t, 0.15 * 0.9 ** (n // 10), rtol=1e-12, atol=0), t
+    assert np.allclose(r, 15.0 * 0.9 ** (n // 14), rtol=1e-12, atol=0), r
+    _, _, etot = B.stats()
+    e = B.energy_fp64()
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+    G = BatchChains(ch, seed=5, dmax_each=(10, 10), dmax_target=(0.0, 0.0), dmax_max=(0.2, 20.0))
+    G.sweep(1)
+    t, r = G.dmax()
+    assert np.all(t <= 0.2) and np.all(r <= 20.0)
+    assert np.all(t > 0.15) and np.all(r > 15.0)
+    with pytest.raises(native.McgError):
+        BatchChains(ch, dmax_each=(10, 0), dmax_max=(0.1, 0.0))      # cap below the initial dmax
+
+
+@pytest.mark.parametrize("speculation", [4, 8])
+def test_speculative_sweep_with_dmax_adjustment_is_sequential(speculation):
+    """Iterations end at the move after which dmax is adjusted, so moves evaluated together share
+    one dmax and the chain equals the sequential one, dmax included."""
+    ch = _waters((2600, 1500), seed=43)
+    kw = dict(seed=23, clusters=-1, dmax_each=(7, 11), dmax_target=(25.0, 15.0))
+    seq = BatchChains(ch, speculation=1, **kw)
+    spec = BatchChains(ch, speculation=speculation, **kw)
+    seq.sweep(2)
+    spec.sweep(2)
+    t1, a1, _ = seq.stats()
+    t2, a2, _ = spec.stats()
+    assert np.array_equal(t1, t2)
+    same = [np.array_equal(seq.coords(k), spec.coords(k)) for k in range(len(ch))]
+    assert sum(same) >= len(ch) - 1, same
+    d1, d2 = seq.dmax(), spec.dmax()
+    for k in range(len(ch)):
+        if same[k]:
+            assert d1[0][k] == d2[0][k] and d1[1][k] == d2[1][k]
+    assert not np.allclose(d1[0], 0.15)          # adjusted
+
+
 def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch):
     monkeypatch.setenv("MCG_TUNE_CACHE", str(tmp_path / "tune.txt"))
     ch = _waters((512, 1500, 3000), seed=41)
