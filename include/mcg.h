@@ -165,6 +165,12 @@ int mcg_build_exclusions(const mcg_system_desc* desc, int* counts, int* entries,
 int mcg_add_move(mcg_system* s, int type, int mode, const int* sele, double dmax, double target, int each);
 int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
                        const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties);
+/* The same run with MC_metropolis::run's outputs (src/MC_metropolis.cpp:156-162, MC::write_traj
+ * src/MC.cpp:93-108): after every save_each-th step (save_each > 0) the coordinates go to frames
+ * (natom (x, y, z) triples per frame; frame k holds step (k + 1) * save_each) and the running total
+ * energy (iu) to energies[k]; both hold nsteps / save_each entries. */
+int mcg_metropolis_run_saving(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, int save_each,
+                              double* frames, double* energies, double* final_etot, int64_t* n_accepted);
 
 /* --- batched independent chains ----------------------------------------------------------------
  * Hundreds of NVT chains of rigid molecules (each chain: identical residues of 1..8 atoms, all

@@ -212,8 +212,13 @@ int mcg_add_move(mcg_system* s, int type, int mode, const int* sele, double dmax
 // only when dE > DBL_EPSILON.  Moves follow Move.hpp: translate then re-wrap each atom; rotate
 // the raw coordinates about the pivot atom (or the centre of mass) by a Rodrigues matrix
 // built from the normalised axis and an angle in degrees, then re-wrap each atom.
-int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
-                       const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties) {
+}  // extern "C"
+
+// MC_metropolis::run (MC_metropolis.cpp:62-165) on this engine; with save_each > 0 the coordinates
+// and the running total after every save_each-th step go to frames / energies (MC.cpp:93-108).
+static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
+                           const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties,
+                           int save_each, double* frames, double* energies) {
     if (!s) return fail(MCG_EINVAL, "null handle");
     if (s->moves.empty()) return fail(MCG_EINVAL, "no move types registered");  // MC.cpp:185-189
     if (nsteps < 0) return fail(MCG_EINVAL, "nsteps must be >= 0");
@@ -341,11 +346,33 @@ int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_
             rec[9] = de; rec[10] = alpha; rec[11] = accepted ? 1.0 : 0.0;
             std::memcpy(trace + 12 * (size_t)(st - 1), rec, sizeof rec);
         }
+        if (save_each > 0 && st % save_each == 0) {   // MC_metropolis.cpp:156-162
+            const size_t k = (size_t)(st / save_each - 1);
+            double* f = frames + k * 3 * (size_t)h.n;
+            for (int a = 0; a < h.n; a++) { f[3 * a] = X[a]; f[3 * a + 1] = Y[a]; f[3 * a + 2] = Z[a]; }
+            energies[k] = etot;
+        }
     }
     if (final_etot) *final_etot = etot;
     if (n_accepted) *n_accepted = acc;
     if (n_ties) *n_ties = ties;
     return MCG_OK;
+}
+
+extern "C" {
+
+int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
+                       const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties) {
+    return metropolis_impl(s, nsteps, seed, acceptance_units, trace, follow, final_etot, n_accepted, n_ties, 0,
+                           nullptr, nullptr);
+}
+
+int mcg_metropolis_run_saving(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, int save_each,
+                              double* frames, double* energies, double* final_etot, int64_t* n_accepted) {
+    if (save_each < 0) return fail(MCG_EINVAL, "save_each must be >= 0");
+    if (save_each > 0 && nsteps >= save_each && (!frames || !energies)) return fail(MCG_EINVAL, "null frame or energy buffer");
+    return metropolis_impl(s, nsteps, seed, acceptance_units, nullptr, nullptr, final_etot, n_accepted, nullptr,
+                           save_each, frames, energies);
 }
 
 }  // extern "C"

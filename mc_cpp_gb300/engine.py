@@ -172,6 +172,20 @@ class FFieldCUDA:
         return tr[:nsteps], fe.value, na.value, nt.value
 
 
+    def metropolis_saving(self, nsteps: int, seed: int, save_each: int, acceptance: str = "reference"):
+        """MC_metropolis::run with its outputs: (frames[nsave, natom, 3], energies[nsave] (iu),
+        final_etot, n_accepted), one frame and energy after every save_each-th step."""
+        nsave = nsteps // save_each if save_each > 0 else 0
+        frames = np.zeros((max(1, nsave), self.n, 3))
+        energies = np.zeros(max(1, nsave))
+        fe = C.c_double(0)
+        na = C.c_int64(0)
+        native.check(native.lib().mcg_metropolis_run_saving(self.h, nsteps, seed, native.ACCEPT[acceptance], save_each,
+                                                            native.pd(frames), native.pd(energies), C.byref(fe),
+                                                            C.byref(na)))
+        return frames[:nsave], energies[:nsave], fe.value, na.value
+
+
 class BatchChains:
     """Hundreds of independent NVT chains advanced by one persistent kernel per sweep."""
 

@@ -91,6 +91,7 @@ class System:
     moves: List[MoveSpec] = dataclasses.field(default_factory=list)
     nsteps: int = 0
     seed: int = 0
+    save_each: int = 0         # <mc save_each>: steps between tr.xyz frames / ener.dat lines (0: none)
 
     def coords(self) -> np.ndarray:
         return np.stack([self.x, self.y, self.z], axis=1)
@@ -232,7 +233,7 @@ def read_xml(path: str) -> System:
     root = ET.parse(path).getroot()
     base = os.path.dirname(os.path.abspath(path))
     kw = dict(pbc_type="none", box=(0.0, 0.0, 0.0), cut_mode="full", cutoff=12.0, cuton=10.0, dcut=2.0,
-              temp=0.0, moves=[], nsteps=10000, seed=0)
+              temp=0.0, moves=[], nsteps=10000, seed=0, save_each=0)
     natom = 0
     ffile = cor = None
     for node in root:
@@ -264,6 +265,7 @@ def read_xml(path: str) -> System:
         elif node.tag == "mc":
             kw["nsteps"] = int(node.attrib.get("nsteps", 10000))
             kw["seed"] = int(node.attrib.get("seed", 0))
+            kw["save_each"] = int(node.attrib.get("save_each", 0))
     c = read_cor(os.path.join(base, cor))
     if c["natom"] != natom:
         raise ValueError("atom count of the .cor differs from the XML")
@@ -321,8 +323,9 @@ def write_forfield(s: System, path: str) -> None:
         f.write("end\n")
 
 
-def write_xml(s: System, path: str, cor_name: str, ff_name: str, nsteps: int = 0, seed: int = 1) -> None:
-    """An input the reference's Parser_XML reads (save_each="0": no trajectory files)."""
+def write_xml(s: System, path: str, cor_name: str, ff_name: str, nsteps: int = 0, seed: int = 1,
+              save_each: int = 0) -> None:
+    """An input the reference's Parser_XML reads (save_each = 0: no trajectory files)."""
     a, b, c = s.box
     mv = "".join('    <move move_type="%s" move_mode="%s" sel_mode="%s" sele="%s" dmax_value="%r" '
                  'dmax_each="%d" dmax_target="%r" />\n' % (m.move_type, m.move_mode, m.sel_mode, m.sele,
@@ -340,7 +343,7 @@ def write_xml(s: System, path: str, cor_name: str, ff_name: str, nsteps: int = 0
             f.write('  <forcefield ff_type="mdbas" ff_file="%s" cut_type="full" />\n' % ff_name)
         f.write('  <atomlist list_mode="file" file_type="cor" cor_path="%s" />\n' % cor_name)
         f.write("  <movelist>\n%s  </movelist>\n" % mv)
-        f.write('  <mc nsteps="%d" save_each="0" seed="%d"/>\n</inputFile>\n' % (nsteps, seed))
+        f.write('  <mc nsteps="%d" save_each="%d" seed="%d"/>\n</inputFile>\n' % (nsteps, save_each, seed))
 
 
 # ---------------------------------------------------------------- compact fixtures

@@ -106,6 +106,7 @@ def lib():
         "mcg_build_exclusions": (C.c_int, [C.POINTER(SystemDesc), _i, _i, C.c_int64, _i64, _i, C.c_int, _i]),
         "mcg_add_move": (C.c_int, [P, C.c_int, C.c_int, _i, C.c_double, C.c_double, C.c_int]),
         "mcg_metropolis_run": (C.c_int, [P, C.c_int, C.c_uint64, C.c_int, _d, _i, _d, _i64, _i64]),
+        "mcg_metropolis_run_saving": (C.c_int, [P, C.c_int, C.c_uint64, C.c_int, C.c_int, _d, _d, _d, _i64]),
         "mcg_batch_create": (C.c_int, [C.POINTER(SystemDesc), C.c_int, C.POINTER(BatchOpts), C.POINTER(P)]),
         "mcg_batch_destroy": (C.c_int, [P]),
         "mcg_batch_sweep": (C.c_int, [P, C.c_int]),
