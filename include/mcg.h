@@ -140,9 +140,11 @@ int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);
  * the number of variants. */
 int mcg_set_pair_kernel(mcg_system* s, int variant);
 int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count);
-/* Cluster form of the current Verlet list (mixed periodic switch systems; zeros otherwise):
- * clusters of 8 atoms, cluster pairs in the list, and the Verlet pairs their masks encode (equal
- * to the half-list size when the cluster list is complete). */
+/* Cluster form of the current Verlet list (mixed periodic switch systems; zeros otherwise), built
+ * on demand from the list in place: clusters of 8 atoms, cluster pairs in the list, and the
+ * Verlet pairs their masks encode (equal to the half-list size when the cluster list is
+ * complete).  The engine builds it only for its first energy (to time the cluster kernels) and
+ * while a cluster kernel is in use. */
 int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
 /* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
  * exclList[i]) and the 1-4 pair list (getNeighList14). */

@@ -156,11 +156,7 @@ int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count) {
 
 int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs) {
     if (!s || !clusters || !cluster_pairs || !mask_pairs) return fail(MCG_EINVAL, "null argument");
-    const ClusterPairs& c = s->eng.clp;
-    *clusters = c.ok ? c.ncl : 0;
-    *cluster_pairs = c.ok ? c.npairs : 0;
-    *mask_pairs = c.ok ? c.nbits : 0;
-    return MCG_OK;
+    return s->eng.cluster_stats(clusters, cluster_pairs, mask_pairs);
 }
 
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {

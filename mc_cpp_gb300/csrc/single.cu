@@ -955,10 +955,9 @@ int SingleEngine::launch_nonbonded(double* nbp) {
     AtomsDev A = atoms();
     if (hs.prec == MCG_PREC_FP64)
         k_energy_list<PREC_F64><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
-    else if (pbc.type != 0) {
-        if (pair_variant < 0) tune_pair_kernel();
-        return launch_pair_variant(pair_variant, nbp);
-    } else
+    else if (pbc.type != 0)
+        return launch_pair_variant(pair_variant < 0 ? 0 : pair_variant, nbp);
+    else
         k_energy_list<PREC_MIX><<<NB_BLOCKS, NB_THREADS, 0, stream>>>(A, n, pbc, cut, d_nbr, d_nup, cap, nbp);
     return NB_BLOCKS;
 }
@@ -1014,11 +1013,59 @@ void SingleEngine::tune_pair_kernel() {
 
 int SingleEngine::set_pair_kernel(int v) {
     if (v < -1 || v >= pair_kernel_count()) return fail(MCG_EINVAL, "pair-kernel variant out of range");
-    if (v >= kListVariants && !clp.ok)
-        return fail(MCG_ENOTSUP, "no cluster-pair list: the cluster kernels need a periodic box, mixed precision and switch mode");
-    if (v >= 0 && (hs.prec != MCG_PREC_MIXED || pbc.type == 0 || hs.cut != MCG_CUT_SWITCH))
+    if (v >= 0 && !uses_pair_variants())
         return fail(MCG_ENOTSUP, "pair-kernel variants apply to the mixed periodic switch energy");
+    if (v >= kListVariants) {
+        int rc = ensure_clusters();
+        if (rc) return rc;
+        if (!clp.ok) return fail(MCG_ENOTSUP, "the cluster-pair list could not be built for this system");
+    }
     pair_variant = v;
+    return MCG_OK;
+}
+
+bool SingleEngine::uses_pair_variants() const {
+    return hs.prec == MCG_PREC_MIXED && pbc.type != 0 && hs.cut == MCG_CUT_SWITCH;
+}
+
+// The cluster-pair form of the current Verlet list, built on first use after a list build (the
+// tuner's first timing, a cluster variant chosen, or the statistics asked for).  A system whose
+// clusters do not fit the build's shared-memory limits keeps the per-atom list kernels only.
+int SingleEngine::ensure_clusters() {
+    if (!clp_dirty) return MCG_OK;
+    clp_dirty = false;
+    const int crc = clp.build(stream, d_fx, n, hs.L, d_nbr, d_nup, d_nlo, cap);
+    launches += clp.build_launches;
+    clp.build_launches = 0;
+    if (crc == MCG_OK) return ensure_part((size_t)2 * clp.ncl + 2 * 64 + 5 * 64 + 16);
+    if (crc == MCG_ECUDA) return crc;
+    set_error("");
+    return MCG_OK;
+}
+
+// Before a launch of the mixed periodic switch energy: the first use times every variant (the
+// cluster list built for it); a chosen cluster variant has its list brought up to date.  Runs
+// before the caller takes the partial-sum buffer, which the cluster build may grow.
+int SingleEngine::prepare_pair_kernel() {
+    if (!uses_pair_variants()) return MCG_OK;
+    int rc;
+    if (pair_variant < 0) {
+        if ((rc = ensure_clusters())) return rc;
+        tune_pair_kernel();
+    }
+    if (pair_variant >= kListVariants) {
+        if ((rc = ensure_clusters())) return rc;
+        if (!clp.ok) pair_variant = 0;
+    }
+    return MCG_OK;
+}
+
+int SingleEngine::cluster_stats(int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs) {
+    *clusters = *cluster_pairs = *mask_pairs = 0;
+    if (!uses_pair_variants()) return MCG_OK;
+    int rc = ensure_clusters();
+    if (rc) return rc;
+    if (clp.ok) { *clusters = clp.ncl; *cluster_pairs = clp.npairs; *mask_pairs = clp.nbits; }
     return MCG_OK;
 }
 
@@ -1059,6 +1106,10 @@ int SingleEngine::ensure_part(size_t count) {
 
 int SingleEngine::time_nonbonded(int reps, float* ms) {
     if (hs.cut != MCG_CUT_SWITCH) return fail(MCG_ENOTSUP, "the pair-kernel timing covers the switch mode");
+    {
+        int rc = prepare_pair_kernel();
+        if (rc) return rc;
+    }
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
@@ -1149,19 +1200,7 @@ int SingleEngine::build_list() {
         CK(cudaStreamSynchronize(stream));
         last_max_row = maxrow;
         if (maxrow <= cap) {
-            if (hs.prec == MCG_PREC_MIXED && pbc.type != 0) {
-                // the cluster-pair form of the list; without it the per-atom list kernels run
-                const int crc = clp.build(stream, d_fx, n, hs.L, d_nbr, d_nup, d_nlo, cap);
-                if (crc == MCG_ECUDA) return crc;
-                if (crc == MCG_OK) {
-                    launches += clp.build_launches;
-                    clp.build_launches = 0;
-                    if ((rc = ensure_part((size_t)2 * clp.ncl + 2 * 64 + 5 * 64 + 16))) return rc;
-                } else {
-                    set_error("");
-                    if (pair_variant >= kListVariants) pair_variant = -1;
-                }
-            }
+            clp_dirty = uses_pair_variants();   // the cluster form follows on first use
             return MCG_OK;
         }
         cudaFree(d_nbr);
@@ -1174,6 +1213,10 @@ int SingleEngine::build_list() {
 }
 
 int SingleEngine::energy(double ener[10]) {
+    if (hs.cut == MCG_CUT_SWITCH) {
+        int rc = prepare_pair_kernel();
+        if (rc) return rc;
+    }
     AtomsDev A = atoms();
     double* nbp = d_part;
     int nnb = 0;

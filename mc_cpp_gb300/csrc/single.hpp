@@ -31,6 +31,7 @@ public:
     int set_pair_kernel(int v);
     int pair_kernel() const { return pair_variant; }
     static int pair_kernel_count();
+    int cluster_stats(int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
     ClusterPairs clp;
 
     HostSystem hs;
@@ -52,6 +53,10 @@ private:
     BondedDev bonded() const;
     ClusterGeom cluster_geom() const;
     int ensure_part(size_t count);
+    bool uses_pair_variants() const;
+    int ensure_clusters();
+    int prepare_pair_kernel();
+    bool clp_dirty = false;       // the Verlet list changed since the cluster form was built
 
     cudaStream_t stream = nullptr;
     PbcDev pbc{};
