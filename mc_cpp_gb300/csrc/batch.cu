@@ -905,20 +905,42 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
         uint4 pa[A];
 #pragma unroll
         for (int k = 0; k < A; k++) pa[k] = k < apr ? Fc[r * apr + k] : make_uint4(0, 0, 0, 0);
+        // r's atoms as offsets from its first atom: an atom pair's displacement is then the exact
+        // fixed-point displacement of q's atom from r's first atom minus r's offset, brought back
+        // to the minimum image in boxes small enough to need it
+        float ro[A][3];
+#pragma unroll
+        for (int k = 0; k < A; k++) {
+            ro[k][0] = fdelta(pa[0].x, pa[k].x, Ls0, Ll0);
+            ro[k][1] = fdelta(pa[0].y, pa[k].y, Ls1, Ll1);
+            ro[k][2] = fdelta(pa[0].z, pa[k].z, Ls2, Ll2);
+        }
+        const bool wrap = C.wrap_offsets != 0;
         float eh = 0.0f, elo = 0.0f, vh = 0.0f, vlo = 0.0f;
         // residue q (>= 0) against r, by this lane
         auto eval = [&](int q) {
             uint4 pb[A];
 #pragma unroll
             for (int b = 0; b < A; b++) pb[b] = b < apr ? Fc[q * apr + b] : make_uint4(0, 0, 0, 0);
+            float d0[A][3];
+#pragma unroll
+            for (int b = 0; b < A; b++) {
+                d0[b][0] = fdelta(pa[0].x, pb[b].x, Ls0, Ll0);
+                d0[b][1] = fdelta(pa[0].y, pb[b].y, Ls1, Ll1);
+                d0[b][2] = fdelta(pa[0].z, pb[b].z, Ls2, Ll2);
+            }
 #pragma unroll
             for (int k = 0; k < A; k++) {
                 if (k >= apr) break;
 #pragma unroll
                 for (int b = 0; b < A; b++) {
                     if (b >= apr) break;
-                    const float dx = fdelta(pa[k].x, pb[b].x, Ls0, Ll0), dy = fdelta(pa[k].y, pb[b].y, Ls1, Ll1),
-                                dz = fdelta(pa[k].z, pb[b].z, Ls2, Ll2);
+                    float dx = d0[b][0] - ro[k][0], dy = d0[b][1] - ro[k][1], dz = d0[b][2] - ro[k][2];
+                    if (wrap) {
+                        dx -= (dx > C.Lhalf[0]) ? C.Lf[0] : ((dx < -C.Lhalf[0]) ? -C.Lf[0] : 0.0f);
+                        dy -= (dy > C.Lhalf[1]) ? C.Lf[1] : ((dy < -C.Lhalf[1]) ? -C.Lf[1] : 0.0f);
+                        dz -= (dz > C.Lhalf[2]) ? C.Lf[2] : ((dz < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
+                    }
                     const float u = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), c2);
                     // slot k of r against slot b of q (F.w holds the slot); float-float charge and
                     // LJ constants: per-type roundings of the products are systematic biases that
@@ -960,8 +982,20 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
         }
         if (lane < head - tail) eval(ring[(tail + lane) & (ERING - 1)]);
         __syncwarp();
-        const double v = warp_sum(((double)eh + (double)elo) + ((double)vh + (double)vlo));
-        if (lane == 0) e_res[gr] = v;
+        // float-float butterfly over the lanes (GB300's FP64 rate is 1/64 of FP32); lane 0 adds the
+        // two parts in FP64
+        float th, tl;
+        two_sum(eh, vh, th, tl);
+        tl += elo + vlo;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, th, o), ol = __shfl_xor_sync(0xffffffffu, tl, o);
+            float sm, er;
+            two_sum(th, oh, sm, er);
+            th = sm;
+            tl = tl + ol + er;
+        }
+        if (lane == 0) e_res[gr] = (double)th + (double)tl;
     }
 }
 
