@@ -216,6 +216,26 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ our arm
+def hbm_rate(traffic, ms_per_sweep):
+    """HBM bandwidth of the sweep kernels: the ncu DRAM bytes of one sweep (profiles/) over the
+    event-timed sweep time, against the measured copy bandwidth (MEASURED_PEAKS.json)."""
+    peak, src = 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                peak = float(json.load(f)["hbm_gbs"])
+            src = "measured copy bandwidth, MEASURED_PEAKS.json"
+        except (ValueError, KeyError, OSError):
+            pass
+    if not traffic or ms_per_sweep <= 0:
+        return None
+    gbs = traffic / (ms_per_sweep * 1e-3) / 1e9
+    return {"traffic_bytes_per_step": traffic, "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
+            "peak_source": src, "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of the sweep kernels, "
+                                                  "profiles/k_batch_sweep_water256.md"}
+
+
 def traffic_from_profiles():
     p = os.path.join(ROOT, "profiles", "k_batch_sweep_water256.md")
     if not os.path.exists(p):
@@ -337,6 +357,7 @@ def run_ours(args):
                          "frac": achieved / tf.value if tf.value > 0 else None, "traffic": traffic,
                          "peak_source": "FFMA-chain probe kernel measured in this run (no FP32 figure in MEASURED_PEAKS.json)",
                          "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
+            "hbm": hbm_rate(traffic, ms_sweep / args.steps),
             "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(3 * natoms * 8),
                     "d2h_bytes_per_step": int(3 * natoms * 8 + args.chains * 16)},
             "gpu_launches": int(nl1 - nl0),
