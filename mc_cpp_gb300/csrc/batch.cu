@@ -465,10 +465,13 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         const int WPG = GS >> 5;               // warps per move
         const int grp = rank * KL + tid / GS, gw = ((tid % GS) >> 5);
         const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
+        // (qk sw2, e4 sw2, ss, qk_lo): the switch normalisation folded into the pair constants
         for (int k = tid; k < MAX_APR * MAX_APR; k += NT)
-            s_tab[k / MAX_APR][k % MAX_APR] = make_float4(C.tab[k / MAX_APR][k % MAX_APR][0], C.tab[k / MAX_APR][k % MAX_APR][1],
-                                                          C.tab[k / MAX_APR][k % MAX_APR][2], C.tab[k / MAX_APR][k % MAX_APR][3]);
-        const float c2f = G.c2f, n2f = G.n2f, sw2f = G.sw2f, k3f = G.c2f - 3.0f * G.n2f;
+            s_tab[k / MAX_APR][k % MAX_APR] = make_float4(
+                (float)((double)C.tab[k / MAX_APR][k % MAX_APR][0] * (double)G.sw2f),
+                (float)((double)C.tab[k / MAX_APR][k % MAX_APR][1] * (double)G.sw2f), C.tab[k / MAX_APR][k % MAX_APR][2],
+                C.tab[k / MAX_APR][k % MAX_APR][3]);
+        const float c2f = G.c2f, n2f = G.n2f, k3f = G.c2f - 3.0f * G.n2f;
         ChainState S = state[c];
         if (tid == 0) { s_err = 0; s_pairs = 0ull; }
         __syncthreads();
@@ -618,7 +621,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                         }
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
                         acc += mixed_pair_delta_clamped(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, c2f, n2f,
-                                                        k3f, sw2f, np);
+                                                        k3f, np);
                     }
                 };
                 int head = 0, tail = 0;

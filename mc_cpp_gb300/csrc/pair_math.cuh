@@ -183,18 +183,20 @@ __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float do
     return d_lj + ((io && in) ? c_both : c_one);
 }
 
-// mixed_pair_delta for the batched sweep, with u clamped to [n2, c2] in the switch polynomial:
-// S(u) = A^2 B sw2 (A = c2 - u, B = 2u + c2 - 3 n2) is then (c2 - n2)^3 sw2 = 1 to one ulp below n2
-// and exactly 0 beyond rc, so no select is needed.  The analytic differences
+// mixed_pair_delta for the batched sweep, with u clamped to [n2, c2] in the switch polynomial.
+// The switch is used unnormalised, P(u) = A^2 B (A = c2 - u, B = 2u + c2 - 3 n2), and the caller
+// passes qk and e4 already multiplied by sw2 = 1 / (c2 - n2)^3, so S = P sw2 without a multiply per
+// pair.  P is then (c2 - n2)^3 below n2 (S = 1 to a relative 6e-8) and exactly 0 beyond rc, so no
+// select is needed.  The analytic differences
 //   1/r_n - 1/r_o = -du (r_o r_n)^2 / (r_o + r_n)
-//   S_n - S_o = sw2 du' [2 A_o^2 - (A_o + A_n) B_n]   (du' = u_n - u_o on the clamped values)
+//   P_n - P_o = du' [2 A_o^2 - (A_o + A_n) B_n]   (du' = u_n - u_o on the clamped values)
 // are exact algebra for any clamped pair, so one formula covers pairs inside, crossing and beyond
-// the cutoff (beyond: S_o = S_n = 0 and the pair contributes 0).  du' is the accurate
+// the cutoff (beyond: P_o = P_n = 0 and the pair contributes 0).  du' is the accurate
 // -m.(d_o + d_n) when both ends lie strictly inside the switch region, the clamped difference
-// otherwise.  The common factor (c2 - n2)^3 sw2 of inner pairs is a relative error <= 6e-8.
+// otherwise.
 __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, float doz, float mx, float my, float mz,
-                                                          float qk, float e4, float ss, float c2, float n2, float k3,
-                                                          float sw2, int& npair) {
+                                                          float qk_sw, float e4_sw, float ss, float c2, float n2, float k3,
+                                                          int& npair) {
     const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
     const float uo = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
     const float un = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
@@ -203,19 +205,19 @@ __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, 
     const float ua = fminf(fmaxf(uo, n2), c2), ub = fminf(fmaxf(un, n2), c2);
     const float Aa = c2 - ua, Ab = c2 - ub;
     const float Ba = fmaf(2.0f, ua, k3), Bb = fmaf(2.0f, ub, k3);
-    const float so = Aa * Aa * Ba * sw2, sn = Ab * Ab * Bb * sw2;
+    const float po = Aa * Aa * Ba, pn = Ab * Ab * Bb;
     // Lennard-Jones, differenced directly (small at these distances)
     const float xo = ss * (ro * ro), xn = ss * (rn * rn);
     const float xo3 = xo * xo * xo, xn3 = xn * xn * xn;
-    const float d_lj = e4 * fmaf(fmaf(xn3, xn3, -xn3), sn, -(fmaf(xo3, xo3, -xo3) * so));
-    // Coulomb: qk (S_n / r_n - S_o / r_o) = qk ((1/r_n - 1/r_o) S_n + (S_n - S_o) / r_o)
+    const float d_lj = e4_sw * fmaf(fmaf(xn3, xn3, -xn3), pn, -(fmaf(xo3, xo3, -xo3) * po));
+    // Coulomb: qk (P_n / r_n - P_o / r_o) = qk ((1/r_n - 1/r_o) P_n + (P_n - P_o) / r_o)
     const float du = -fmaf(mx, dox + dnx, fmaf(my, doy + dny, mz * (doz + dnz)));
     const float p = ro * rn;
     const float dinv = __fdividef(-du * p * p, ro + rn);
     const bool sw_both = uo > n2 && un > n2 && uo < c2 && un < c2;
     const float dd = sw_both ? du : (ub - ua);
-    const float ds = sw2 * dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
-    return fmaf(qk, fmaf(dinv, sn, ro * ds), d_lj);
+    const float dp = dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
+    return fmaf(qk_sw, fmaf(dinv, pn, ro * dp), d_lj);
 }
 
 }  // namespace mcg

@@ -120,6 +120,19 @@ def test_cluster_kernels_on_dense_region_and_orthorhombic_box():
     _check_variants(s, ff, FFieldCUDA(s, "fp64", moves=False).getE10())
 
 
+def test_cluster_kernels_follow_frozen_pairs():
+    """Pairs of two frozen atoms are not in the Verlet list (List_nonBonded.cpp:867), so they are not
+    in the masks either."""
+    s = goldens.system("water512", "switch")
+    s.frozen = np.zeros(s.natom, np.uint8)
+    s.frozen[:600] = 1
+    ff = FFieldCUDA(s, "mixed", moves=False)
+    lp, _ = ff.pair_count()
+    assert ff.cluster_stats()[2] == lp
+    assert lp < FFieldCUDA(goldens.system("water512", "switch"), "mixed", moves=False).pair_count()[0]
+    _check_variants(s, ff, FFieldCUDA(s, "fp64", moves=False).getE10())
+
+
 def test_pair_kernel_selection_errors():
     s = goldens.system("water512", "switch")
     ff = FFieldCUDA(s, "fp64", moves=False)
