@@ -192,8 +192,8 @@ __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float do
 //   P_n - P_o = du' [2 A_o^2 - (A_o + A_n) B_n]   (du' = u_n - u_o on the clamped values)
 // are exact algebra for any clamped pair, so one formula covers pairs inside, crossing and beyond
 // the cutoff (beyond: P_o = P_n = 0 and the pair contributes 0).  du' is the accurate
-// -m.(d_o + d_n) when both ends lie strictly inside the switch region, the clamped difference
-// otherwise.
+// -m.(d_o + d_n) when both ends lie inside the switch region (ends on its boundaries included, where
+// the two agree), the clamped difference otherwise.
 __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, float doz, float mx, float my, float mz,
                                                           float qk_sw, float e4_sw, float ss, float c2, float n2, float k3,
                                                           int& npair) {
@@ -214,8 +214,8 @@ __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, 
     const float du = -fmaf(mx, dox + dnx, fmaf(my, doy + dny, mz * (doz + dnz)));
     const float p = ro * rn;
     const float dinv = __fdividef(-du * p * p, ro + rn);
-    const bool sw_both = uo > n2 && un > n2 && uo < c2 && un < c2;
-    const float dd = sw_both ? du : (ub - ua);
+    // both ends inside [ron^2, rc^2] exactly when the clamp left them unchanged
+    const float dd = (ua == uo && ub == un) ? du : (ub - ua);
     const float dp = dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
     return fmaf(qk_sw, fmaf(dinv, pn, ro * dp), d_lj);
 }
