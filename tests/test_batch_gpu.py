@@ -150,6 +150,29 @@ def test_lists_kept_between_sweeps_stay_complete():
     assert not np.allclose(B.energy_fp64(), e0)
 
 
+def test_orthorhombic_chain():
+    """A chain in an orthorhombic box (different edge per axis): the fixed-point mirrors, the
+    minimum image of every displacement, the cell grid and the lists follow each axis's edge."""
+    cub = systems.water_box(700, seed=51)
+    orb = systems.water_box(900, seed=52)
+    L = orb.box[0]
+    scale = np.array([1.0, 1.08, 0.93])
+    orb.set_coords(orb.coords() * scale)
+    orb.pbc_type = "orbic"
+    orb.box = tuple(L * scale)
+    B = BatchChains([cub, orb], seed=9)
+    B.sweep(2)
+    _, a, etot = B.stats()
+    e = B.energy_fp64()
+    assert np.all(a > 0)
+    assert (np.abs(etot - e) / np.abs(e)).max() <= 1e-6
+    assert abs(e[1] - _oracle_nonbonded(orb, B.coords(1))) <= 1e-10 * abs(e[1])
+    rows = [set(r.tolist()) for r in B.lists(1)]
+    miss = [(r, q) for r, q in _pairs_within(B.coords(1), 3, np.array(orb.box), 12.0)
+            if q not in rows[r] or r not in rows[q]]
+    assert not miss, miss[:5]
+
+
 def test_argon_chains_and_mixed_residue_sizes():
     ar = [systems.argon_random(n, rho, seed, temp=t) for n, rho, seed, t in ((500, 0.02, 1, 100.0), (900, 0.018, 2, 130.0))]
     B = BatchChains(ar, seed=3)
