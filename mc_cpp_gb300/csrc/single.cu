@@ -150,6 +150,10 @@ struct ListParams {
     double cutnb2;
     int cap;
     int maxspan;
+    // periodic boxes: FP32 prefilter on the fixed-point mirrors.  A pair whose FP32 r^2 lies below
+    // lo2 is inside, above hi2 outside; only the band between takes the reference's FP64 test.
+    float Ls[3], Ll[3];
+    float lo2, hi2;
 };
 
 __device__ __forceinline__ bool stored_excluded(int lo, int hi, const int* __restrict__ xs,
@@ -160,8 +164,13 @@ __device__ __forceinline__ bool stored_excluded(int lo, int hi, const int* __res
     return false;
 }
 
-// One warp per atom i; lanes walk the candidates of the stencil cells 32 at a time.
-__global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restrict__ pq, const uint8_t* __restrict__ frozen,
+// One warp per atom i; lanes walk the candidates of the stencil cells 32 at a time.  In periodic
+// boxes each candidate is first placed by its FP32 distance from the exact fixed-point mirrors
+// (error ~2e-7 of (rc + skin)^2); the reference's FP64 distance decides only the pairs within 1e-4
+// of the list radius, so the rows are the reference's sets at a fraction of the FP64 work (GB300's
+// FP64 rate is 1/64 of FP32).
+__global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restrict__ pq, const uint4* __restrict__ fx,
+                                                    const uint8_t* __restrict__ frozen,
                                                     int n, PbcDev pbc, Grid g, ListParams lp,
                                                     const int* __restrict__ cell_of, const int* __restrict__ cell_start,
                                                     const int* __restrict__ cell_atoms, const int* __restrict__ xs,
@@ -170,8 +179,10 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restric
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const bool periodic = pbc.type != 0;
     for (int i = warp; i < n; i += nwarps) {
         double4_32a pi = pq[i];
+        const uint4 xi = periodic ? fx[i] : make_uint4(0, 0, 0, 0);
         bool fi = frozen[i] != 0;
         int c = cell_of[i];
         int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
@@ -202,9 +213,22 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restric
                         if (t < e) {
                             j = cell_atoms[t];
                             if (j != i) {
-                                double4_32a pj = pq[j];
-                                double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
-                                if (r2 <= lp.cutnb2 && !(fi && frozen[j])) {
+                                bool in;
+                                float r2f = 0.0f;
+                                if (periodic) {
+                                    const uint4 xj = fx[j];
+                                    const float dx = fixed_delta(xi.x, xj.x, lp.Ls[0], lp.Ll[0]);
+                                    const float dy = fixed_delta(xi.y, xj.y, lp.Ls[1], lp.Ll[1]);
+                                    const float dz = fixed_delta(xi.z, xj.z, lp.Ls[2], lp.Ll[2]);
+                                    r2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                }
+                                if (periodic && r2f < lp.lo2) in = true;
+                                else if (periodic && r2f > lp.hi2) in = false;
+                                else {
+                                    double4_32a pj = pq[j];
+                                    in = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc) <= lp.cutnb2;
+                                }
+                                if (in && !(fi && frozen[j])) {
                                     int a = min(i, j), bb = max(i, j);
                                     if (!stored_excluded(a, bb, xs, xd, lp.maxspan)) {
                                         ok_up = j > i;
@@ -1179,10 +1203,14 @@ int SingleEngine::build_list() {
         cap = (cap + 31) & ~31;
         if ((rc = dalloc(&d_nbr, (size_t)n * cap))) return rc;
     }
-    ListParams lp{rl * rl, cap, hs.maxExclSpan};
+    ListParams lp{rl * rl, cap, hs.maxExclSpan, {0, 0, 0}, {0, 0, 0}, 0.f, 0.f};
     {
         double t = hs.rc + hs.dcut;  // (cutoff + deltacut)^2 as List_nonBonded.cpp:842-843
         lp.cutnb2 = t * t;
+        const AtomsDev A = atoms();
+        for (int k = 0; k < 3; k++) { lp.Ls[k] = A.Ls[k]; lp.Ll[k] = A.Lsl[k]; }
+        lp.lo2 = (float)(lp.cutnb2 * (1.0 - 1e-4));
+        lp.hi2 = (float)(lp.cutnb2 * (1.0 + 1e-4));
     }
     for (int attempt = 0; attempt < 3; attempt++) {
         CK(cudaMemsetAsync(d_cell_count, 0, sizeof(int) * ncell, stream));
@@ -1192,7 +1220,7 @@ int SingleEngine::build_list() {
         k_cell_scatter<<<(n + 255) / 256, 256, 0, stream>>>(d_cell_of, n, d_cell_start, d_cell_fill, d_cell_atoms);
         k_cell_sort<<<ncell, 256, 0, stream>>>(d_cell_start, ncell, d_cell_atoms);
         int blocks = std::min((n + 7) / 8, NB_BLOCKS * 2);
-        k_build_rows<<<blocks, 256, 0, stream>>>(d_pq, d_frozen, n, pbc, g, lp, d_cell_of, d_cell_start, d_cell_atoms,
+        k_build_rows<<<blocks, 256, 0, stream>>>(d_pq, d_fx, d_frozen, n, pbc, g, lp, d_cell_of, d_cell_start, d_cell_atoms,
                                                  d_xs, d_xd, d_nbr, d_nup, d_nlo, d_maxrow);
         CK(cudaGetLastError());
         int maxrow = 0;
