@@ -52,9 +52,12 @@ enum { PREC_F64 = 0, PREC_MIX = 1 };
 // Verlet list build with a cell grid (replaces the O(N^2) List_nonBonded::update_verlet_list,
 // List_nonBonded.cpp:836-915; same acceptance rule: r^2 <= (rc + skin)^2 in the reference's FP64
 // arithmetic, not both frozen, not in the stored exclusion row of the lower index).
+// Cells at least half the list radius wide: a neighbour within the radius lies within two cells
+// along each axis, so an atom scans up to 5 x 5 x 5 cells (a whole axis when it has fewer than 5).
 struct Grid {
     int nc[3];
-    double lo[3], inv[3];   // PBC none: bounding-box origin and 1/cell size
+    double lo[3], inv[3];   // PBC none: bounding-box origin and 1 / extent
+    float csf[3];           // cell widths, rounded down
     int periodic;
 };
 
@@ -154,6 +157,7 @@ struct ListParams {
     // lo2 is inside, above hi2 outside; only the band between takes the reference's FP64 test.
     float Ls[3], Ll[3];
     float lo2, hi2;
+    float reach2;   // rows of cells farther than this (squared, with a margin) are not scanned
 };
 
 __device__ __forceinline__ bool stored_excluded(int lo, int hi, const int* __restrict__ xs,
@@ -184,74 +188,130 @@ __global__ void __launch_bounds__(256) k_build_rows(const double4_32a* __restric
         double4_32a pi = pq[i];
         const uint4 xi = periodic ? fx[i] : make_uint4(0, 0, 0, 0);
         bool fi = frozen[i] != 0;
-        int c = cell_of[i];
-        int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
-        int rng[3][2], ctr[3] = {cx, cy, cz};
+        const int c = cell_of[i];
+        const int ctr[3] = {c % g.nc[0], (c / g.nc[0]) % g.nc[1], c / (g.nc[0] * g.nc[1])};
+        // per axis: the offsets scanned, and the atom's place inside its cell (in cell widths) for
+        // the distance from the atom to a cell d away along that axis.  FP32 throughout (FP64 here,
+        // warp-uniform but at GB300's FP64 rate, had cost more than the candidate tests): pos is
+        // off by ~1e-6 cell widths, inside the margin of lp.reach2.
+        int dlo[3], dhi[3];
+        bool whole[3];
+        float pos[3];
+        const uint32_t fi3[3] = {xi.x, xi.y, xi.z};
+        const double ci[3] = {pi.x, pi.y, pi.z};
         for (int k = 0; k < 3; k++) {
-            if (g.nc[k] >= 3) { rng[k][0] = -1; rng[k][1] = 1; }
-            else { rng[k][0] = -ctr[k]; rng[k][1] = g.nc[k] - 1 - ctr[k]; }
-            if (!g.periodic && g.nc[k] >= 3) {
-                rng[k][0] = max(-1, -ctr[k]);
-                rng[k][1] = min(1, g.nc[k] - 1 - ctr[k]);
+            float p;
+            if (g.periodic) {   // the mirror holds the box fraction in units of 2^-32
+                p = (float)fi3[k] * 2.3283064365386963e-10f * (float)g.nc[k] - (float)ctr[k];
+                if (p < -0.5f * g.nc[k]) p += (float)g.nc[k];       // fraction just below 1, stored as 0
+                else if (p > 0.5f * g.nc[k]) p -= (float)g.nc[k];
+            } else {
+                p = (float)((ci[k] - g.lo[k]) * g.inv[k]) * (float)g.nc[k] - (float)ctr[k];
             }
+            pos[k] = fminf(fmaxf(p, 0.f), 1.f);
+            whole[k] = g.periodic && g.nc[k] < 5;
+            if (whole[k]) { dlo[k] = -ctr[k]; dhi[k] = g.nc[k] - 1 - ctr[k]; }
+            else if (g.periodic) { dlo[k] = -2; dhi[k] = 2; }
+            else { dlo[k] = max(-2, -ctr[k]); dhi[k] = min(2, g.nc[k] - 1 - ctr[k]); }
         }
+        auto gap2 = [&](int k, int d) -> float {   // squared lower bound on |displacement| along axis k
+            if (whole[k] || d == 0) return 0.f;
+            const float w = (d > 0 ? (float)(d - 1) + (1.f - pos[k]) : (float)(-d - 1) + pos[k]) * g.csf[k];
+            return w * w;
+        };
         int up = 0, lo = 0;
         int* row = nbr + (size_t)i * lp.cap;
-        for (int dz = rng[2][0]; dz <= rng[2][1]; dz++)
-            for (int dy = rng[1][0]; dy <= rng[1][1]; dy++)
-                for (int dx = rng[0][0]; dx <= rng[0][1]; dx++) {
-                    int x = cx + dx, y = cy + dy, z = cz + dz;
-                    if (g.periodic) {
-                        x = (x + g.nc[0]) % g.nc[0]; y = (y + g.nc[1]) % g.nc[1]; z = (z + g.nc[2]) % g.nc[2];
-                    }
-                    int cc = (z * g.nc[1] + y) * g.nc[0] + x;
-                    int b = cell_start[cc], e = cell_start[cc + 1];
-                    for (int base = b; base < e; base += 32) {
-                        int t = base + lane;
-                        bool ok_up = false, ok_lo = false;
-                        int j = -1;
-                        if (t < e) {
-                            j = cell_atoms[t];
-                            if (j != i) {
-                                bool in;
-                                float r2f = 0.0f;
-                                if (periodic) {
-                                    const uint4 xj = fx[j];
-                                    const float dx = fixed_delta(xi.x, xj.x, lp.Ls[0], lp.Ll[0]);
-                                    const float dy = fixed_delta(xi.y, xj.y, lp.Ls[1], lp.Ll[1]);
-                                    const float dz = fixed_delta(xi.z, xj.z, lp.Ls[2], lp.Ll[2]);
-                                    r2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                }
-                                if (periodic && r2f < lp.lo2) in = true;
-                                else if (periodic && r2f > lp.hi2) in = false;
-                                else {
-                                    double4_32a pj = pq[j];
-                                    in = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc) <= lp.cutnb2;
-                                }
-                                if (in && !(fi && frozen[j])) {
-                                    int a = min(i, j), bb = max(i, j);
-                                    if (!stored_excluded(a, bb, xs, xd, lp.maxspan)) {
-                                        ok_up = j > i;
-                                        ok_lo = j < i;
-                                    }
-                                }
+        // candidates b .. e-1 of cell_atoms, four batches of 32 in flight per warp (the index load
+        // and the gather behind it are the latency); rows keep the candidates' order
+        auto scan = [&](int b, int e) {
+            constexpr int U = 4;
+            for (int base = b; base < e; base += 32 * U) {
+                int jj[U];
+                uint4 xj[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int t = base + 32 * u + lane;
+                    jj[u] = t < e ? cell_atoms[t] : -1;
+                }
+                if (periodic) {
+#pragma unroll
+                    for (int u = 0; u < U; u++) xj[u] = jj[u] >= 0 ? fx[jj[u]] : make_uint4(0, 0, 0, 0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (base + 32 * u >= e) break;   // warp-uniform
+                    const int j = jj[u];
+                    bool ok_up = false, ok_lo = false;
+                    if (j >= 0 && j != i) {
+                        bool in;
+                        float r2f = 0.0f;
+                        if (periodic) {
+                            const float dx = fixed_delta(xi.x, xj[u].x, lp.Ls[0], lp.Ll[0]);
+                            const float dy = fixed_delta(xi.y, xj[u].y, lp.Ls[1], lp.Ll[1]);
+                            const float dz = fixed_delta(xi.z, xj[u].z, lp.Ls[2], lp.Ll[2]);
+                            r2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        }
+                        if (periodic && r2f < lp.lo2) in = true;
+                        else if (periodic && r2f > lp.hi2) in = false;
+                        else {
+                            double4_32a pj = pq[j];
+                            in = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc) <= lp.cutnb2;
+                        }
+                        if (in && !(fi && frozen[j])) {
+                            int a = min(i, j), bb = max(i, j);
+                            if (!stored_excluded(a, bb, xs, xd, lp.maxspan)) {
+                                ok_up = j > i;
+                                ok_lo = j < i;
                             }
                         }
-                        unsigned bu = __ballot_sync(0xffffffffu, ok_up);
-                        unsigned bl = __ballot_sync(0xffffffffu, ok_lo);
-                        unsigned lt = (1u << lane) - 1u;
-                        if (ok_up) {
-                            int pos = up + __popc(bu & lt);
-                            if (pos + lo < lp.cap) row[pos] = j;
-                        }
-                        if (ok_lo) {
-                            int pos = lo + __popc(bl & lt);
-                            if (up + pos < lp.cap) row[lp.cap - 1 - pos] = j;
-                        }
-                        up += __popc(bu);
-                        lo += __popc(bl);
                     }
+                    unsigned bu = __ballot_sync(0xffffffffu, ok_up);
+                    unsigned bl = __ballot_sync(0xffffffffu, ok_lo);
+                    unsigned lt = (1u << lane) - 1u;
+                    if (ok_up) {
+                        int p = up + __popc(bu & lt);
+                        if (p + lo < lp.cap) row[p] = j;
+                    }
+                    if (ok_lo) {
+                        int p = lo + __popc(bl & lt);
+                        if (up + p < lp.cap) row[lp.cap - 1 - p] = j;
+                    }
+                    up += __popc(bu);
+                    lo += __popc(bl);
                 }
+            }
+        };
+        // the stencil's rows of cells along x (at most 5 x 5), one per lane: rows and end cells out
+        // of reach are dropped, and each row becomes one or two contiguous ranges of cell_atoms
+        const int ny = dhi[1] - dlo[1] + 1, nrow = ny * (dhi[2] - dlo[2] + 1);
+        int rb0 = 0, re0 = 0, rb1 = 0, re1 = 0;
+        bool keep = false;
+        if (lane < nrow) {
+            const int dy = dlo[1] + lane % ny, dz = dlo[2] + lane / ny;
+            const float left = lp.reach2 - gap2(2, dz) - gap2(1, dy);
+            if (left >= 0.f) {
+                keep = true;
+                int x0 = dlo[0], x1 = dhi[0];
+                while (x0 < 0 && gap2(0, x0) > left) x0++;
+                while (x1 > 0 && gap2(0, x1) > left) x1--;
+                int y = ctr[1] + dy, z = ctr[2] + dz;
+                if (g.periodic) { y = (y + g.nc[1]) % g.nc[1]; z = (z + g.nc[2]) % g.nc[2]; }
+                const int rowc = (z * g.nc[1] + y) * g.nc[0];
+                int a0 = ctr[0] + x0, a1 = ctr[0] + x1;   // both wrap only on a whole axis, which has none
+                if (a0 < 0) { rb1 = cell_start[rowc + a0 + g.nc[0]]; re1 = cell_start[rowc + g.nc[0]]; a0 = 0; }
+                if (a1 >= g.nc[0]) { rb1 = cell_start[rowc]; re1 = cell_start[rowc + a1 - g.nc[0] + 1]; a1 = g.nc[0] - 1; }
+                rb0 = cell_start[rowc + a0];
+                re0 = cell_start[rowc + a1 + 1];
+            }
+        }
+        // rows in lane order (z outer, y inner), the wrapped part of a row first
+        for (unsigned km = __ballot_sync(0xffffffffu, keep); km; km &= km - 1) {
+            const int r = __ffs(km) - 1;
+            const int b1 = __shfl_sync(0xffffffffu, rb1, r), e1 = __shfl_sync(0xffffffffu, re1, r);
+            const int b0 = __shfl_sync(0xffffffffu, rb0, r), e0 = __shfl_sync(0xffffffffu, re0, r);
+            if (e1 > b1) scan(b1, e1);
+            scan(b0, e0);
+        }
         if (lane == 0) {
             nup[i] = up;
             nlo[i] = lo;
@@ -633,10 +693,13 @@ __global__ void k_finalize(const double* __restrict__ nb, int nnb, const double*
 }
 
 // ------------------------------------------------------------------------------------------
-// Energy change of a moved set.  Block b < m handles moved atom mv[b] against its partners
-// (Verlet row in switch mode, every atom in full mode) and its 1-4 partners; block m evaluates
-// the listed bonded terms.  Pairs with both atoms moved are counted once, by the lower index.
-// The last block to finish sums the partials in block order and writes de (iu).
+// Energy change of a moved set.  Blocks b < m*S take moved atom mv[b / S] against slice b % S of
+// its partners (Verlet row in switch mode, every atom in full mode) and of its 1-4 partners; block
+// m*S evaluates the listed bonded terms.  Pairs with both atoms moved are counted once, by the
+// lower index.  Spreading a row over S blocks matters most in FP64, which GB300 runs at about two
+// lane operations per clock per SM: one block per moved atom left a water move's ~1,150 partners
+// on three SMs.  The last block to finish sums the partials (a fixed tree over the block index,
+// so de is reproducible) and writes de (iu).
 struct MoveDev {
     int m;
     const int* idx;        // sorted moved atoms
@@ -645,17 +708,30 @@ struct MoveDev {
     int nterms;
 };
 
+// A small proposal travels inside the launch (kernel parameter space, read through the constant
+// cache), so that a trial move costs one launch and no copy; m = 0 means it was staged in device
+// memory and MoveDev points there.
+constexpr int INL_M = 32, INL_T = 96;
+struct MoveInline {
+    int m, nterms;
+    int idx[INL_M];
+    int terms[2 * INL_T];
+    double xyz[3 * INL_M];
+};
+
 template <int P>
 __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, CutDev cut, MoveDev mv,
                                                  const int* __restrict__ nbr, const int* __restrict__ nup,
                                                  const int* __restrict__ nlo, int cap,
                                                  const int* __restrict__ fxs, const int* __restrict__ fxd,
                                                  const int* __restrict__ c14s, const int* __restrict__ c14d,
-                                                 BondedDev B, double* part, unsigned* ticket, double* out) {
+                                                 BondedDev B, int S, double* part, unsigned* ticket, double* out,
+                                                 const __grid_constant__ MoveInline inl) {
     __shared__ int s_idx[MAX_MOVED];
     __shared__ double s_xyz[3 * MAX_MOVED];
     __shared__ uint4 s_fx[MAX_MOVED];
     __shared__ bool s_last;
+    if (inl.m > 0) { mv.m = inl.m; mv.idx = inl.idx; mv.xyz = inl.xyz; mv.terms = inl.terms; mv.nterms = inl.nterms; }
     const int m = mv.m;
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         s_idx[k] = mv.idx[k];
@@ -679,8 +755,9 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
     };
     double del = 0.0, dvd = 0.0, dbd = 0.0;
     const bool sw = cut.mode == 1;
-    if ((int)blockIdx.x < m) {
-        const int ka = blockIdx.x;
+    if ((int)blockIdx.x < m * S) {
+        const int ka = blockIdx.x / S;
+        const int k0 = (blockIdx.x % S) * blockDim.x + threadIdx.x, kstep = S * blockDim.x;
         const int a = s_idx[ka];
         const double4_32a ao = A.pq[a];
         const double4_32a an = make_double4_32a(s_xyz[3 * ka], s_xyz[3 * ka + 1], s_xyz[3 * ka + 2], ao.w);
@@ -760,12 +837,12 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         if (sw) {
             const int* row = nbr + (size_t)a * cap;
             int u = nup[a], l = nlo[a];
-            for (int k = threadIdx.x; k < u + l; k += blockDim.x) {
+            for (int k = k0; k < u + l; k += kstep) {
                 int j = k < u ? row[k] : row[cap - 1 - (k - u)];
                 visit(j, false, true);
             }
         } else {
-            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            for (int j = k0; j < n; j += kstep) {
                 if (j == a) continue;
                 int lo_ = min(a, j), hi_ = max(a, j);
                 bool ex = false;
@@ -773,7 +850,7 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
                 if (!ex) visit(j, false, false);
             }
         }
-        for (int k = c14s[a] + threadIdx.x; k < c14s[a + 1]; k += blockDim.x) visit(c14d[k], true, sw);
+        for (int k = c14s[a] + k0; k < c14s[a + 1]; k += kstep) visit(c14d[k], true, sw);
     } else {
         CrdSrc S_old{A.pq, nullptr, nullptr, 0};
         CrdSrc S_new{A.pq, s_idx, s_xyz, m};
@@ -811,23 +888,29 @@ __global__ void __launch_bounds__(256) k_delta_e(AtomsDev A, int n, PbcDev pbc, 
         s_last = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (s_last && threadIdx.x == 0) {
+    if (s_last) {   // uniform over the block
         __threadfence();
         double se = 0.0, sv = 0.0, sb = 0.0;
-        for (unsigned b = 0; b < gridDim.x; b++) {
-            se += ((volatile double*)part)[3 * b];
-            sv += ((volatile double*)part)[3 * b + 1];
-            sb += ((volatile double*)part)[3 * b + 2];
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            se += __ldcg(part + 3 * b);
+            sv += __ldcg(part + 3 * b + 1);
+            sb += __ldcg(part + 3 * b + 2);
         }
-        out[0] = CHGCHARMM * KCALTOIU * se + 4.0 * sv + sb;
-        out[1] = se; out[2] = sv; out[3] = sb;
-        *ticket = 0u;
+        block_reduce2(se, sv, red);
+        __shared__ double rb[2];
+        block_reduce2(sb, 0.0, rb);
+        if (threadIdx.x == 0) {
+            out[0] = CHGCHARMM * KCALTOIU * red[0] + 4.0 * red[1] + rb[0];
+            out[1] = red[0]; out[2] = red[1]; out[3] = rb[0];
+            *ticket = 0u;
+        }
     }
 }
 
 template <int P>
-__global__ void k_commit(int m, const int* __restrict__ idx, const double* __restrict__ xyz, double4_32a* pq, uint4* fx,
-                         PbcDev pbc) {
+__global__ void k_commit(int m, const int* idx, const double* xyz, double4_32a* pq, uint4* fx, PbcDev pbc,
+                         const __grid_constant__ MoveInline inl) {
+    if (inl.m > 0) { idx = inl.idx; xyz = inl.xyz; }
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m) return;
     int a = idx[k];
@@ -876,10 +959,12 @@ SingleEngine::~SingleEngine() { release(); }
 void SingleEngine::release() {
     void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_prmf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
                     d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
-                    d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_out, d_maxrow,
+                    d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_maxrow,
                     d_stage};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (h_stage) cudaFreeHost(h_stage);
+    if (h_map) cudaFreeHost(h_map);
+    h_map = nullptr; d_map = nullptr;
     if (stream) cudaStreamDestroy(stream);
     d_pq = nullptr; stream = nullptr; h_stage = nullptr;
 }
@@ -955,13 +1040,16 @@ int SingleEngine::init(const HostSystem& h) {
     ntile = (n + TILE - 1) / TILE;
     size_t nparts = std::max<size_t>({(size_t)152 * 8, (size_t)ntile * (ntile + 1) / 2, (size_t)MAX_MOVED + 1});
     part_cap = nparts * 3 + 2 * 64 + 5 * 64 + 16;
-    if ((rc = dalloc(&d_part, part_cap)) || (rc = dalloc(&d_ticket, 1)) || (rc = dalloc(&d_out, 16)) ||
+    if ((rc = dalloc(&d_part, part_cap)) || (rc = dalloc(&d_ticket, 1)) ||
         (rc = dalloc(&d_maxrow, 1)))
         return rc;
     CK(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned), stream));
     // staging for moves: idx (sorted), xyz, terms
     stage_bytes = (size_t)MAX_MOVED * (4 + 24) + 64 * 1024 * 8;
     CK(cudaMallocHost(&h_stage, stage_bytes));
+    // results the host reads after a sync: de at [0, 4), the ten energy terms at [8, 18)
+    CK(cudaHostAlloc((void**)&h_map, 32 * sizeof(double), cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer((void**)&d_map, h_map, 0));
     if ((rc = dalloc((char**)&d_stage, stage_bytes))) return rc;
     k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
     CK(cudaGetLastError());
@@ -1169,20 +1257,22 @@ int SingleEngine::build_list() {
     const double rl = hs.rc + hs.dcut;
     Grid g;
     g.periodic = hs.pbc != MCG_PBC_NONE;
+    double ext[3];
     if (g.periodic) {
-        for (int k = 0; k < 3; k++) { g.nc[k] = std::max(1, (int)std::floor(hs.L[k] / rl)); g.lo[k] = 0; g.inv[k] = 0; }
+        for (int k = 0; k < 3; k++) { ext[k] = hs.L[k]; g.lo[k] = 0; g.inv[k] = 0; }
     } else {
         for (int k = 0; k < 3; k++) {
             const std::vector<double>& c = k == 0 ? host_x : (k == 1 ? host_y : host_z);
             double lo = *std::min_element(c.begin(), c.end()), hi = *std::max_element(c.begin(), c.end());
-            double ext = std::max(hi - lo, 1e-6);
-            g.nc[k] = std::max(1, (int)std::floor(ext / rl));
+            ext[k] = std::max(hi - lo, 1e-6);
             g.lo[k] = lo;
-            g.inv[k] = 1.0 / ext * (1.0 - 1e-12);
+            g.inv[k] = 1.0 / ext[k] * (1.0 - 1e-12);
         }
     }
+    for (int k = 0; k < 3; k++) g.nc[k] = std::max(1, (int)std::floor(2.0 * ext[k] / rl));
     while ((long long)g.nc[0] * g.nc[1] * g.nc[2] > (1 << 20))
         for (int k = 0; k < 3; k++) g.nc[k] = std::max(1, g.nc[k] / 2);
+    for (int k = 0; k < 3; k++) g.csf[k] = (float)(ext[k] / g.nc[k] * (1.0 - 1e-6));
     int ncell = g.nc[0] * g.nc[1] * g.nc[2];
     int rc;
     if (ncell > ncell_cap) {
@@ -1203,7 +1293,7 @@ int SingleEngine::build_list() {
         cap = (cap + 31) & ~31;
         if ((rc = dalloc(&d_nbr, (size_t)n * cap))) return rc;
     }
-    ListParams lp{rl * rl, cap, hs.maxExclSpan, {0, 0, 0}, {0, 0, 0}, 0.f, 0.f};
+    ListParams lp{rl * rl, cap, hs.maxExclSpan, {0, 0, 0}, {0, 0, 0}, 0.f, 0.f, 0.f};
     {
         double t = hs.rc + hs.dcut;  // (cutoff + deltacut)^2 as List_nonBonded.cpp:842-843
         lp.cutnb2 = t * t;
@@ -1211,6 +1301,7 @@ int SingleEngine::build_list() {
         for (int k = 0; k < 3; k++) { lp.Ls[k] = A.Ls[k]; lp.Ll[k] = A.Lsl[k]; }
         lp.lo2 = (float)(lp.cutnb2 * (1.0 - 1e-4));
         lp.hi2 = (float)(lp.cutnb2 * (1.0 + 1e-4));
+        lp.reach2 = (float)(lp.cutnb2 * (1.0 + 1e-5) + 1e-2);
     }
     for (int attempt = 0; attempt < 3; attempt++) {
         CK(cudaMemsetAsync(d_cell_count, 0, sizeof(int) * ncell, stream));
@@ -1272,11 +1363,10 @@ int SingleEngine::energy(double ener[10]) {
         nbd = std::min(64, (nterm + 255) / 256);
         k_bonded<<<nbd, 256, 0, stream>>>(B, pbc, d_pq, bd);
     }
-    k_finalize<<<1, 256, 0, stream>>>(nbp, nnb, p14, n14b, bd, nbd, d_out);
+    k_finalize<<<1, 256, 0, stream>>>(nbp, nnb, p14, n14b, bd, nbd, d_map + 8);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h_stage, d_out, 10 * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    memcpy(ener, h_stage, 10 * sizeof(double));
+    for (int k = 0; k < 10; k++) ener[k] = ((volatile double*)h_map)[8 + k];
     launches += 1 + (n14b > 0) + (nbd > 0) + 1;
     return MCG_OK;
 }
@@ -1305,15 +1395,19 @@ int SingleEngine::get_coords(double* x, double* y, double* z) {
 }
 
 int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const double* ny, const double* nz, double* de) {
+    pending_m = 0;   // a new proposal replaces the pending one, also when it is rejected
     if (m <= 0 || m > MAX_MOVED) return fail(MCG_EINVAL, "moved-set size must be in [1, 1024]");
     // sort the moved set (keeps proposal coordinates paired), reject duplicates
     std::vector<int> ord(m);
     std::iota(ord.begin(), ord.end(), 0);
     std::sort(ord.begin(), ord.end(), [&](int a, int b) { return atoms_in[a] < atoms_in[b]; });
+    // staged as [idx: m ints | xyz: 3m doubles | terms: 2 ints each], packed so that one small
+    // copy carries the proposal; the device copy stays in place for commit()
+    const size_t off_xyz = ((size_t)4 * m + 15) & ~(size_t)15, off_terms = off_xyz + (size_t)24 * m;
     char* st = (char*)h_stage;
     int* idx = (int*)st;
-    double* xyz = (double*)(st + 4 * (size_t)MAX_MOVED);
-    int* terms = (int*)(st + 28 * (size_t)MAX_MOVED);
+    double* xyz = (double*)(st + off_xyz);
+    int* terms = (int*)(st + off_terms);
     for (int k = 0; k < m; k++) {
         int a = atoms_in[ord[k]];
         if (a < 0 || a >= n) return fail(MCG_EINVAL, "moved atom index out of range");
@@ -1326,7 +1420,7 @@ int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const do
     // bonded terms touching the moved set, each once
     stamp++;
     int nt = 0;
-    const size_t tcap = (stage_bytes - 28 * (size_t)MAX_MOVED) / 8;
+    const size_t tcap = (stage_bytes - 64 - off_terms) / 8;   // the last 64 bytes take de back
     for (int k = 0; k < m; k++) {
         int a = idx[k];
         for (int t = term_start[a]; t < term_start[a + 1]; t++) {
@@ -1340,28 +1434,44 @@ int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const do
             nt++;
         }
     }
-    size_t bytes = 28 * (size_t)MAX_MOVED + (size_t)nt * 8;
-    CK(cudaMemcpyAsync(d_stage, h_stage, bytes, cudaMemcpyHostToDevice, stream));
     MoveDev mv;
     mv.m = m;
     mv.idx = (const int*)d_stage;
-    mv.xyz = (const double*)((char*)d_stage + 4 * (size_t)MAX_MOVED);
-    mv.terms = (const int*)((char*)d_stage + 28 * (size_t)MAX_MOVED);
+    mv.xyz = (const double*)((char*)d_stage + off_xyz);
+    mv.terms = (const int*)((char*)d_stage + off_terms);
     mv.nterms = nt;
+    MoveInline inl;
+    inl.m = 0; inl.nterms = 0;
+    if (m <= INL_M && nt <= INL_T) {
+        inl.m = m; inl.nterms = nt;
+        memcpy(inl.idx, idx, 4 * (size_t)m);
+        memcpy(inl.xyz, xyz, 24 * (size_t)m);
+        memcpy(inl.terms, terms, 8 * (size_t)nt);
+    } else {
+        CK(cudaMemcpyAsync(d_stage, h_stage, off_terms + (size_t)nt * 8, cudaMemcpyHostToDevice, stream));
+    }
     AtomsDev A = atoms();
     BondedDev B = bonded();
+    // slices per moved atom: about one partner per thread for a Verlet row (64 threads), about
+    // four per thread over all atoms in full mode (256 threads), at most two blocks per SM in all
+    const bool sw = hs.cut == MCG_CUT_SWITCH;
+    const int threads = sw ? 64 : 256;
+    const int span = sw ? cap : n;
+    int S = (span + (sw ? 64 : 1024) - 1) / (sw ? 64 : 1024);
+    S = std::max(1, std::min(S, std::max(1, 304 / m)));
+    S = std::min(S, std::max(1, MAX_MOVED / m));   // m*S + 1 partials fit the scratch
     if (hs.prec == MCG_PREC_FP64)
-        k_delta_e<PREC_F64><<<m + 1, 256, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs, d_fxd,
-                                                        d_c14s, d_c14d, B, d_part, d_ticket, d_out);
+        k_delta_e<PREC_F64><<<m * S + 1, threads, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs,
+                                                                d_fxd, d_c14s, d_c14d, B, S, d_part, d_ticket, d_map, inl);
     else
-        k_delta_e<PREC_MIX><<<m + 1, 256, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs, d_fxd,
-                                                        d_c14s, d_c14d, B, d_part, d_ticket, d_out);
+        k_delta_e<PREC_MIX><<<m * S + 1, threads, 0, stream>>>(A, n, pbc, cut, mv, d_nbr, d_nup, d_nlo, cap, d_fxs,
+                                                                d_fxd, d_c14s, d_c14d, B, S, d_part, d_ticket, d_map, inl);
     CK(cudaGetLastError());
-    double* hout = (double*)(st + stage_bytes - 64);
-    CK(cudaMemcpyAsync(hout, d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    *de = hout[0];
+    CK(cudaStreamSynchronize(stream));   // de lands in mapped host memory
+    *de = ((volatile double*)h_map)[0];
     pending_m = m;
+    pending_inline = inl.m > 0;
+    pending_off_xyz = off_xyz;
     pending_idx.assign(idx, idx + m);
     pending_xyz.assign(xyz, xyz + 3 * m);
     launches += 1;
@@ -1370,17 +1480,20 @@ int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const do
 
 int SingleEngine::commit() {
     if (pending_m <= 0) return fail(MCG_EINVAL, "no pending proposal to commit");
-    // the staged proposal is still on the device (d_stage) unless a later call overwrote it;
-    // re-upload from the host copy to be safe against interleaved calls
-    char* st = (char*)h_stage;
-    memcpy(st, pending_idx.data(), 4 * pending_m);
-    memcpy(st + 4 * (size_t)MAX_MOVED, pending_xyz.data(), 24 * pending_m);
-    CK(cudaMemcpyAsync(d_stage, h_stage, 28 * (size_t)MAX_MOVED, cudaMemcpyHostToDevice, stream));
+    // the pending proposal is still staged on the device: only delta_e writes d_stage, and each
+    // delta_e call replaces the pending proposal.  Stream order puts the update before any later
+    // call's work, so the host does not wait for it.
     const int* didx = (const int*)d_stage;
-    const double* dxyz = (const double*)((char*)d_stage + 4 * (size_t)MAX_MOVED);
-    k_commit<0><<<(pending_m + 127) / 128, 128, 0, stream>>>(pending_m, didx, dxyz, d_pq, d_fx, pbc);
+    const double* dxyz = (const double*)((char*)d_stage + pending_off_xyz);
+    MoveInline inl;
+    inl.m = 0; inl.nterms = 0;
+    if (pending_inline) {
+        inl.m = pending_m;
+        memcpy(inl.idx, pending_idx.data(), 4 * (size_t)pending_m);
+        memcpy(inl.xyz, pending_xyz.data(), 24 * (size_t)pending_m);
+    }
+    k_commit<0><<<(pending_m + 127) / 128, 128, 0, stream>>>(pending_m, didx, dxyz, d_pq, d_fx, pbc, inl);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(stream));
     for (int k = 0; k < pending_m; k++) {
         int a = pending_idx[k];
         host_x[a] = pending_xyz[3 * k]; host_y[a] = pending_xyz[3 * k + 1]; host_z[a] = pending_xyz[3 * k + 2];

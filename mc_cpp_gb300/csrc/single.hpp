@@ -80,7 +80,8 @@ private:
     double* d_part = nullptr;
     size_t part_cap = 0;
     unsigned* d_ticket = nullptr;
-    double* d_out = nullptr;
+    double* h_map = nullptr;   // mapped pinned results (d_map is its device address)
+    double* d_map = nullptr;
     int* d_maxrow = nullptr;
     void* h_stage = nullptr;
     void* d_stage = nullptr;
@@ -89,6 +90,8 @@ private:
     std::vector<unsigned> term_seen;
     unsigned stamp = 0;
     int pending_m = 0;
+    bool pending_inline = false;
+    size_t pending_off_xyz = 0;
     std::vector<int> pending_idx;
     std::vector<double> pending_xyz;
 };
