@@ -483,6 +483,14 @@ def _water100k(tf_peak):
                 ff.set_pair_kernel(v)
                 per[str(v)] = ff.time_nonbonded(20) / 20
             ff.set_pair_kernel(chosen)
+            # pruned rows (the default) against the whole Verlet rows, same variant
+            p_entries, _, p_ms = ff.prune_stats()
+            ff.set_prune_buffer(0.0)
+            whole_ms = ff.time_nonbonded(20) / 20
+            ff.set_prune_buffer(0.5)
+            ff.getE()
+            res5[prec]["prune"] = {"buffer_A": 0.5, "pruned_entries": p_entries, "prune_ms": p_ms,
+                                   "pair_kernel_ms_whole_list": whole_ms}
             ncl, ncp, nbits = ff.cluster_stats()
             res5[prec].update({"pair_kernel_variant": chosen, "variant_ms": per,
                                "clusters": ncl, "cluster_pairs": ncp, "cluster_mask_pairs": nbits,

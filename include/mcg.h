@@ -146,6 +146,18 @@ int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count);
  * complete).  The engine builds it only for its first energy (to time the cluster kernels) and
  * while a cluster kernel is in use. */
 int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
+/* Dynamic pruning of the rows the per-atom list kernels of the mixed periodic switch energy read
+ * (an addition without a reference counterpart: FField_MDBAS sums its whole Verlet list).  Before
+ * a launch, each half Verlet row is pruned on the device to the partners within cutoff + buffer
+ * (A) of it, once after every list build and again whenever an atom has moved more than half the
+ * buffer since the last prune (set_coords and commit track this on the host).  Every list pair
+ * within the cutoff stays in the pruned rows, so the energy sums the same pairs as over the whole
+ * list; pairs the Verlet build left out stay out.  buffer 0 turns pruning off; the default is
+ * 0.5 A.  MCG_ENOTSUP for a non-zero buffer on other systems.  mcg_prune_stats reports the
+ * entries of the last pruned rows, the number of prunes so far and the last prune's device time
+ * (ms, CUDA events on the handle's stream); zeros before the first prune. */
+int mcg_set_prune_buffer(mcg_system* s, double buffer);
+int mcg_prune_stats(mcg_system* s, int64_t* entries, int64_t* prunes, float* last_ms);
 /* Effective exclusion rows as the reference stores them (first exclPair[i] entries of
  * exclList[i]) and the 1-4 pair list (getNeighList14). */
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total);

@@ -159,6 +159,16 @@ int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, 
     return s->eng.cluster_stats(clusters, cluster_pairs, mask_pairs);
 }
 
+int mcg_set_prune_buffer(mcg_system* s, double buffer) {
+    if (!s) return fail(MCG_EINVAL, "null argument");
+    return s->eng.set_prune_buffer(buffer);
+}
+
+int mcg_prune_stats(mcg_system* s, int64_t* entries, int64_t* prunes, float* last_ms) {
+    if (!s || !entries || !prunes || !last_ms) return fail(MCG_EINVAL, "null argument");
+    return s->eng.prune_stats(entries, prunes, last_ms);
+}
+
 int mcg_get_exclusions(mcg_system* s, int* counts, int* entries, int64_t cap, int64_t* total) {
     if (!s || !counts) return fail(MCG_EINVAL, "null argument");
     const HostSystem& h = s->eng.hs;

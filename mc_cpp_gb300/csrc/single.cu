@@ -494,6 +494,59 @@ __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint
     block_reduce2(((double)EH + (double)EL) * inv_f1, ((double)VH + (double)VL) * inv_f1, part + 2 * blockIdx.x);
 }
 
+// Dynamic pruning of the half Verlet rows for the pair kernel: row i keeps, in its order, the
+// partners j > i whose FP32 distance (the pair kernel's own fixed-point displacement) lies within
+// the prune radius rp at the current positions.  While no atom has moved more than (rp - rc) / 2
+// since, every list pair within rc is still in the pruned rows, so the pair kernel sums the same
+// pairs over ~30% fewer entries (rc + skin = 14 A list, rp = 12.5 A).  The reference's stale-list
+// set is kept: pruning only removes pairs, never adds one the Verlet build left out.  A warp per
+// row, U entries in flight per lane, survivors compacted by ballot.
+constexpr int PRUNE_U = 4;
+
+__global__ void __launch_bounds__(NB_THREADS) k_prune_rows(const uint4* __restrict__ fx, int n, float Ls0, float Ls1,
+                                                        float Ls2, float Ll0, float Ll1, float Ll2, float rp2,
+                                                        const int* __restrict__ nbr, const int* __restrict__ nup,
+                                                        int cap, int* __restrict__ prn, int* __restrict__ pnup,
+                                                        unsigned long long* kept_total) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    unsigned long long kept = 0;
+    for (int i = warp; i < n; i += nwarps) {
+        const uint4 fi = fx[i];
+        const int* row = nbr + (size_t)i * cap;
+        int* out = prn + (size_t)i * cap;
+        const int m = nup[i];
+        int w = 0;
+        for (int k0 = 0; k0 < m; k0 += 32 * PRUNE_U) {
+            int j[PRUNE_U];
+            uint4 fj[PRUNE_U];
+#pragma unroll
+            for (int u = 0; u < PRUNE_U; u++) {
+                const int k = k0 + u * 32 + lane;
+                j[u] = k < m ? row[k] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < PRUNE_U; u++) fj[u] = j[u] >= 0 ? fx[j[u]] : fi;
+#pragma unroll
+            for (int u = 0; u < PRUNE_U; u++) {
+                const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
+                            dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
+                const bool keep = j[u] >= 0 && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rp2;
+                const unsigned b = __ballot_sync(0xffffffffu, keep);
+                if (keep) out[w + __popc(b & below)] = j[u];
+                w += __popc(b);
+            }
+        }
+        if (lane == 0) {
+            pnup[i] = w;
+            kept += (unsigned long long)w;
+        }
+    }
+    if (lane == 0 && kept) atomicAdd(kept_total, kept);
+}
+
 // Full energy: all pairs j > i not in the full-mode exclusion row of i, no cutoff.  Triangular
 // grid of TILE x TILE blocks; each thread owns one i and walks a shared-memory j tile with the
 // reference's sorted-row cursor (FField_MDBAS.cpp:227-234).
@@ -960,8 +1013,9 @@ void SingleEngine::release() {
     void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_prmf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
                     d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
                     d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_maxrow,
-                    d_stage};
+                    d_stage, d_prn, d_pnup, d_pkept};
     for (void* p : ptrs) if (p) cudaFree(p);
+    for (cudaEvent_t& e : ev_prune) if (e) { cudaEventDestroy(e); e = nullptr; }
     if (h_stage) cudaFreeHost(h_stage);
     if (h_map) cudaFreeHost(h_map);
     h_map = nullptr; d_map = nullptr;
@@ -1085,16 +1139,21 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     }
     AtomsDev A = atoms();
     const double inv_f1 = cluster_geom().inv_f1;
+    // the pruned rows when they are current (prepare_pair_kernel prunes before every launch that
+    // needs it), else the Verlet rows
+    const bool pr = prune_buf > 0.0 && !prune_dirty && d_prn;
+    const int* rows = pr ? d_prn : d_nbr;
+    const int* lens = pr ? d_pnup : d_nup;
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
     case 0: k_energy_list_mix<4, 4><<<152 * 4, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
     case 1: k_energy_list_mix<4, 6><<<152 * 6, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
     case 2: k_energy_list_mix<2, 8><<<152 * 8, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
+                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
     default: k_energy_list_mix<8, 3><<<152 * 3, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                        A.Lsl[1], A.Lsl[2], cut, inv_f1, d_nbr, d_nup, cap, nbp); break;
+                                                                        A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
     }
     static const int kBlocks[kListVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
     return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
@@ -1161,6 +1220,7 @@ int SingleEngine::ensure_clusters() {
 int SingleEngine::prepare_pair_kernel() {
     if (!uses_pair_variants()) return MCG_OK;
     int rc;
+    if ((rc = ensure_pruned())) return rc;
     if (pair_variant < 0) {
         if ((rc = ensure_clusters())) return rc;
         tune_pair_kernel();
@@ -1169,6 +1229,77 @@ int SingleEngine::prepare_pair_kernel() {
         if ((rc = ensure_clusters())) return rc;
         if (!clp.ok) pair_variant = 0;
     }
+    return MCG_OK;
+}
+
+// Prunes the Verlet rows for the pair kernel when they are stale: after a list build, a change of
+// the buffer, or once an atom has moved more than half the buffer (less 1e-3 A) from its position
+// at the last prune (host-side positions, minimum image).  The prune runs on the handle's stream
+// between event records, so its device time can be read back without a synchronisation here.
+int SingleEngine::ensure_pruned() {
+    if (prune_buf <= 0.0 || !prune_dirty) return MCG_OK;
+    int rc;
+    if (prn_cap != cap) {   // the pruned rows share the Verlet rows' stride
+        if (d_prn) cudaFree(d_prn);
+        d_prn = nullptr;
+        prn_cap = 0;
+        if ((rc = dalloc(&d_prn, (size_t)n * cap))) return rc;
+        prn_cap = cap;
+    }
+    if (!d_pnup && ((rc = dalloc(&d_pnup, n)) || (rc = dalloc(&d_pkept, 1)))) return rc;
+    for (cudaEvent_t& e : ev_prune)
+        if (!e) CK(cudaEventCreate(&e));
+    const AtomsDev A = atoms();
+    const double rp = hs.rc + prune_buf;
+    const float rp2 = (float)(rp * rp * (1.0 + 1e-5));   // above any FP32 rounding of r^2
+    CK(cudaMemsetAsync(d_pkept, 0, sizeof(unsigned long long), stream));
+    CK(cudaEventRecord(ev_prune[0], stream));
+    k_prune_rows<<<NB_BLOCKS, NB_THREADS, 0, stream>>>(d_fx, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2],
+                                                       rp2, d_nbr, d_nup, cap, d_prn, d_pnup, d_pkept);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev_prune[1], stream));
+    prune_x = host_x;
+    prune_y = host_y;
+    prune_z = host_z;
+    const double lim = std::max(0.0, 0.5 * prune_buf - 1e-3);
+    prune_lim2 = lim * lim;
+    prune_dirty = false;
+    prunes++;
+    launches += 1;
+    return MCG_OK;
+}
+
+// An atom's coordinates changed on the host side: the pruned rows go stale once it is further
+// than the limit from where it was at the last prune.
+void SingleEngine::note_moved(int a) {
+    double d2 = 0.0;
+    const double p[3] = {host_x[a] - prune_x[a], host_y[a] - prune_y[a], host_z[a] - prune_z[a]};
+    for (int k = 0; k < 3; k++) {
+        const double d = p[k] - hs.L[k] * std::nearbyint(p[k] / hs.L[k]);
+        d2 += d * d;
+    }
+    if (!(d2 <= prune_lim2)) prune_dirty = true;
+}
+
+int SingleEngine::set_prune_buffer(double buffer) {
+    if (!(buffer >= 0.0) || !std::isfinite(buffer)) return fail(MCG_EINVAL, "prune buffer must be finite and >= 0");
+    if (buffer > 0.0 && !uses_pair_variants())
+        return fail(MCG_ENOTSUP, "pruning applies to the mixed periodic switch energy");
+    prune_buf = buffer;
+    prune_dirty = true;
+    return MCG_OK;
+}
+
+int SingleEngine::prune_stats(int64_t* entries, int64_t* nprunes, float* last_ms) {
+    *entries = 0;
+    *nprunes = prunes;
+    *last_ms = 0.f;
+    if (prunes == 0 || !d_pkept) return MCG_OK;
+    unsigned long long k = 0;
+    CK(cudaMemcpyAsync(&k, d_pkept, sizeof(k), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaEventElapsedTime(last_ms, ev_prune[0], ev_prune[1]));
+    *entries = (int64_t)k;
     return MCG_OK;
 }
 
@@ -1320,6 +1451,7 @@ int SingleEngine::build_list() {
         last_max_row = maxrow;
         if (maxrow <= cap) {
             clp_dirty = uses_pair_variants();   // the cluster form follows on first use
+            prune_dirty = true;                 // and so do the pruned rows
             return MCG_OK;
         }
         cudaFree(d_nbr);
@@ -1379,6 +1511,8 @@ int SingleEngine::set_coords(const double* x, const double* y, const double* z) 
         pq[i] = make_double4_32a(x[i], y[i], z[i], hs.q[i]);
         host_x[i] = x[i]; host_y[i] = y[i]; host_z[i] = z[i];
     }
+    if (!prune_dirty)
+        for (int i = 0; i < n && !prune_dirty; i++) note_moved(i);
     CK(cudaMemcpyAsync(d_pq, pq.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
     k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
     CK(cudaGetLastError());
@@ -1497,6 +1631,7 @@ int SingleEngine::commit() {
     for (int k = 0; k < pending_m; k++) {
         int a = pending_idx[k];
         host_x[a] = pending_xyz[3 * k]; host_y[a] = pending_xyz[3 * k + 1]; host_z[a] = pending_xyz[3 * k + 2];
+        if (!prune_dirty) note_moved(a);
     }
     pending_m = 0;
     launches += 1;

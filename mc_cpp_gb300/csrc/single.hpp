@@ -32,6 +32,10 @@ public:
     int pair_kernel() const { return pair_variant; }
     static int pair_kernel_count();
     int cluster_stats(int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
+    // Dynamic pruning of the rows the mixed periodic switch energy reads: buffer (A) beyond rc,
+    // 0 = the pair kernel reads the Verlet rows themselves.
+    int set_prune_buffer(double buffer);
+    int prune_stats(int64_t* entries, int64_t* prunes, float* last_ms);
     ClusterPairs clp;
 
     HostSystem hs;
@@ -57,6 +61,17 @@ private:
     int ensure_clusters();
     int prepare_pair_kernel();
     bool clp_dirty = false;       // the Verlet list changed since the cluster form was built
+    int ensure_pruned();
+    void note_moved(int atom);
+    double prune_buf = 0.5;       // prune radius rc + prune_buf
+    bool prune_dirty = true;      // rows to be pruned again before the next pair-kernel launch
+    double prune_lim2 = 0.0;      // squared displacement since the prune that forces a new one
+    int prn_cap = 0;
+    int64_t prunes = 0;
+    std::vector<double> prune_x, prune_y, prune_z;   // positions at the last prune
+    int *d_prn = nullptr, *d_pnup = nullptr;         // pruned rows (stride cap) and their lengths
+    unsigned long long* d_pkept = nullptr;
+    cudaEvent_t ev_prune[2] = {nullptr, nullptr};
 
     cudaStream_t stream = nullptr;
     PbcDev pbc{};

@@ -116,6 +116,16 @@ class FFieldCUDA:
         native.check(native.lib().mcg_cluster_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def set_prune_buffer(self, buffer: float) -> None:
+        """Prune buffer (A) of the rows the mixed periodic switch energy reads; 0 = whole list."""
+        native.check(native.lib().mcg_set_prune_buffer(self.h, float(buffer)))
+
+    def prune_stats(self):
+        """(entries of the pruned rows, prunes so far, last prune's device time in ms)."""
+        a, b, t = C.c_int64(0), C.c_int64(0), C.c_float(0)
+        native.check(native.lib().mcg_prune_stats(self.h, C.byref(a), C.byref(b), C.byref(t)))
+        return a.value, b.value, t.value
+
     def pair_count(self):
         """(list pairs, pairs within the cutoff at the current coordinates)."""
         a, b = C.c_int64(0), C.c_int64(0)

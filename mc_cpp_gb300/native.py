@@ -132,6 +132,8 @@ def lib():
         "mcg_set_pair_kernel": (C.c_int, [P, C.c_int]),
         "mcg_get_pair_kernel": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "mcg_cluster_stats": (C.c_int, [P, _i64, _i64, _i64]),
+        "mcg_set_prune_buffer": (C.c_int, [P, C.c_double]),
+        "mcg_prune_stats": (C.c_int, [P, _i64, _i64, C.POINTER(C.c_float)]),
         "mcg_mdbas_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P)]),
         "mcg_mdbas_natom": (C.c_int, [P]),
         "mcg_mdbas_fill": (C.c_int, [P, C.POINTER(SystemDesc)]),
