@@ -425,10 +425,18 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
 // pairs have S = 1 exactly.  Same terms as mixed_pair (unscaled, k_finalize scales).
 // U list entries in flight per lane; MINB resident CTAs per SM requested from the register
 // allocator (occupancy against registers); the engine times the variants once and keeps the fastest.
-template <int U, int MINB>
+// Both gathers of an entry (position and parameters) are issued together, unconditionally: over
+// pruned rows ~88% of the entries lie within rc, so the parameter load is rarely wasted and the
+// two dependent gather phases become one.  A padded slot (past the row's end) reads atom i itself
+// and is masked by its index.  Slots wholly past the row's end are skipped by a warp-uniform test.
+// ISO (cubic boxes): r^2 is summed in fixed-point units (exact integer differences converted to
+// FP32) and scaled once by the float-float square of the unit length, two instructions per entry
+// instead of a float-float scale per axis.
+template <int U, int MINB, bool ISO>
 __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint4* __restrict__ fx, const float4* __restrict__ prm,
                                                                       int n, float Ls0, float Ls1, float Ls2, float Ll0,
-                                                                      float Ll1, float Ll2, CutDev cut, double inv_f1,
+                                                                      float Ll1, float Ll2, float L2h, float L2l,
+                                                                      CutDev cut, double inv_f1,
                                                                       const int* __restrict__ nbr,
                                                                       const int* __restrict__ nup, int cap, double* part) {
     const int lane = threadIdx.x & 31;
@@ -446,27 +454,34 @@ __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint
             int j[U];
             uint4 fj[U];
             float4 pj[U];
-            float r2[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * 32 + lane;
-                j[u] = k < m ? row[k] : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < U; u++) fj[u] = j[u] >= 0 ? fx[j[u]] : fi;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
-                            dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
-                r2[u] = j[u] >= 0 ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 2.0f * c2;
-                pj[u] = r2[u] <= c2 ? prm[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+                j[u] = k < m ? row[k] : i;
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                if (r2[u] <= c2) {
-                    float rinv = rsqrtf(r2[u]);
-                    rinv = rinv * fmaf(-0.5f * r2[u] * rinv, rinv, 1.5f);   // one Newton step
-                    const float uu = fmaxf(r2[u], n2);
+                fj[u] = fx[j[u]];
+                pj[u] = prm[j[u]];
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (k0 + u * 32 >= m) break;   // warp-uniform: this and later slots are past the row
+                float r2;
+                if (ISO) {
+                    const float ux = __int2float_rn((int)(fj[u].x - fi.x)), uy = __int2float_rn((int)(fj[u].y - fi.y)),
+                                uz = __int2float_rn((int)(fj[u].z - fi.z));
+                    const float r2u = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+                    r2 = fmaf(r2u, L2h, r2u * L2l);
+                } else {
+                    const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
+                                dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
+                    r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                }
+                if (j[u] != i && r2 <= c2) {
+                    float rinv = rsqrtf(r2);
+                    rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
+                    const float uu = fmaxf(r2, n2);
                     const float a = c2 - uu;
                     const float f = a * a * fmaf(2.0f, uu, k3);
                     const float g = rinv * f;
@@ -1144,18 +1159,29 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     const bool pr = prune_buf > 0.0 && !prune_dirty && d_prn;
     const int* rows = pr ? d_prn : d_nbr;
     const int* lens = pr ? d_pnup : d_nup;
+    // cubic boxes: r^2 in fixed-point units scaled by the float-float square of the unit length
+    const bool iso = A.Ls[0] == A.Ls[1] && A.Ls[1] == A.Ls[2] && A.Lsl[0] == A.Lsl[1] && A.Lsl[1] == A.Lsl[2];
+    const double l2 = (double)A.Ls[0] + (double)A.Lsl[0];
+    const double l2sq = l2 * l2;
+    const float L2h = (float)l2sq, L2l = (float)(l2sq - (double)L2h);
+#define MCG_LIST_MIX(U_, B_)                                                                                   \
+    if (iso)                                                                                                  \
+        k_energy_list_mix<U_, B_, true><<<152 * B_, NB_THREADS, 0, stream>>>(                                 \
+            d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, rows, \
+            lens, cap, nbp);                                                                                  \
+    else                                                                                                      \
+        k_energy_list_mix<U_, B_, false><<<152 * B_, NB_THREADS, 0, stream>>>(                                \
+            d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, rows, \
+            lens, cap, nbp);
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
-    case 0: k_energy_list_mix<4, 4><<<152 * 4, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
-    case 1: k_energy_list_mix<4, 6><<<152 * 6, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
-    case 2: k_energy_list_mix<2, 8><<<152 * 8, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                       A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
-    default: k_energy_list_mix<8, 3><<<152 * 3, NB_THREADS, 0, stream>>>(d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0],
-                                                                        A.Lsl[1], A.Lsl[2], cut, inv_f1, rows, lens, cap, nbp); break;
+    case 0: MCG_LIST_MIX(4, 4) break;
+    case 1: MCG_LIST_MIX(6, 3) break;
+    case 2: MCG_LIST_MIX(2, 5) break;
+    default: MCG_LIST_MIX(8, 2) break;
     }
-    static const int kBlocks[kListVariants] = {152 * 4, 152 * 6, 152 * 8, 152 * 3};
+#undef MCG_LIST_MIX
+    static const int kBlocks[kListVariants] = {152 * 4, 152 * 3, 152 * 5, 152 * 2};
     return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
 }
 
