@@ -4,7 +4,8 @@
 //   pq[n]        double4_32a (x, y, z, q)      FP64 master coordinates + charge (32 B, aligned loads)
 //   es[n]        double2 (eps, sig)        sqrt(eps*418.4) and MDBAS half-sigma
 //   es14[n]      double2 (eps14, sig14)
-//   fx[n]        uint4 (fx, fy, fz, q as float bits)  fixed-point mirror for the mixed kernels
+//   fx[n]        uint4 (fx, fy, fz, parameter class)  fixed-point mirror for the mixed kernels
+//   cls_of[n], cls[ncls]  parameter class of each atom and the classes' (q hi, q lo, eps, sig)
 //   esf[n]       float2 (eps, sig)
 //   nbr[n*cap]   int   Verlet rows: partners j > i from the front, j < i from the back
 //   nup[n], nlo[n]
@@ -22,6 +23,8 @@
 //   k_delta_e<P>       energy change of a moved atom set, one launch
 //   k_commit           write accepted coordinates
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -45,6 +48,7 @@ constexpr int NB_BLOCKS = 152 * 4;   // grid of the list-driven kernels: 4 CTAs 
 constexpr int NB_THREADS = 256;
 constexpr int MAX_MOVED = 1024;
 constexpr int SORT_MAX = 2048;       // cells larger than this are sorted by one thread
+constexpr int CLS_MAX = 1024;        // parameter classes the mixed pair kernel keeps in shared memory
 
 enum { PREC_F64 = 0, PREC_MIX = 1 };
 
@@ -432,13 +436,22 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
 // ISO (cubic boxes): r^2 is summed in fixed-point units (exact integer differences converted to
 // FP32) and scaled once by the float-float square of the unit length, two instructions per entry
 // instead of a float-float scale per axis.
-template <int U, int MINB, bool ISO>
+// TYPED: the atoms' parameters come from a table of the system's distinct (q, eps, sig) classes
+// in shared memory, indexed by the class the fixed-point mirror carries in w, so an entry costs
+// one global gather (its position) instead of two.
+template <int U, int MINB, bool ISO, bool TYPED>
 __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint4* __restrict__ fx, const float4* __restrict__ prm,
+                                                                      const float4* __restrict__ cls, int ncls,
                                                                       int n, float Ls0, float Ls1, float Ls2, float Ll0,
                                                                       float Ll1, float Ll2, float L2h, float L2l,
                                                                       CutDev cut, double inv_f1,
                                                                       const int* __restrict__ nbr,
                                                                       const int* __restrict__ nup, int cap, double* part) {
+    extern __shared__ float4 s_cls[];
+    if (TYPED) {
+        for (int c = threadIdx.x; c < ncls; c += blockDim.x) s_cls[c] = cls[c];
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -462,11 +475,12 @@ __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 fj[u] = fx[j[u]];
-                pj[u] = prm[j[u]];
+                if (!TYPED) pj[u] = prm[j[u]];
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (k0 + u * 32 >= m) break;   // warp-uniform: this and later slots are past the row
+                if (TYPED) pj[u] = s_cls[fj[u].w];
                 float r2;
                 if (ISO) {
                     const float ux = __int2float_rn((int)(fj[u].x - fi.x)), uy = __int2float_rn((int)(fj[u].y - fi.y)),
@@ -992,14 +1006,15 @@ __global__ void k_commit(int m, const int* idx, const double* xyz, double4_32a* 
     }
 }
 
-__global__ void k_fix_all(int n, const double4_32a* __restrict__ pq, uint4* fx, PbcDev pbc) {
+// Fixed-point mirror of every atom from the FP64 masters; w carries the atom's parameter class.
+__global__ void k_fix_all(int n, const double4_32a* __restrict__ pq, const int* __restrict__ cls_of, uint4* fx, PbcDev pbc) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double4_32a p = pq[i];
     uint4 f;
     if (pbc.type != 0) { f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]); }
     else { f.x = f.y = f.z = 0; }
-    f.w = __float_as_uint((float)p.w);
+    f.w = (unsigned)cls_of[i];
     fx[i] = f;
 }
 
@@ -1028,7 +1043,7 @@ void SingleEngine::release() {
     void* ptrs[] = {d_pq, d_es, d_es14, d_fx, d_esf, d_esf14, d_qf, d_prmf, d_frozen, d_xs, d_xd, d_fxs, d_fxd, d_p14, d_c14s,
                     d_c14d, d_bonds, d_ubs, d_angles, d_dihes, d_imprs, d_nbr, d_nup, d_nlo, d_cell_of,
                     d_cell_count, d_cell_start, d_cell_fill, d_cell_atoms, d_part, d_ticket, d_maxrow,
-                    d_stage, d_prn, d_pnup, d_pkept};
+                    d_stage, d_prn, d_pnup, d_pkept, d_cls_of, d_cls};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (cudaEvent_t& e : ev_prune) if (e) { cudaEventDestroy(e); e = nullptr; }
     if (h_stage) cudaFreeHost(h_stage);
@@ -1066,7 +1081,30 @@ int SingleEngine::init(const HostSystem& h) {
         qf[i] = make_float2(qh, (float)(hs.q[i] - (double)qh));
         prmf[i] = make_float4(qf[i].x, qf[i].y, esf[i].x, esf[i].y);
     }
+    // parameter classes: the distinct (q hi, q lo, eps, sig) of the mixed pair kernel, in first-seen
+    // order; more than CLS_MAX classes leave the table empty (the kernel gathers per atom)
+    std::vector<int> cls_of(n, 0);
+    std::vector<float4> cls;
+    {
+        std::map<std::array<uint32_t, 4>, int> seen;
+        for (int i = 0; i < n && (int)cls.size() <= CLS_MAX; i++) {
+            std::array<uint32_t, 4> key;
+            memcpy(key.data(), &prmf[i], sizeof(float4));
+            auto it = seen.find(key);
+            if (it == seen.end()) {
+                it = seen.emplace(key, (int)cls.size()).first;
+                cls.push_back(prmf[i]);
+            }
+            cls_of[i] = it->second;
+        }
+        if ((int)cls.size() > CLS_MAX) {
+            cls.clear();
+            std::fill(cls_of.begin(), cls_of.end(), 0);
+        }
+        ncls = (int)cls.size();
+    }
     int rc;
+    if ((rc = dupload(&d_cls_of, cls_of, stream)) || (rc = dupload(&d_cls, cls, stream))) return rc;
     if ((rc = dupload(&d_pq, pq, stream)) || (rc = dupload(&d_es, es, stream)) || (rc = dupload(&d_es14, es14, stream)) ||
         (rc = dupload(&d_esf, esf, stream)) || (rc = dupload(&d_esf14, esf14, stream)) || (rc = dupload(&d_qf, qf, stream)) ||
         (rc = dupload(&d_prmf, prmf, stream)) ||
@@ -1120,7 +1158,7 @@ int SingleEngine::init(const HostSystem& h) {
     CK(cudaHostAlloc((void**)&h_map, 32 * sizeof(double), cudaHostAllocMapped));
     CK(cudaHostGetDevicePointer((void**)&d_map, h_map, 0));
     if ((rc = dalloc((char**)&d_stage, stage_bytes))) return rc;
-    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
+    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_cls_of, d_fx, pbc);
     CK(cudaGetLastError());
     host_x = hs.x; host_y = hs.y; host_z = hs.z;
     if (hs.cut == MCG_CUT_SWITCH) {
@@ -1164,15 +1202,15 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     const double l2 = (double)A.Ls[0] + (double)A.Lsl[0];
     const double l2sq = l2 * l2;
     const float L2h = (float)l2sq, L2l = (float)(l2sq - (double)L2h);
+#define MCG_LIST_MIX_ONE(U_, B_, ISO_, TY_)                                                                  \
+    k_energy_list_mix<U_, B_, ISO_, TY_><<<152 * B_, NB_THREADS, TY_ ? sizeof(float4) * ncls : 0, stream>>>(   \
+        d_fx, d_prmf, d_cls, ncls, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, \
+        rows, lens, cap, nbp);
 #define MCG_LIST_MIX(U_, B_)                                                                                   \
-    if (iso)                                                                                                  \
-        k_energy_list_mix<U_, B_, true><<<152 * B_, NB_THREADS, 0, stream>>>(                                 \
-            d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, rows, \
-            lens, cap, nbp);                                                                                  \
-    else                                                                                                      \
-        k_energy_list_mix<U_, B_, false><<<152 * B_, NB_THREADS, 0, stream>>>(                                \
-            d_fx, d_prmf, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, rows, \
-            lens, cap, nbp);
+    if (iso && ncls > 0) { MCG_LIST_MIX_ONE(U_, B_, true, true) }                                             \
+    else if (iso) { MCG_LIST_MIX_ONE(U_, B_, true, false) }                                                   \
+    else if (ncls > 0) { MCG_LIST_MIX_ONE(U_, B_, false, true) }                                              \
+    else { MCG_LIST_MIX_ONE(U_, B_, false, false) }
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
     case 0: MCG_LIST_MIX(4, 4) break;
@@ -1181,6 +1219,7 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     default: MCG_LIST_MIX(8, 2) break;
     }
 #undef MCG_LIST_MIX
+#undef MCG_LIST_MIX_ONE
     static const int kBlocks[kListVariants] = {152 * 4, 152 * 3, 152 * 5, 152 * 2};
     return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
 }
@@ -1540,7 +1579,7 @@ int SingleEngine::set_coords(const double* x, const double* y, const double* z) 
     if (!prune_dirty)
         for (int i = 0; i < n && !prune_dirty; i++) note_moved(i);
     CK(cudaMemcpyAsync(d_pq, pq.data(), sizeof(double4_32a) * n, cudaMemcpyHostToDevice, stream));
-    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_fx, pbc);
+    k_fix_all<<<(n + 255) / 256, 256, 0, stream>>>(n, d_pq, d_cls_of, d_fx, pbc);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
     return MCG_OK;

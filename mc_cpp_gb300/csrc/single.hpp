@@ -82,6 +82,9 @@ private:
     uint4* d_fx = nullptr;
     float2 *d_esf = nullptr, *d_esf14 = nullptr, *d_qf = nullptr;
     float4* d_prmf = nullptr;     // (q as float-float, eps, sig) per atom for the mixed pair kernel
+    int* d_cls_of = nullptr;      // parameter class of each atom (also in the mirror's w)
+    float4* d_cls = nullptr;      // the classes' (q hi, q lo, eps, sig); ncls = 0: per-atom gathers
+    int ncls = 0;
     uint8_t* d_frozen = nullptr;
     int *d_xs = nullptr, *d_xd = nullptr, *d_fxs = nullptr, *d_fxd = nullptr;
     int2* d_p14 = nullptr;

@@ -1,4 +1,4 @@
-"""Dynamic pruning of the Verlet rows read by the mixed periodic switch energy, through the C ABI.
+"""The mixed periodic switch pair kernel's row pruning and parameter classes, through the C ABI.
 
 Pruning only shortens the rows the pair kernel walks; the pairs it sums must stay the Verlet
 list's pairs within the cutoff.  So, for every per-atom list variant:
@@ -9,7 +9,13 @@ list's pairs within the cutoff.  So, for every per-atom list variant:
 The pruned rows hold at least the pairs within the cutoff and fewer entries than the list.
 Displacements below half the buffer keep the rows (no new prune); a displacement beyond it, by
 set_coords or by a committed move, prunes again before the next energy.
+
+Atom parameters reach the kernel from a shared-memory table of the system's distinct
+(q, eps, sig) classes when there are at most 1024 of them, else by a per-atom gather; a system
+with a distinct charge on every atom takes the second path and must meet the same tolerance.
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -113,3 +119,17 @@ def test_prune_buffer_arguments():
     f64 = FFieldCUDA(s, "fp64", moves=False)
     assert L.mcg_set_prune_buffer(f64.h, 0.5) == native.MCG_ENOTSUP
     assert L.mcg_set_prune_buffer(f64.h, 0.0) == native.MCG_OK
+
+
+def test_per_atom_parameters_beyond_the_class_table():
+    s = copy.deepcopy(goldens.system("water4096", "switch"))
+    rng = np.random.default_rng(3)
+    s.q = np.asarray(s.q, np.float64) * (1.0 + 1e-3 * rng.uniform(-1.0, 1.0, s.natom))   # 12,288 classes
+    want = FFieldCUDA(s, "fp64", moves=False).getE10()
+    ff = FFieldCUDA(s, "mixed", moves=False)
+    whole = FFieldCUDA(s, "mixed", moves=False)
+    whole.set_prune_buffer(0.0)
+    for v in range(N_LIST_VARIANTS):
+        ff.set_pair_kernel(v)
+        whole.set_pair_kernel(v)
+        _agree(ff.getE10(), whole.getE10(), want, ("per-atom", v))
