@@ -436,6 +436,59 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
 // ISO (cubic boxes): r^2 is summed in fixed-point units (exact integer differences converted to
 // FP32) and scaled once by the float-float square of the unit length, two instructions per entry
 // instead of a float-float scale per axis.
+// One batch of U entries per lane of row i (the pair terms of the kernel below).
+template <int U, bool ISO, bool TYPED>
+__device__ __forceinline__ void mix_batch(const int (&j)[U], const uint4 (&fj)[U], float4 (&pj)[U], const float4* s_cls,
+                                          int i, uint4 fi, float4 pi, int k0, int m, float Ls0, float Ls1, float Ls2,
+                                          float Ll0, float Ll1, float Ll2, float L2h, float L2l, float c2, float n2,
+                                          float k3, float& ch, float& cl, float& vs) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        if (k0 + u * 32 >= m) break;   // warp-uniform: this and later slots are past the row
+        if (TYPED) pj[u] = s_cls[fj[u].w];
+        float r2;
+        if (ISO) {
+            const float ux = __int2float_rn((int)(fj[u].x - fi.x)), uy = __int2float_rn((int)(fj[u].y - fi.y)),
+                        uz = __int2float_rn((int)(fj[u].z - fi.z));
+            const float r2u = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+            r2 = fmaf(r2u, L2h, r2u * L2l);
+        } else {
+            const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
+                        dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
+            r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        }
+        if (j[u] != i && r2 <= c2) {
+            float rinv = rsqrtf(r2);
+            rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
+            const float uu = fmaxf(r2, n2);
+            const float a = c2 - uu;
+            const float f = a * a * fmaf(2.0f, uu, k3);
+            const float g = rinv * f;
+            float sm, er;
+            two_sum(ch, pj[u].x * g, sm, er);
+            ch = sm;
+            cl = fmaf(pj[u].y, g, cl + er);
+            const float y = (pi.w + pj[u].w) * rinv;
+            const float x2 = y * y;
+            const float x6 = x2 * x2 * x2;
+            vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
+        }
+    }
+}
+
+// the lane's share of row i: q_i (ch + cl) and eps_i vs, into the lane's float-float totals
+__device__ __forceinline__ void mix_row_flush(float4 pi, float ch, float cl, float vs, float& EH, float& EL, float& VH,
+                                              float& VL) {
+    float ph, pl, sm, er;
+    ff_mul(pi.x, pi.y, ch, cl, ph, pl);
+    two_sum(EH, ph, sm, er);
+    EH = sm;
+    EL += er + pl;
+    two_sum(VH, pi.z * vs, sm, er);
+    VH = sm;
+    VL += er;
+}
+
 // TYPED: the atoms' parameters come from a table of the system's distinct (q, eps, sig) classes
 // in shared memory, indexed by the class the fixed-point mirror carries in w, so an entry costs
 // one global gather (its position) instead of two.
@@ -477,48 +530,10 @@ __global__ void __launch_bounds__(NB_THREADS, MINB) k_energy_list_mix(const uint
                 fj[u] = fx[j[u]];
                 if (!TYPED) pj[u] = prm[j[u]];
             }
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                if (k0 + u * 32 >= m) break;   // warp-uniform: this and later slots are past the row
-                if (TYPED) pj[u] = s_cls[fj[u].w];
-                float r2;
-                if (ISO) {
-                    const float ux = __int2float_rn((int)(fj[u].x - fi.x)), uy = __int2float_rn((int)(fj[u].y - fi.y)),
-                                uz = __int2float_rn((int)(fj[u].z - fi.z));
-                    const float r2u = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-                    r2 = fmaf(r2u, L2h, r2u * L2l);
-                } else {
-                    const float dx = fixed_delta(fi.x, fj[u].x, Ls0, Ll0), dy = fixed_delta(fi.y, fj[u].y, Ls1, Ll1),
-                                dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
-                    r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                }
-                if (j[u] != i && r2 <= c2) {
-                    float rinv = rsqrtf(r2);
-                    rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
-                    const float uu = fmaxf(r2, n2);
-                    const float a = c2 - uu;
-                    const float f = a * a * fmaf(2.0f, uu, k3);
-                    const float g = rinv * f;
-                    float sm, er;
-                    two_sum(ch, pj[u].x * g, sm, er);
-                    ch = sm;
-                    cl = fmaf(pj[u].y, g, cl + er);
-                    const float y = (pi.w + pj[u].w) * rinv;
-                    const float x2 = y * y;
-                    const float x6 = x2 * x2 * x2;
-                    vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
-                }
-            }
+            mix_batch<U, ISO, TYPED>(j, fj, pj, s_cls, i, fi, pi, k0, m, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, L2h, L2l, c2, n2,
+                                     k3, ch, cl, vs);
         }
-        // the lane's share of row i: q_i (ch + cl) and eps_i vs, into the float-float totals
-        float ph, pl, sm, er;
-        ff_mul(pi.x, pi.y, ch, cl, ph, pl);
-        two_sum(EH, ph, sm, er);
-        EH = sm;
-        EL += er + pl;
-        two_sum(VH, pi.z * vs, sm, er);
-        VH = sm;
-        VL += er;
+        mix_row_flush(pi, ch, cl, vs, EH, EL, VH, VL);
     }
     block_reduce2(((double)EH + (double)EL) * inv_f1, ((double)VH + (double)VL) * inv_f1, part + 2 * blockIdx.x);
 }
@@ -1202,8 +1217,10 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     const double l2 = (double)A.Ls[0] + (double)A.Lsl[0];
     const double l2sq = l2 * l2;
     const float L2h = (float)l2sq, L2l = (float)(l2sq - (double)L2h);
+    int blocks = 0;
 #define MCG_LIST_MIX_ONE(U_, B_, ISO_, TY_)                                                                  \
-    k_energy_list_mix<U_, B_, ISO_, TY_><<<152 * B_, NB_THREADS, TY_ ? sizeof(float4) * ncls : 0, stream>>>(   \
+    blocks = 152 * B_;                                                                                        \
+    k_energy_list_mix<U_, B_, ISO_, TY_><<<152 * B_, NB_THREADS, TY_ ? sizeof(float4) * ncls : 0, stream>>>( \
         d_fx, d_prmf, d_cls, ncls, n, A.Ls[0], A.Ls[1], A.Ls[2], A.Lsl[0], A.Lsl[1], A.Lsl[2], L2h, L2l, cut, inv_f1, \
         rows, lens, cap, nbp);
 #define MCG_LIST_MIX(U_, B_)                                                                                   \
@@ -1215,13 +1232,12 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     switch (v) {
     case 0: MCG_LIST_MIX(4, 4) break;
     case 1: MCG_LIST_MIX(6, 3) break;
-    case 2: MCG_LIST_MIX(2, 5) break;
-    default: MCG_LIST_MIX(8, 2) break;
+    case 2: MCG_LIST_MIX(4, 5) break;
+    default: MCG_LIST_MIX(8, 3) break;
     }
 #undef MCG_LIST_MIX
 #undef MCG_LIST_MIX_ONE
-    static const int kBlocks[kListVariants] = {152 * 4, 152 * 3, 152 * 5, 152 * 2};
-    return kBlocks[v < 0 || v >= kListVariants ? kListVariants - 1 : v];
+    return blocks;
 }
 
 // Times every pair-kernel variant on the current system (3 launches each) and keeps the fastest;
