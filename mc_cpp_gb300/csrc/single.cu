@@ -1231,9 +1231,9 @@ int SingleEngine::launch_pair_variant(int v, double* nbp) {
     // grids sized to the residency each variant asks for (NB_THREADS threads per CTA)
     switch (v) {
     case 0: MCG_LIST_MIX(4, 4) break;
-    case 1: MCG_LIST_MIX(6, 3) break;
-    case 2: MCG_LIST_MIX(4, 5) break;
-    default: MCG_LIST_MIX(8, 3) break;
+    case 1: MCG_LIST_MIX(5, 4) break;
+    case 2: MCG_LIST_MIX(3, 5) break;
+    default: MCG_LIST_MIX(6, 4) break;
     }
 #undef MCG_LIST_MIX
 #undef MCG_LIST_MIX_ONE
