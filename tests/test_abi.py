@@ -39,6 +39,17 @@ def test_abi_version_and_errors_without_device():
         assert b"no CUDA device" in L.mcg_last_error()
 
 
+def test_null_handles_rejected_on_host():
+    """Handle-taking entry points check their arguments before any device work."""
+    L = native.lib()
+    i64, f32 = C.c_int64(0), C.c_float(0)
+    assert L.mcg_set_prune_buffer(None, 0.5) == native.MCG_EINVAL
+    assert L.mcg_prune_stats(None, C.byref(i64), C.byref(i64), C.byref(f32)) == native.MCG_EINVAL
+    assert L.mcg_set_pair_kernel(None, 0) == native.MCG_EINVAL
+    assert L.mcg_cluster_stats(None, C.byref(i64), C.byref(i64), C.byref(i64)) == native.MCG_EINVAL
+    assert b"null" in L.mcg_last_error()
+
+
 def test_host_exclusions_match_reference_rows():
     # the library's host-side List_nonBonded restatement, no device needed
     for name in ("diala_vac", "nma_solvated", "peptide"):
