@@ -1327,7 +1327,8 @@ int SingleEngine::ensure_pruned() {
         if ((rc = dalloc(&d_prn, (size_t)n * cap))) return rc;
         prn_cap = cap;
     }
-    if (!d_pnup && ((rc = dalloc(&d_pnup, n)) || (rc = dalloc(&d_pkept, 1)))) return rc;
+    if (!d_pnup && (rc = dalloc(&d_pnup, n))) return rc;
+    if (!d_pkept && (rc = dalloc(&d_pkept, 1))) return rc;
     for (cudaEvent_t& e : ev_prune)
         if (!e) CK(cudaEventCreate(&e));
     const AtomsDev A = atoms();
