@@ -10,8 +10,10 @@
   - Reversal: a move followed by the move back gives dE(move) + dE(back) = 0.
 
 Tolerances: FP64 (the oracle and the plain engine) 1e-9 relative on totals (each side is within
-1e-10 of the reference's arithmetic) and 1e-8 kcal/mol on dE; mixed 2e-6 relative on totals and
-2e-4 kcal/mol on dE (twice the per-result mixed tolerances, 1e-6 relative and 1e-4 kcal/mol).
+1e-10 of the reference's arithmetic) and 1e-8 kcal/mol on dE; mixed 3e-6 relative on totals and
+2e-4 kcal/mol on dE (each side is within the per-result mixed tolerances of FP64, 1e-6 relative
+and 1e-4 kcal/mol, so their difference is within twice those; 3e-6 leaves room for the division
+by the mixed total instead of the FP64 one).
 """
 import numpy as np
 import pytest
@@ -21,7 +23,7 @@ import oracle as orc
 
 KCAL = 418.4
 FP64_REL = 1e-9
-MIX_REL = 2e-6
+MIX_REL = 3e-6
 FP64_DE = 1e-8 * KCAL
 MIX_DE = 2e-4 * KCAL
 SHIFT = np.array([3.1, -7.3, 11.9])
