@@ -45,12 +45,14 @@ int mcg_device_count(void) {
 int mcg_create(const mcg_system_desc* desc, mcg_system** out) {
     if (!out) return fail(MCG_EINVAL, "null output handle");
     *out = nullptr;
-    if (mcg_device_count() <= 0) return fail(MCG_ECUDA, "no CUDA device available");
-    std::unique_ptr<mcg_system> s(new (std::nothrow) mcg_system);
-    if (!s) return fail(MCG_ECUDA, "host allocation failed");
+    // the description is validated on the host first: an invalid one is MCG_EINVAL with or
+    // without a device
     HostSystem hs;
     int rc = build_host_system(desc, hs);
     if (rc) return rc;
+    if (mcg_device_count() <= 0) return fail(MCG_ECUDA, "no CUDA device available");
+    std::unique_ptr<mcg_system> s(new (std::nothrow) mcg_system);
+    if (!s) return fail(MCG_ECUDA, "host allocation failed");
     rc = s->eng.init(hs);
     if (rc) return rc;
     *out = s.release();

@@ -30,10 +30,13 @@ def test_exports_every_declared_symbol():
 def test_abi_version_and_errors_without_device():
     L = native.lib()
     assert L.mcg_abi_version() == 1
+    h = C.c_void_p()
+    # an invalid description is rejected on the host, with or without a device
+    d, keep = native.make_desc(systems.argon_fcc(2))          # 11.45 A box: cutoff beyond half the box
+    assert L.mcg_create(C.byref(d), C.byref(h)) == native.MCG_EINVAL
+    assert b"half the box" in L.mcg_last_error()
     if L.mcg_device_count() == 0:
-        s = systems.argon_fcc(2)
-        d, keep = native.make_desc(s)
-        h = C.c_void_p()
+        d, keep = native.make_desc(systems.argon_fcc(6))
         rc = L.mcg_create(C.byref(d), C.byref(h))
         assert rc == native.MCG_ECUDA
         assert b"no CUDA device" in L.mcg_last_error()
