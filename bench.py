@@ -342,7 +342,8 @@ def run_ours(args):
         line = {
             "metric": "accepted MC moves/s", "value": value, "unit": "moves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 pair terms, f64 sums and acceptance, 64-bit fixed-point coordinates",
+            "vs_baseline": None, "dtype": "f32",
+            "precision": "f32 pair terms, f64 sums and acceptance, 64-bit fixed-point coordinates",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "chains": args.chains, "atoms_per_gpu": natoms,
                        "molecules_per_sweep_per_gpu": int(natoms // 3),
