@@ -156,3 +156,50 @@ def test_engine_move_then_move_back_cancels(_engine, prec):
         d2 = ff.delta_e(idx, xyz[idx])
         ff.commit()
         assert abs(d1 + d2) <= tol, (prec, d1, d2)
+
+
+def test_pruning_criterion_keeps_every_pair_within_cutoff(_oracle_built):
+    """The mixed pair kernel's row pruning rule, checked on the oracle's Verlet list in FP64.
+
+    Rows pruned at positions P0 to the pairs within rc + b keep every list pair that is within rc
+    at P1, as long as no atom moved more than b/2 between P0 and P1 (triangle inequality through
+    the minimum image).  Moves of up to b/2 - 1e-3 A (the engine's re-prune limit) are tried in
+    the directions that close pairs fastest, each atom towards the centre of the box."""
+    s = goldens.system("water4096", "switch")
+    o = orc.Oracle(s, moves=False)
+    L = np.asarray(s.box, np.float64)
+    rc, b = s.cutoff, 0.5
+    xyz0 = s.coords()
+    rows = o.verlet_rows()
+    i = np.repeat(np.arange(s.natom), [len(r) for r in rows])
+    j = np.concatenate(rows)
+
+    def dist(xyz):
+        d = xyz[j] - xyz[i]
+        d -= L * np.round(d / L)
+        return np.sqrt((d * d).sum(1))
+
+    kept = dist(xyz0) <= rc + b
+    assert kept.sum() < len(j)                         # pruning removes entries
+    rng = np.random.default_rng(11)
+    lim = 0.5 * b - 1e-3
+    for trial in range(3):
+        if trial == 0:                                 # every atom towards the box centre
+            v = -xyz0 / np.linalg.norm(xyz0, axis=1, keepdims=True)
+        else:                                          # random directions
+            v = rng.normal(size=xyz0.shape)
+            v /= np.linalg.norm(v, axis=1, keepdims=True)
+        xyz1 = xyz0 + lim * v
+        inside = dist(xyz1) <= rc
+        assert not np.any(inside & ~kept), int(np.sum(inside & ~kept))
+    # and the limit is needed: two atoms of a pruned-out pair, each moved 0.35 A (more than b/2)
+    # towards the other, come within rc, so rows this old must be pruned again
+    d0 = dist(xyz0)
+    k = int(np.flatnonzero((~kept) & (d0 <= rc + b + 0.2))[0])
+    dv = xyz0[j[k]] - xyz0[i[k]]
+    dv -= L * np.round(dv / L)
+    u = dv / np.linalg.norm(dv)
+    xyz1 = xyz0.copy()
+    xyz1[i[k]] += 0.35 * u
+    xyz1[j[k]] -= 0.35 * u
+    assert dist(xyz1)[k] <= rc and not kept[k]
