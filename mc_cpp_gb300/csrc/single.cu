@@ -417,26 +417,7 @@ __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, P
     block_reduce2(sel, svd, part + 2 * blockIdx.x);
 }
 
-// Mixed-precision switched energy over the half list for periodic boxes: the pair kernel.  A warp
-// per row i, lanes over its j > i entries.  One 16-byte load per list entry (the fixed-point
-// position: exact minimum-image displacement by 32-bit wrap-around, scaled by a float-float box
-// length) and one 16-byte load per pair inside the cutoff (charge as float-float, eps, sig).
-// The row's sums are factored: each lane sums q_j g (g = S(r^2)/r, float-float by TwoSum) and
-// eps_j l S (l = x^12 - x^6, FP32) over its entries of row i, and at the row's end multiplies them
-// by q_i (float-float) and eps_i into float-float totals; no FP64 arithmetic until the block sum.
-// The switch is formed unscaled as A^2 B with A = rc^2 - u, B = 2u + rc^2 - 3 ron^2 and u = r^2
-// raised to ron^2; inv_f1 = 1 / (that FP32 polynomial at ron^2) scales the block sums, so inner
-// pairs have S = 1 exactly.  Same terms as mixed_pair (unscaled, k_finalize scales).
-// U list entries in flight per lane; MINB resident CTAs per SM requested from the register
-// allocator (occupancy against registers); the engine times the variants once and keeps the fastest.
-// Both gathers of an entry (position and parameters) are issued together, unconditionally: over
-// pruned rows ~88% of the entries lie within rc, so the parameter load is rarely wasted and the
-// two dependent gather phases become one.  A padded slot (past the row's end) reads atom i itself
-// and is masked by its index.  Slots wholly past the row's end are skipped by a warp-uniform test.
-// ISO (cubic boxes): r^2 is summed in fixed-point units (exact integer differences converted to
-// FP32) and scaled once by the float-float square of the unit length, two instructions per entry
-// instead of a float-float scale per axis.
-// One batch of U entries per lane of row i (the pair terms of the kernel below).
+// One batch of U entries per lane of row i: the pair terms of k_energy_list_mix.
 template <int U, bool ISO, bool TYPED>
 __device__ __forceinline__ void mix_batch(const int (&j)[U], const uint4 (&fj)[U], float4 (&pj)[U], const float4* s_cls,
                                           int i, uint4 fi, float4 pi, int k0, int m, float Ls0, float Ls1, float Ls2,
@@ -489,6 +470,25 @@ __device__ __forceinline__ void mix_row_flush(float4 pi, float ch, float cl, flo
     VL += er;
 }
 
+// Mixed-precision switched energy over the half list for periodic boxes: the pair kernel.  A warp
+// per row i, lanes over its j > i entries.  One 16-byte load per list entry (the fixed-point
+// position: exact minimum-image displacement by 32-bit wrap-around, scaled by a float-float box
+// length) and one 16-byte load per pair inside the cutoff (charge as float-float, eps, sig).
+// The row's sums are factored: each lane sums q_j g (g = S(r^2)/r, float-float by TwoSum) and
+// eps_j l S (l = x^12 - x^6, FP32) over its entries of row i, and at the row's end multiplies them
+// by q_i (float-float) and eps_i into float-float totals; no FP64 arithmetic until the block sum.
+// The switch is formed unscaled as A^2 B with A = rc^2 - u, B = 2u + rc^2 - 3 ron^2 and u = r^2
+// raised to ron^2; inv_f1 = 1 / (that FP32 polynomial at ron^2) scales the block sums, so inner
+// pairs have S = 1 exactly.  Same terms as mixed_pair (unscaled, k_finalize scales).
+// U list entries in flight per lane; MINB resident CTAs per SM requested from the register
+// allocator (occupancy against registers); the engine times the variants once and keeps the fastest.
+// Without the class table (TYPED below), both gathers of an entry (position and parameters) are
+// issued together, unconditionally: over pruned rows ~88% of the entries lie within rc, so the
+// parameter load is rarely wasted and the two dependent gather phases become one.  A padded slot (past the row's end) reads atom i itself
+// and is masked by its index.  Slots wholly past the row's end are skipped by a warp-uniform test.
+// ISO (cubic boxes): r^2 is summed in fixed-point units (exact integer differences converted to
+// FP32) and scaled once by the float-float square of the unit length, two instructions per entry
+// instead of a float-float scale per axis.
 // TYPED: the atoms' parameters come from a table of the system's distinct (q, eps, sig) classes
 // in shared memory, indexed by the class the fixed-point mirror carries in w, so an entry costs
 // one global gather (its position) instead of two.
