@@ -1,0 +1,125 @@
+"""A float32 restatement of the mixed pair kernel's arithmetic (numpy), against the FP64 oracle.
+
+k_energy_list_mix (mc_cpp_gb300/csrc/single.cu) forms each displacement exactly as a 32-bit
+fixed-point difference (box = 2^32 units, wrap-around = minimum image), sums r^2 in FP32 units and
+scales it by the float-float square of the unit length (cubic boxes), and evaluates the switched
+Coulomb and LJ terms in FP32: the switch as (rc^2 - u)^2 (2u + rc^2 - 3 ron^2) with
+u = max(r^2, ron^2), normalised once by its value at ron^2; per lane and row, q_j S/r summed in
+float-float and eps_j (x^12 - x^6) S summed in FP32 (lane = entry index mod 32), multiplied by
+q_i and eps_i at the row's end.  This restatement runs the same arithmetic in numpy float32 (an FMA
+is emulated as one float64 product-sum rounded once to float32; 1/sqrt as the correctly rounded
+float32 value, within 2 ulp of the kernel's rsqrt + Newton step) over the oracle's Verlet rows.
+
+It checks the design, not the device: the total energy within 1e-6 relative of the oracle's FP64
+value (the tolerance the GPU tests apply to the kernel), each component within 1e-6 of the larger
+of the two.
+"""
+import numpy as np
+import pytest
+
+import goldens
+import oracle as orc
+
+KCALTOIU = 418.4
+CHGCHARMM = 332.0716
+TOL = 1e-6
+f32 = np.float32
+
+
+def _fma(a, b, c):
+    return (a.astype(np.float64) * b.astype(np.float64) + np.asarray(c, np.float64)).astype(f32)
+
+
+def _to_fixed(x, L):
+    u = x / L
+    u = u - np.rint(u)                                       # [-0.5, 0.5]
+    v = np.rint(u * 4294967296.0).astype(np.int64)
+    return (v & 0xFFFFFFFF).astype(np.uint32)
+
+
+def mixed_energy(s, rows, scale_lo=True):
+    """(elec, vdw) in internal units, by the kernel's arithmetic in float32.  scale_lo=False drops
+    the low part of the squared unit length: a float-rounded scale, for the test below."""
+    L = float(s.box[0])
+    assert s.box[0] == s.box[1] == s.box[2], "cubic boxes (the kernel's ISO path)"
+    n = s.natom
+    i = np.repeat(np.arange(n), [len(r) for r in rows])
+    j = np.concatenate(rows).astype(np.int64)
+    k = np.concatenate([np.arange(len(r)) for r in rows])   # entry index within its row
+    fx = [_to_fixed(np.asarray(c, np.float64), L) for c in (s.x, s.y, s.z)]
+    # the unit length L / 2^32 as a float-float pair, and its square as a float-float pair
+    ls = L / 4294967296.0
+    lh = f32(ls)
+    ll = f32(ls - float(lh))
+    l2 = (float(lh) + float(ll)) ** 2
+    L2h = f32(l2)
+    L2l = f32(l2 - float(L2h)) if scale_lo else f32(0.0)
+    u = [(fx[a][j] - fx[a][i]).astype(np.uint32).view(np.int32).astype(f32) for a in range(3)]
+    r2u = _fma(u[0], u[0], _fma(u[1], u[1], u[2] * u[2]))
+    r2 = _fma(r2u, np.full_like(r2u, L2h), r2u * L2l)
+    c2, n2 = f32(s.cutoff * s.cutoff), f32(s.cuton * s.cuton)
+    k3 = f32(c2 - f32(3.0) * n2)
+    inside = r2 <= c2
+    i, j, k, r2 = i[inside], j[inside], k[inside], r2[inside]
+    rinv = (1.0 / np.sqrt(r2.astype(np.float64))).astype(f32)
+    uu = np.maximum(r2, n2)
+    a = (c2 - uu).astype(f32)
+    f = (a * a * _fma(np.full_like(uu, 2.0), uu, k3)).astype(f32)
+    g = (rinv * f).astype(f32)
+    # per-atom parameters as the kernel holds them
+    q = np.asarray(s.q, np.float64)
+    qh = q.astype(f32)
+    ql = (q - qh.astype(np.float64)).astype(f32)
+    eps = np.sqrt(np.asarray(s.eps, np.float64) * KCALTOIU).astype(f32)
+    sig = np.asarray(s.sig, np.float64).astype(f32)
+    # Coulomb: q_j g summed per (row, lane) in float-float (~exact: float64 sums of FP32 products)
+    lane = i * 32 + (k % 32)
+    ce = np.zeros(32 * n, np.float64)
+    np.add.at(ce, lane, (qh[j] * g).astype(np.float64) + (ql[j] * g).astype(np.float64))
+    # LJ: eps_j (x^12 - x^6) f summed per (row, lane) in FP32, in entry order
+    y = ((sig[i] + sig[j]) * rinv).astype(f32)
+    x2 = (y * y).astype(f32)
+    x6 = (x2 * x2 * x2).astype(f32)
+    term = (eps[j] * (_fma(x6, x6, -x6) * f).astype(f32)).astype(f32)
+    ve = np.zeros(32 * n, f32)
+    np.add.at(ve, lane, term)
+    # row flush: q_i (float-float) and eps_i, then the normalisation of the switch
+    rowq = (qh.astype(np.float64) + ql.astype(np.float64))[np.arange(32 * n) // 32]
+    rowe = eps.astype(np.float64)[np.arange(32 * n) // 32]
+    a1 = float(c2 - n2)
+    f1 = float(f32(f32(a1 * a1) * _fma(np.array([2.0], f32), np.array([n2], f32), k3)[0]))
+    elec = float(np.sum(rowq * ce)) / f1
+    vdw = float(np.sum(rowe * ve.astype(np.float64))) / f1
+    return CHGCHARMM * KCALTOIU * elec, 4.0 * vdw
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    orc.build()
+
+
+@pytest.mark.parametrize("name", ["argon864", "water512", "water4096"])
+def test_mixed_arithmetic_within_tolerance_of_fp64(name):
+    s = goldens.system(name, "switch")
+    o = orc.Oracle(s, moves=False)
+    want = o.energy()
+    elec, vdw = mixed_energy(s, o.verlet_rows())
+    scale = max(1.0, abs(want[3]), abs(want[4]))
+    assert abs(elec - want[3]) <= TOL * scale, (elec, want[3])
+    assert abs(vdw - want[4]) <= TOL * scale, (vdw, want[4])
+    assert abs((elec + vdw) - (want[3] + want[4])) <= TOL * max(1.0, abs(want[3] + want[4])), (elec + vdw, want)
+
+
+def test_float_float_scale_removes_the_scale_bias():
+    """Why the unit length is a float-float pair: rounded to one float, the scale stretches every
+    distance by the same factor, and the unrelaxed box's virial turns that into a total-energy
+    error several times larger (water, 12,288 atoms: ~8e-8 with the pair, ~7e-7 without)."""
+    s = goldens.system("water4096", "switch")
+    o = orc.Oracle(s, moves=False)
+    want = o.energy()
+    rows = o.verlet_rows()
+    tot = want[3] + want[4]
+    err_ff = abs(sum(mixed_energy(s, rows)) - tot) / abs(tot)
+    err_f = abs(sum(mixed_energy(s, rows, scale_lo=False)) - tot) / abs(tot)
+    assert err_ff <= 2e-7, err_ff
+    assert err_f >= 3.0 * err_ff, (err_f, err_ff)
