@@ -123,3 +123,101 @@ def test_float_float_scale_removes_the_scale_bias():
     err_f = abs(sum(mixed_energy(s, rows, scale_lo=False)) - tot) / abs(tot)
     assert err_ff <= 2e-7, err_ff
     assert err_f >= 3.0 * err_ff, (err_f, err_ff)
+
+
+def _pair_delta(do, m, qk_sw, e4_sw, ss, c2, n2, k3):
+    """mixed_pair_delta_clamped (mc_cpp_gb300/csrc/pair_math.cuh) in numpy float32: the energy
+    change of pairs whose first atom moves by m (d_new = d_old - m), Coulomb differenced
+    analytically.  Arrays of shape (npairs, 3) / (npairs,)."""
+    dn = (do - m).astype(f32)
+    uo = _fma(do[:, 0], do[:, 0], _fma(do[:, 1], do[:, 1], do[:, 2] * do[:, 2]))
+    un = _fma(dn[:, 0], dn[:, 0], _fma(dn[:, 1], dn[:, 1], dn[:, 2] * dn[:, 2]))
+    ro = (1.0 / np.sqrt(uo.astype(np.float64))).astype(f32)
+    rn = (1.0 / np.sqrt(un.astype(np.float64))).astype(f32)
+    ua = np.minimum(np.maximum(uo, n2), c2)
+    ub = np.minimum(np.maximum(un, n2), c2)
+    Aa, Ab = (c2 - ua).astype(f32), (c2 - ub).astype(f32)
+    two = np.full_like(ua, 2.0)
+    Ba, Bb = _fma(two, ua, k3), _fma(two, ub, k3)
+    po, pn = (Aa * Aa * Ba).astype(f32), (Ab * Ab * Bb).astype(f32)
+    xo, xn = (ss * (ro * ro)).astype(f32), (ss * (rn * rn)).astype(f32)
+    xo3, xn3 = (xo * xo * xo).astype(f32), (xn * xn * xn).astype(f32)
+    d_lj = (e4_sw * _fma(_fma(xn3, xn3, -xn3), pn, -(_fma(xo3, xo3, -xo3) * po))).astype(f32)
+    s = (do + dn).astype(f32)
+    du = -_fma(m[:, 0], s[:, 0], _fma(m[:, 1], s[:, 1], m[:, 2] * s[:, 2]))
+    p = (ro * rn).astype(f32)
+    dinv = ((-du * p * p).astype(f32) / (ro + rn).astype(f32)).astype(f32)
+    dd = np.where((ua == uo) & (ub == un), du, (ub - ua).astype(f32))
+    dp = (dd * _fma((two * Aa).astype(f32), Aa, -((Aa + Ab) * Bb).astype(f32))).astype(f32)
+    return _fma(qk_sw, _fma(dinv, pn, (ro * dp).astype(f32)), d_lj)
+
+
+def _pair_direct(d, qk_sw, e4_sw, ss, c2, n2, k3):
+    """The same pair energy evaluated directly in float32 (for the comparison below)."""
+    u = _fma(d[:, 0], d[:, 0], _fma(d[:, 1], d[:, 1], d[:, 2] * d[:, 2]))
+    r = (1.0 / np.sqrt(u.astype(np.float64))).astype(f32)
+    uc = np.minimum(np.maximum(u, n2), c2)
+    A = (c2 - uc).astype(f32)
+    P = (A * A * _fma(np.full_like(uc, 2.0), uc, k3)).astype(f32)
+    x = (ss * (r * r)).astype(f32)
+    x3 = (x * x * x).astype(f32)
+    return (qk_sw * (r * P).astype(f32) + e4_sw * (_fma(x3, x3, -x3) * P).astype(f32)).astype(f32)
+
+
+def test_mixed_delta_e_within_tolerance_and_analytic_coulomb_difference():
+    """Residue moves of the 12,288-atom water box (translations <= 0.15 A, rotations <= 15 deg
+    about the oxygen): the float32 dE over the moved atoms' Verlet partners against the oracle's
+    FP64 dE.  The analytic Coulomb difference keeps every dE within 1e-4 kcal/mol; the pair
+    energies differenced directly in float32 would err several times more."""
+    s = goldens.system("water4096", "switch")
+    o = orc.Oracle(s, moves=False)
+    rows = o.verlet_rows()
+    pi = np.repeat(np.arange(s.natom), [len(r) for r in rows])
+    pj = np.concatenate(rows).astype(np.int64)
+    L = float(s.box[0])
+    fx = np.stack([_to_fixed(np.asarray(c, np.float64), L) for c in (s.x, s.y, s.z)], 1)
+    ls = L / 4294967296.0
+    lh = f32(ls)
+    ll = f32(ls - float(lh))
+    c2, n2 = f32(s.cutoff * s.cutoff), f32(s.cuton * s.cuton)
+    k3 = f32(c2 - f32(3.0) * n2)
+    sw2 = f32(1.0 / (float(s.cutoff) ** 2 - float(s.cuton) ** 2) ** 3)
+    q = np.asarray(s.q, np.float64)
+    eps = np.sqrt(np.asarray(s.eps, np.float64) * KCALTOIU).astype(f32)
+    sig = np.asarray(s.sig, np.float64).astype(f32)
+    xyz = s.coords()
+    rng = np.random.default_rng(21)
+    worst_a, worst_d = 0.0, 0.0
+    for t in range(24):
+        r = int(rng.integers(0, 4096))
+        idx = np.arange(3 * r, 3 * r + 3)
+        if t % 2 == 0:
+            v = rng.normal(size=3)
+            new = xyz[idx] + 0.15 * rng.uniform() ** (1 / 3) * v / np.linalg.norm(v)
+        else:
+            ax = rng.normal(size=3)
+            ax /= np.linalg.norm(ax)
+            th = np.radians(rng.uniform(-15.0, 15.0))
+            K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+            R = np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+            new = xyz[idx[0]] + (xyz[idx] - xyz[idx[0]]) @ R.T
+        want = o.delta_e(idx, new)
+        da, dd = 0.0, 0.0
+        for k, a in enumerate(idx):
+            sel = (pi == a) | (pj == a)
+            other = np.where(pi[sel] == a, pj[sel], pi[sel])
+            other = other[(other < idx[0]) | (other > idx[-1])]
+            f = (fx[other].astype(np.int64) - fx[a].astype(np.int64)).astype(np.uint32).view(np.int32).astype(f32)
+            do = _fma(f, np.full_like(f, lh), f * ll)                       # fixed_delta, per axis
+            m = np.broadcast_to((new[k] - xyz[a]).astype(f32), do.shape).astype(f32)
+            qk_sw = (CHGCHARMM * KCALTOIU * q[a] * q[other]).astype(f32) * sw2
+            e4_sw = (f32(4.0) * eps[a] * eps[other]).astype(f32) * sw2
+            ss = ((sig[a] + sig[other]) ** 2).astype(f32)
+            da += float(np.sum(_pair_delta(do, m, qk_sw, e4_sw, ss, c2, n2, k3).astype(np.float64)))
+            dn = (do - m).astype(f32)
+            dd += float(np.sum(_pair_direct(dn, qk_sw, e4_sw, ss, c2, n2, k3).astype(np.float64)
+                               - _pair_direct(do, qk_sw, e4_sw, ss, c2, n2, k3).astype(np.float64)))
+        worst_a = max(worst_a, abs(da - want) / KCALTOIU)
+        worst_d = max(worst_d, abs(dd - want) / KCALTOIU)
+    assert worst_a <= 1e-4, worst_a
+    assert worst_d >= 3.0 * worst_a, (worst_d, worst_a)
