@@ -35,7 +35,8 @@ def _worker(rank, world, port, out):
 
 def test_two_gloo_ranks_shard_chains_and_aggregate():
     world = 2
-    with mp.Manager() as m:
+    # spawned, not forked: earlier tests in this process may have started thread pools (OpenMP)
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
