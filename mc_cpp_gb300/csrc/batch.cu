@@ -1728,6 +1728,16 @@ int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_
 static std::mutex g_tune_mu;
 static std::map<std::string, mcg_batch_tuning> g_tune_cache;
 
+// A cached shape is used only if mcg_batch_create would accept it as options: a damaged or
+// hand-edited cache line is skipped (and the shapes timed again), never launched.
+static bool tuning_valid(const mcg_batch_tuning& v) {
+    const bool th = v.threads_per_chain == 128 || v.threads_per_chain == 256 || v.threads_per_chain == 512;
+    const bool cp = v.ctas_per_sm >= 1 && v.ctas_per_sm <= 8;
+    const bool sp = v.speculation >= 0 && v.speculation <= KMAX && (v.speculation & (v.speculation - 1)) == 0;
+    const bool cl = v.clusters == 0 || v.clusters == 1;
+    return th && cp && sp && cl && std::isfinite(v.ms_per_sweep);
+}
+
 static bool tune_lookup(const std::string& sig, mcg_batch_tuning* t) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(sig);
@@ -1741,7 +1751,7 @@ static bool tune_lookup(const std::string& sig, mcg_batch_tuning* t) {
     bool found = false;
     while (fscanf(f, "%255s %d %d %d %d %f", key, &v.threads_per_chain, &v.ctas_per_sm, &v.speculation, &v.clusters,
                   &v.ms_per_sweep) == 6)
-        if (sig == key) { *t = v; found = true; }
+        if (sig == key && tuning_valid(v)) { *t = v; found = true; }
     fclose(f);
     if (found) g_tune_cache[sig] = *t;
     return found;
