@@ -23,7 +23,7 @@ INC = os.path.join(ROOT, "include")
 @pytest.fixture(scope="module")
 def lib_dir():
     build.build()
-    return os.path.dirname(native.LIB_PATH) if hasattr(native, "LIB_PATH") else os.path.join(ROOT, "mc_cpp_gb300", "_lib")
+    return os.path.dirname(native.LIB_PATH)
 
 
 def test_header_compiles_as_cxx11(tmp_path):
