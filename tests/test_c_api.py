@@ -4,7 +4,8 @@ include/mcg.h is the drop-in boundary, so it must compile as C99 with every warn
 link against libmcgpu.so alone.  tests/c_api/host_calls.c makes the calls of the integration
 notes: the MDBAS reader, the exclusion and 1-4 builder, null-argument rejection, and the device
 calls, which without a GPU must fail with MCG_ECUDA and an error text.  The header must also
-compile as C++11, the standard mc_cpp itself is built with.
+compile as C++11, the standard mc_cpp itself is built with.  The Fortran/C interface header
+(include/charmmene_gpu.h) must compile as C and its seven symbols link from libcharmmene_gpu.so.
 """
 import ctypes as C
 import os
@@ -33,6 +34,23 @@ def test_header_compiles_as_cxx11(tmp_path):
     src.write_text('#include "mcg.h"\nint main() { mcg_system_desc d = {}; return d.natom; }\n')
     r = subprocess.run(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + INC, str(src),
                         "-o", str(tmp_path / "h")], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+
+
+def test_fortran_interface_header_compiles_as_c_and_links(lib_dir, tmp_path):
+    """include/charmmene_gpu.h from C: the seven symbols resolve in libcharmmene_gpu.so."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "f.c"
+    src.write_text('#include "charmmene_gpu.h"\n'
+                   'int main(void) {\n'
+                   '    void (*fns[7])(void) = {(void (*)(void))set_pbc_, (void (*)(void))set_ens_,\n'
+                   '        (void (*)(void))set_ff_and_cor_, (void (*)(void))get_energy_, (void (*)(void))set_coords_,\n'
+                   '        (void (*)(void))get_mass_, (void (*)(void))clean_};\n'
+                   '    return fns[0] == 0;\n}\n')
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I" + INC, str(src), "-o",
+                        str(tmp_path / "f"), "-L" + lib_dir, "-lcharmmene_gpu", "-Wl,-rpath," + lib_dir],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
 
 
