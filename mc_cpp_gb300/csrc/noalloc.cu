@@ -13,6 +13,12 @@
 // launches before they are read, so nothing has to start at zero.  All calls share the array:
 // calls that overlap on the GPU (different streams, or different host threads on one device)
 // race on it and must be serialised by the caller.
+//
+// The neighbour rows come from the caller, not from this library, so the kernel trusts none of
+// their contents: a row count above the row capacity is clamped to it and a partner index outside
+// [0, natom) is skipped, so a damaged list can give a wrong energy but never an access outside the
+// caller's buffers.
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -40,9 +46,10 @@ __global__ void __launch_bounds__(256) k_noalloc_energy(const double4_32a* __res
         const double4_32a pi = pq[i];
         const double2 ai = es[i];
         const int* row = nbr + (size_t)i * cap;
-        const int m = nup[i];
+        const int m = min(nup[i], cap);
         for (int k = lane; k < m; k += 32) {
             const int j = row[k];
+            if ((unsigned)j >= (unsigned)n) continue;   // not an atom of this system
             const double4_32a pj = pq[j];
             const double r2 = ref64_dist2(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, pbc);
             if (r2 > cut.c2) continue;
@@ -85,14 +92,20 @@ __global__ void k_noalloc_finalize(const double* __restrict__ partials, int nblo
     }
 }
 
-// Device address of the static scratch, looked up once per device with that device current.
+// Device address of the static scratch, looked up once per device with that device current and
+// kept for the process.  The table is guarded by a mutex, so host threads may call concurrently.
+// A cudaDeviceReset() of the device unloads the module and makes the kept address stale; callers
+// that reset a device must not call this entry point on it afterwards.
 static double* noalloc_scratch(int dev, int* rc) {
+    static std::mutex mu;
     static double* addr[64] = {nullptr};
     if (dev < 0 || dev >= 64) { *rc = fail(MCG_ENOTSUP, "device ordinal above 63"); return nullptr; }
+    std::lock_guard<std::mutex> lock(mu);
     if (!addr[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
         if (e != cudaSuccess) {
+            cudaGetLastError();   // this call's own error: not left pending for the caller's next call
             *rc = fail(MCG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             return nullptr;
         }
@@ -139,9 +152,21 @@ extern "C" int mcg_energy_switch_fp64_noalloc(int natom, const double* pq, const
     cut.c2f = (float)cut.c2; cut.n2f = (float)cut.n2; cut.sw2f = (float)cut.sw2;
     cudaStream_t st = (cudaStream_t)stream;
     const int nblocks = (natom + NOALLOC_ROWS_PER_BLOCK - 1) / NOALLOC_ROWS_PER_BLOCK;
-    k_noalloc_energy<<<nblocks, 256, 0, st>>>((const double4_32a*)pq, (const double2*)es, nbr, nup, natom, cap, pbc, cut, scratch);
-    k_noalloc_finalize<<<1, 256, 0, st>>>(scratch, nblocks, out);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
+    // launched through cudaLaunchKernel, whose return value is this launch's own status: an error
+    // left by the caller's earlier asynchronous work is neither reported here nor cleared
+    const double4_32a* a_pq = (const double4_32a*)pq;
+    const double2* a_es = (const double2*)es;
+    int a_n = natom, a_cap = cap, a_nb = nblocks;
+    void* args1[] = {(void*)&a_pq, (void*)&a_es, (void*)&nbr, (void*)&nup, (void*)&a_n, (void*)&a_cap, (void*)&pbc,
+                     (void*)&cut, (void*)&scratch};
+    cudaError_t e = cudaLaunchKernel((const void*)k_noalloc_energy, dim3(nblocks), dim3(256), args1, 0, st);
+    if (e == cudaSuccess) {
+        void* args2[] = {(void*)&scratch, (void*)&a_nb, (void*)&out};
+        e = cudaLaunchKernel((const void*)k_noalloc_finalize, dim3(1), dim3(256), args2, 0, st);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // the failed launch's error is reported here, not left for the next call
+        return fail(MCG_ECUDA, std::string("launch: ") + cudaGetErrorString(e));
+    }
     return MCG_OK;
 }
