@@ -1,7 +1,7 @@
 # Builds the unmodified FHedin/mc_cpp reference (scalar FField_MDBAS path) from the sources
 # where they lie, plus this repository's own probe driver linked against those objects.
 #
-#   make -f oracle/ref.mk REF=/root/reference        (run from the repository root)
+#   make -f oracle/ref.mk REF=<directory of the mc_cpp sources>    (run from the repository root)
 #
 # Outputs go to oracle/_ref/ only (git-ignored).  Nothing here is shipped or measured as the
 # product: the probe is test infrastructure used to pin the oracle restatement and to generate
@@ -18,7 +18,9 @@
 #  * -std=c++11 keeps GCC in ISO mode, so no FMA contraction (-ffp-contract=off is implied); the
 #    restatement in oracle/mc_oracle.cpp is built the same way so FP64 sums agree bit for bit.
 
-REF      ?= /root/reference
+ifeq ($(strip $(REF)),)
+$(error REF must name the directory of the FHedin/mc_cpp sources: make -f oracle/ref.mk REF=<dir>)
+endif
 OUT      := oracle/_ref
 CXX      ?= g++
 CXXFLAGS := -std=c++11 -O3 -ffp-contract=off -fopenmp -w -include cmath -include limits \

@@ -2,7 +2,8 @@
 
 Run from the repository root in a container that has the reference sources:
 
-    python tests/golden/make_golden.py --ref /root/reference
+    python tests/golden/make_golden.py --ref <path of the mc_cpp sources>
+    python tests/golden/make_golden.py --ref <path> --only-argon-long   # the 1e5-move trace alone
 
 It builds the reference and the probe (oracle/ref.mk), converts the reference's own example
 inputs (test/*.xml) into compact .npz fixtures, and records what the reference computes on them
@@ -11,7 +12,9 @@ and on the seeded synthetic systems of mc_cpp_gb300.systems:
 * golden.json   energies (10 components, internal units, 17 significant digits), Verlet and
                 exclusion row digests and sizes, 1-4 pair lists, coordinate digests of the
                 synthetic systems, MC summaries;
-* trace_*.npy   per-step Metropolis traces (12 doubles per step, see oracle/ref_probe.cpp).
+* trace_*.npy   per-step Metropolis traces (12 doubles per step, see oracle/ref_probe.cpp);
+* argon864_long.npz  the 1e5-move argon run (seed 1234) in compact form: per step the moved atom,
+                the reference's dE (iu), its alpha draw (-1 when none was drawn) and the decision.
 
 Nothing at test time reads the reference: tests load only these files.
 """
@@ -103,12 +106,37 @@ def record_mc(s, name, tmp, nsteps, seed):
                 seconds=res["seconds"])
 
 
+def record_mc_long(s, name, tmp, nsteps, seed):
+    """A long single-move-type run kept compact: moved atom, dE, alpha and decision per step."""
+    xml = write_inputs(s, tmp, name + "_mc", None)
+    tr = os.path.join(tmp, "trace_long.bin")
+    res = probe("mc", xml, str(nsteps), str(seed), tr, cwd=tmp)
+    t = np.fromfile(tr, np.float64).reshape(-1, 12)
+    assert len(t) == nsteps and (t[:, 1] == 0).all()
+    np.savez_compressed(os.path.join(GOLD, "%s.npz" % name), imvatm=t[:, 2].astype(np.int32), de=t[:, 9],
+                        alpha=t[:, 10], accepted=np.packbits(t[:, 11].astype(np.uint8)),
+                        eold=t[::1000, 7], enew=t[::1000, 8])
+    print(name, "mc", res, int(t[:, 11].sum()), flush=True)
+    return dict(nsteps=nsteps, seed=seed, final_etot=res["final_etot"], trials=[nsteps],
+                accepted=[int(t[:, 11].sum())], seconds=res["seconds"])
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="directory of the FHedin/mc_cpp sources")
     ap.add_argument("--skip-large", action="store_true")
+    ap.add_argument("--only-argon-long", action="store_true",
+                    help="record only the 1e5-move argon trace and merge it into golden.json")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "REF=" + a.ref, "-j8"], cwd=ROOT)
+    if a.only_argon_long:
+        with open(os.path.join(GOLD, "golden.json")) as f:
+            gold = json.load(f)
+        with tempfile.TemporaryDirectory() as tmp:
+            gold["mc"]["argon864_long"] = record_mc_long(systems.argon_fcc(), "argon864_long", tmp, 100000, 1234)
+        with open(os.path.join(GOLD, "golden.json"), "w") as f:
+            json.dump(gold, f, indent=1)
+        return
     gold = {"units": "internal (1 kcal/mol = 418.4 iu)", "systems": {}, "mc": {}, "synthetic": {}}
     with tempfile.TemporaryDirectory() as tmp:
         # the reference's own example inputs
@@ -140,6 +168,7 @@ def main():
         gold["mc"]["argon864"] = record_mc(syn["argon864"], "argon864", tmp, 2000, 1234)
         gold["mc"]["water512"] = record_mc(syn["water512"], "water512", tmp, 300, 99)
         gold["mc"]["peptide"] = record_mc(syn["peptide"], "peptide", tmp, 30, 5)
+        gold["mc"]["argon864_long"] = record_mc_long(syn["argon864"], "argon864_long", tmp, 100000, 1234)
     with open(os.path.join(GOLD, "golden.json"), "w") as f:
         json.dump(gold, f, indent=1)
 
