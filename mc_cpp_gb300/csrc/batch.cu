@@ -383,6 +383,17 @@ struct MoveRec {
     uint32_t ahi, alo;                   // Philox words of alpha in (0, 1] (u01d_open0)
 };
 
+// Per-move record of a logged sweep (mcg_batch_sweep_logged): the layout of mcg_batch_move, with
+// the proposed positions as raw 64-bit masters (the host converts them to Angstrom in place).
+struct MoveLogDev {
+    double de;
+    int res;
+    int flags;                           // bit 0 rotation, bit 1 accepted
+    uint32_t ahi, alo;
+    unsigned long long pos[MAX_APR][3];
+};
+static_assert(sizeof(MoveLogDev) == sizeof(mcg_batch_move), "record layout of mcg_batch_move");
+
 // Master-unit increment for a displacement d (Angstrom): d * 2^64 / L as a 64-bit integer, formed
 // in FP32 + integer arithmetic (v = d * 2^32 / L; integer part -> high word, fraction -> low word).
 __device__ __forceinline__ unsigned long long master_step(float d, float tofix32) {
@@ -420,7 +431,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
-                                                       const int* __restrict__ cta_chains, int nchains) {
+                                                       const int* __restrict__ cta_chains, int nchains,
+                                                       MoveLogDev* mlog) {
     namespace cg = cooperative_groups;
     constexpr int NW = NT / 32;
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
@@ -764,6 +776,22 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 const int a = Q[grp].res * apr + lane;
                 Mc[a] = make_ulonglong4_32a(Q[grp].mn[lane][0], Q[grp].mn[lane][1], Q[grp].mn[lane][2], 0ull);
                 Fc[a] = Q[grp].fn[lane];
+            }
+            if (mlog && rank == 0 && warp == 0) {   // logged sweep: the standing moves in chain order
+                MoveLogDev* lg = mlog + C.res0 + mv;
+                const int g = lane / apr, j = lane - g * apr;
+                if (g < ng) {
+                    lg[g].pos[j][0] = Q[g].mn[j][0];
+                    lg[g].pos[j][1] = Q[g].mn[j][1];
+                    lg[g].pos[j][2] = Q[g].mn[j][2];
+                }
+                if (lane < ng) {
+                    lg[lane].de = (double)deh + (double)del;
+                    lg[lane].res = Q[lane].res;
+                    lg[lane].flags = Q[lane].rot | (int)(((accmask >> lane) & 1u) << 1);
+                    lg[lane].ahi = Q[lane].ahi;
+                    lg[lane].alo = Q[lane].alo;
+                }
             }
             if (grp < ng) npairs += np;
             if (adjust) {   // dmax adjustment after the standing moves, in move order (every thread alike)
@@ -1133,6 +1161,8 @@ struct mcg_batch {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string signature;        // workload + device key of the autotuner cache
     double* d_xyz = nullptr;      // staging for host-buffer runs (3 x natoms)
+    MoveLogDev* d_mlog = nullptr; // per-move records the next direct sweep launch writes (null: none)
+    MoveLogDev* d_log = nullptr;  // their buffer (one record per residue of all chains), on first use
     double* d_eres = nullptr;     // per-residue energy shares (mixed recompute)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int threads = 256;
@@ -1148,7 +1178,7 @@ struct mcg_batch {
         if (d_cl_start) cudaFree(d_cl_start);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
                      d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos, d_item_chain,
-                     d_chain_item0, d_build};
+                     d_chain_item0, d_build, d_log};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -1328,13 +1358,13 @@ struct mcg_batch {
         if (!ncta) return;
         if (threads == 512)
             k_batch_sweep<APR, 512, 1><<<ncta, 512, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
-                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains, d_mlog);
         else if (threads == 128)
             k_batch_sweep<APR, 128, 1><<<ncta, 128, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
-                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains, d_mlog);
         else
             k_batch_sweep<APR, 256, 1><<<ncta, 256, 0, st>>>(d_chains, G, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell,
-                                                             d_gpos, d_state, d_cta_start, d_order, nchains);
+                                                             d_gpos, d_state, d_cta_start, d_order, nchains, d_mlog);
     }
     template <int APR>
     cudaError_t cluster_kernel(cudaStream_t st) {
@@ -1352,7 +1382,7 @@ struct mcg_batch {
         cfg.numAttrs = 1;
         return cudaLaunchKernelEx(&cfg, k_batch_sweep<APR, 512, 2>, (const ChainDev*)d_chains, G, d_M, d_F, d_FB, d_LST,
                                   d_NL, d_gorder, d_gcell, d_gpos, d_state, (const int*)d_cl_start, (const int*)d_cl_order,
-                                  nchains);
+                                  nchains, d_mlog);
     }
     // The cluster chains on a second stream branch, concurrently with the regular CTAs.
     int launch_sweep(cudaStream_t st) {
@@ -1679,6 +1709,34 @@ int mcg_batch_sweep(mcg_batch* b, int nsweeps) {
     if (r) return r;
     for (int s = 0; s < nsweeps; s++) BK(cudaGraphLaunch(b->graph, b->stream));
     b->launches += b->kernels_per_sweep() * (int64_t)nsweeps;
+    return MCG_OK;
+}
+
+int mcg_batch_sweep_logged(mcg_batch* b, mcg_batch_move* moves, int64_t cap) {
+    if (!b || !moves) return fail(MCG_EINVAL, "null argument");
+    if (cap < b->nres) return fail(MCG_EINVAL, "the record buffer needs one entry per residue of all chains");
+    int r;
+    if (!b->d_log && (r = balloc(&b->d_log, (size_t)b->nres))) return r;
+    BK(cudaMemsetAsync(b->d_log, 0, sizeof(MoveLogDev) * b->nres, b->stream));
+    // the sweep graph's kernels with the record pointer set, launched directly (the graph keeps null)
+    b->d_mlog = b->d_log;
+    r = b->launch_build(b->stream, 0);
+    if (!r) r = b->launch_sweep(b->stream);
+    b->d_mlog = nullptr;
+    if (r) return r;
+    b->launches += (b->ncta > 0 ? 1 : 0) + (b->ncl > 0 ? 1 : 0);
+    BK(cudaMemcpyAsync(moves, b->d_log, sizeof(MoveLogDev) * b->nres, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (const ChainDev& C : b->chains)
+        for (int k = 0; k < C.nres; k++) {
+            mcg_batch_move& m = moves[C.res0 + k];
+            for (int j = 0; j < C.apr; j++)
+                for (int t = 0; t < 3; t++) {
+                    uint64_t raw;
+                    std::memcpy(&raw, &m.xyz[j][t], sizeof raw);
+                    m.xyz[j][t] = host_view(raw, C.L[t]);
+                }
+        }
     return MCG_OK;
 }
 

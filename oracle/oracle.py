@@ -72,6 +72,19 @@ def lib():
         L.orc_set_acceptance_units.argtypes = [C.c_void_p, C.c_int]
         L.orc_delta_e.restype = C.c_double
         L.orc_delta_e.argtypes = [C.c_void_p, C.c_int, _i, _d, _d, _d]
+        # batched chain restatement (batch_oracle.cpp)
+        L.orcb_create.restype = C.c_void_p
+        L.orcb_create.argtypes = [C.c_int, C.c_int, _d, _d, _d, _d, C.c_double, C.c_double, C.c_double, C.c_int,
+                                  C.c_uint64, C.c_int, _d, _i, _d, _d]
+        L.orcb_destroy.argtypes = [C.c_void_p]
+        L.orcb_set_coords.argtypes = [C.c_void_p, _d, _d, _d]
+        L.orcb_get_coords.argtypes = [C.c_void_p, _d, _d, _d]
+        L.orcb_set_moves.argtypes = [C.c_void_p, C.c_uint64]
+        L.orcb_get_dmax.argtypes = [C.c_void_p, _d]
+        L.orcb_energy.restype = C.c_double
+        L.orcb_energy.argtypes = [C.c_void_p]
+        L.orcb_follow.argtypes = [C.c_void_p, C.c_int, C.c_void_p, _d]
+        L.orcb_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -207,3 +220,70 @@ class Oracle:
         idx = np.ascontiguousarray(idx, np.int32)
         new_xyz = np.asarray(new_xyz, np.float64)
         return lib().orc_delta_e(self.h, len(idx), _pi(idx), _pd(new_xyz[:, 0]), _pd(new_xyz[:, 1]), _pd(new_xyz[:, 2]))
+
+
+def philox4x32_10(ctr, key) -> tuple:
+    """One block of the batched engine's random stream, from the restatement."""
+    c = np.asarray(ctr, np.uint32)
+    k = np.asarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().orcb_philox(c.ctypes.data, k.ctypes.data, o.ctypes.data)
+    return tuple(int(v) for v in o)
+
+
+class BatchChainOracle:
+    """One batched chain (rigid residues of apr atoms, periodic box) on the FP64 restatement of
+    the batched sweep's moves (batch_oracle.cpp), with the batch's Philox key (seed, chain)."""
+
+    FIELDS = ("match", "pos_err", "de64", "acc64", "acc_rule", "alpha", "thr64", "alpha_match")
+
+    def __init__(self, s, chain: int, seed: int, dmax=(0.15, 15.0), each=(0, 0), target=(50.0, 50.0), cap=None,
+                 acceptance: str = "physical"):
+        apr = int(np.count_nonzero(s.resid == s.resid[0]))
+        box = np.array(s.box if s.pbc_type == "orbic" else (s.box[0],) * 3, np.float64)
+        if cap is None:
+            cap = tuple(2.0 * d if e > 0 else d for d, e in zip(dmax, each))
+        self._arrays = [box, np.asarray(dmax, np.float64), np.asarray(each, np.int32), np.asarray(target, np.float64),
+                        np.asarray(cap, np.float64)]
+        self.n = s.natom
+        self.h = lib().orcb_create(s.natom, apr, _pd(box), _pd(s.q), _pd(s.eps), _pd(s.sig), s.cutoff, s.cuton, s.temp,
+                                   {"reference": 0, "physical": 1}[acceptance], seed, chain,
+                                   _pd(self._arrays[1]), _pi(self._arrays[2]), _pd(self._arrays[3]),
+                                   _pd(self._arrays[4]))
+        if not self.h:
+            raise ValueError("invalid batched chain")
+        self.set_coords(s.coords())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orcb_destroy(self.h)
+            self.h = None
+
+    def set_coords(self, xyz):
+        xyz = np.asarray(xyz, np.float64)
+        lib().orcb_set_coords(self.h, _pd(xyz[:, 0]), _pd(xyz[:, 1]), _pd(xyz[:, 2]))
+
+    def coords(self) -> np.ndarray:
+        x, y, z = (np.zeros(self.n) for _ in range(3))
+        lib().orcb_get_coords(self.h, x.ctypes.data_as(_d), y.ctypes.data_as(_d), z.ctypes.data_as(_d))
+        return np.stack([x, y, z], 1)
+
+    def set_moves(self, moves: int):
+        lib().orcb_set_moves(self.h, int(moves))
+
+    def dmax(self):
+        d = np.zeros(2)
+        lib().orcb_get_dmax(self.h, d.ctypes.data_as(_d))
+        return d
+
+    def energy(self) -> float:
+        return float(lib().orcb_energy(self.h))
+
+    def follow(self, records) -> dict:
+        """Checks and follows a chain's records of one logged sweep (structured array of
+        struct mcg_batch_move); returns per-move arrays named by FIELDS."""
+        rec = np.ascontiguousarray(records)
+        assert rec.dtype.itemsize == 216
+        out = np.zeros((len(rec), 8))
+        lib().orcb_follow(self.h, len(rec), rec.ctypes.data, out.ctypes.data_as(_d))
+        return {k: out[:, i] for i, k in enumerate(self.FIELDS)}

@@ -99,3 +99,38 @@ def test_delta_e_matches_energy_difference():
         o.set_coords(xyz)
         # nonbonded only: bonded terms of a rigidly translated water are unchanged up to rounding
         assert abs(de - (e1 - e0)) < 1e-6 * max(1.0, abs(e0)) * 1e-6 + 1e-6
+
+
+# ---- the batched chain restatement (oracle/batch_oracle.cpp) --------------------------------
+def test_philox_restatement_known_answers():
+    """Philox4x32-10 against the known-answer vectors published with the algorithm (Random123)."""
+    assert orc.philox4x32_10([0, 0, 0, 0], [0, 0]) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
+    assert orc.philox4x32_10([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+    assert orc.philox4x32_10([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == \
+        (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)
+
+
+@pytest.mark.parametrize("name", ["water512", "argon864"])
+def test_batch_restatement_energy_equals_pinned_oracle(name):
+    """The batched restatement's all-pairs FP64 energy equals the pinned oracle's switched energy
+    (every pair within the cutoff is in the Verlet list, so both sum the same pairs)."""
+    s = goldens.system(name, "switch")
+    want = orc.Oracle(s, moves=False).energy()
+    b = orc.BatchChainOracle(s, chain=0, seed=1)
+    assert abs(b.energy() - (want[3] + want[4])) <= 1e-10 * abs(want[3] + want[4])
+
+
+def test_long_argon_fixture_extends_the_short_trace():
+    """The 1e5-move argon fixture and the 2,000-step trace come from the same reference run
+    (seed 1234): their common steps agree exactly."""
+    import os
+    g = goldens.golden()["mc"]["argon864_long"]
+    ref = np.load(os.path.join(goldens.GOLD_DIR, "argon864_long.npz"))
+    short = goldens.trace("argon864")
+    k = len(short)
+    assert g["nsteps"] == 100000 and g["seed"] == goldens.golden()["mc"]["argon864"]["seed"]
+    assert np.array_equal(ref["imvatm"][:k], short[:, 2].astype(np.int32))
+    assert np.array_equal(ref["de"][:k], short[:, 9])
+    assert np.array_equal(ref["alpha"][:k], short[:, 10])
+    assert np.array_equal(np.unpackbits(ref["accepted"])[:k], short[:, 11].astype(np.uint8))
+    assert int(np.unpackbits(ref["accepted"])[:g["nsteps"]].sum()) == g["accepted"][0]
