@@ -22,6 +22,17 @@ graph; 68 flops per pair interaction: distance + minimum image 23, square root a
 Coulomb + LJ 30, accumulation 2, switch polynomial 8) against an FFMA probe measured in the same
 run; `cpu_baseline` = the reference's algorithm (oracle/ port, two full energies per move, one
 chain per host thread) on a bounded stratified sample of the same chains.
+
+N GPUs (`--gpus N`, one rank per GPU; launched with torchrun by the driver, or by this script when
+started without it): the job's chains are the first 256*N of the same seeded generator, split
+over the ranks by a greedy longest-first partition of their atom counts (shard_chains), so every
+rank holds about 256 chains' worth of atoms (weak scaling); chains never exchange data, and the
+only collectives are the timing max and the counter sums.
+
+After the timed region (untimed): one logged sweep checks the mixed-precision dE of every move of a
+sample of chains against the FP64 engine on the same coordinates (`batched_error`), every chain's
+running energy is compared with an FP64 recompute (`max_rel_E_drift`), and the plain FP64 path is
+timed through the drop-in call sequence (`plain_fp64.dropin`).
 """
 from __future__ import annotations
 
@@ -47,10 +58,29 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_chains(rank: int, nchains: int, **kw):
-    """Rank r's own chains (weak scaling: every rank runs nchains independent chains, seeded by r)."""
+CHAIN_SEED = 3
+
+
+def job_specs(nchains: int, world: int, **kw):
+    """(molecules, seed, temperature) of all the job's chains: nchains per GPU (kw: the
+    generator's size and temperature ranges)."""
     from mc_cpp_gb300 import systems
-    return systems.water_chains(nchains=nchains, seed=3 + 7919 * rank, **kw)
+    return systems.water_chain_specs(nchains=nchains * world, seed=CHAIN_SEED, **kw)
+
+
+def rank_chains(rank: int, world: int, nchains: int, **kw):
+    """This rank's shard of the job's chains (shard_chains over their atom counts) and its indices."""
+    from mc_cpp_gb300 import systems
+    specs = job_specs(nchains, world, **kw)
+    mine = systems.shard_chains([3 * n for n, _, _ in specs], world)[rank]
+    return systems.water_chains(nchains=nchains * world, seed=CHAIN_SEED, only=mine, **kw), mine
+
+
+def workload_config(args, world: int):
+    """The `config` of both arms' lines (the same dict, so the records compare)."""
+    return {"workload": WORKLOAD, "chains_per_gpu": args.chains, "chains_total": args.chains * world,
+            "l2": "no flush: per-sweep working set (1.5 GB lists, 134 MB coordinates per GPU) > 129 MB L2",
+            "acceptance": "physical", "parallelism": "chains sharded over GPUs by atoms (shard_chains), weak scaling"}
 
 
 class Reducer:
@@ -140,23 +170,26 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU baseline (reference algorithm)
-def cpu_sample(chains, budget_s: float, threads: int, seed: int = 17):
+def cpu_sample(specs, budget_s: float, threads: int, seed: int = 17):
     """Runs the reference's Metropolis algorithm (two full getE per move, oracle/ port) on a
-    stratified sample of the chains, one chain per host thread, and estimates the accepted-moves/s
-    rate of the whole workload on `threads` cores.  Returns (rate, description, cores)."""
+    stratified sample of the chains (specs: (molecules, seed, temperature) per chain), one chain
+    per host thread, and estimates the accepted-moves/s rate of the whole workload on `threads`
+    cores.  Returns (rate, description, cores)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
+    from mc_cpp_gb300 import systems
     orc.build()
-    sizes = np.array([c.natom for c in chains])
-    order = np.argsort(sizes)
-    nsamp = min(threads, len(chains))
-    picks = [int(order[int((k + 0.5) * len(chains) / nsamp)]) for k in range(nsamp)]
+    sizes = np.array([3 * n for n, _, _ in specs])
+    order = np.argsort(sizes, kind="stable")
+    nsamp = min(threads, len(specs))
+    picks = [int(order[int((k + 0.5) * len(specs) / nsamp)]) for k in range(nsamp)]
     groups = np.array_split(order, nsamp)          # each sample stands for one size stratum
-    weight = [float(sum(chains[i].natom // 3 for i in g)) for g in groups]
+    weight = [float(sum(sizes[i] // 3 for i in g)) for g in groups]
     res = [None] * nsamp
+    built = {i: systems.water_box(specs[i][0], 0.0334, specs[i][1], specs[i][2]) for i in picks}
 
     def work(k):
-        s = chains[picks[k]]
+        s = built[picks[k]]
         o = orc.Oracle(s)
         o.set_acceptance_units("physical")
         t0 = time.perf_counter()
@@ -194,21 +227,21 @@ def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    chains = make_chains(0, args.chains)
+    specs = job_specs(args.chains, world)
     threads = host_threads()
     for _ in range(args.warmup):
-        cpu_sample(chains, 0.5, threads)
+        cpu_sample(specs, 0.5, threads)
     rates = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, desc, cores = cpu_sample(chains, args.ref_budget, threads)
+        r, desc, cores = cpu_sample(specs, args.ref_budget, threads)
         rates.append(r)
     wall = time.perf_counter() - t0
     v = float(np.mean(rates))
     line = {"impl": "reference", "metric": "accepted MC moves/s", "value": v, "unit": "moves/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "chains": args.chains, "l2": "n/a (CPU)"},
+            "config": workload_config(args, world),
             "cpu_baseline": {"value": v, "unit": "moves/s", "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -270,7 +303,7 @@ def run_ours(args):
     red = Reducer(world, "cuda")
     allmax, allsum = red.max, red.sum
 
-    chains = make_chains(rank, args.chains)
+    chains, mine = rank_chains(rank, world, args.chains)
     B = BatchChains(chains, dmax_trn=0.15, dmax_rot=15.0, acceptance="physical", seed=1000 + rank,
                     threads_per_chain=args.threads, ctas_per_sm=args.ctas_per_sm)
     natoms = B.natoms
@@ -317,6 +350,14 @@ def run_ours(args):
     barrier()
     e2e_s = allmax(time.perf_counter() - t_e)
     e2e = allsum(acc_e) / e2e_s
+    # untimed checks: running energies against an FP64 recompute, then the dE of every move of a
+    # logged sweep on sampled chains against the FP64 engine
+    _, _, e_run = B.stats()
+    e_64 = B.energy_fp64()
+    drift = allmax(float(np.max(np.abs(e_run - e_64) / np.abs(e_64))))
+    h2d = allsum(3 * natoms * 8)
+    d2h = allsum(3 * natoms * 8 + len(chains) * 16)
+    berr = batched_error(B, chains) if rank == 0 and not args.no_check else None
     # plain single-chain FP64 path (host-driven replay of MC_metropolis on one water box)
     plain = None
     if rank == 0 and not args.no_plain:
@@ -330,10 +371,12 @@ def run_ours(args):
                  "workload": "one 4096-molecule water box, FP64, MC_metropolis replay through the C ABI",
                  "steps": args.plain_steps}
         ff.close()
-    cpu = None
+        plain["dropin"] = dropin_rates(w)
+    cpu = cpu_cfg = None
     if rank == 0 and not args.no_cpu:
-        rate, desc, cores = cpu_sample(chains, args.cpu_budget, host_threads())
+        rate, desc, cores = cpu_sample(job_specs(args.chains, world), args.cpu_budget, host_threads())
         cpu = {"value": rate, "unit": "moves/s", "cores": cores, "kind": "port", "sample": desc}
+        cpu_cfg = cpu_config_baselines(args.cpu_budget)
     rb, nl = B.counters()
     configs = None
     if rank == 0 and not args.no_configs:
@@ -345,11 +388,12 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32",
             "precision": "f32 pair terms, f64 sums and acceptance, 64-bit fixed-point coordinates",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "chains": args.chains, "atoms_per_gpu": natoms,
-                       "molecules_per_sweep_per_gpu": int(natoms // 3),
-                       "l2": "no flush: per-sweep working set (1.5 GB lists, 134 MB coordinates) > 129 MB L2",
-                       "acceptance": "physical", "parallelism": "independent chains, weak scaling over GPUs",
-                       "tuning": tuning},
+            "config": workload_config(args, world),
+            "rank0": {"chains": len(chains), "atoms": natoms, "molecules_per_sweep": int(natoms // 3), "tuning": tuning,
+                      "chain_indices_first": mine[:8]},
+            "max_dE_err_kcal_mol": berr["max_dE_err_kcal_mol"] if berr else None,
+            "max_rel_E_drift": drift,
+            "batched_error": berr,
             "phase_ms_per_step": {"list_rebuild": ms_lists / args.steps, "sweep_kernel": ms_sweep / args.steps},
             "trials_per_s": agg["trials_per_s"],
             "acceptance_ratio": acc / max(1.0, trials),
@@ -359,14 +403,14 @@ def run_ours(args):
                          "peak_source": "FFMA-chain probe kernel measured in this run (no FP32 figure in MEASURED_PEAKS.json)",
                          "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
             "hbm": hbm_rate(traffic, ms_sweep / args.steps),
-            "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(3 * natoms * 8),
-                    "d2h_bytes_per_step": int(3 * natoms * 8 + args.chains * 16)},
+            "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(nl1 - nl0),
             "list_rebuilds_total": int(rb),
             "clocks": clk.summary(),
             "plain_fp64": plain,
             "batched_vs_plain_accepted": (value / plain["accepted_moves_per_s"]) if plain else None,
             "cpu_baseline": cpu,
+            "cpu_baseline_configs": cpu_cfg,
             "configs": configs,
         }
         print(json.dumps(line), flush=True)
@@ -374,6 +418,134 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ------------------------------------------------------------------ untimed checks of the headline run
+def batched_error(B, chains, nsample: int = 4, list_every: int = 10):
+    """One logged sweep (the production sweep kernels with per-move records).  For a sample of
+    chains (smallest, two middle, largest) every move is replayed on the plain FP64 engine from the
+    chain's coordinates before the sweep: its FP64 dE of the recorded proposal against the sweep's
+    mixed dE, and the FP64 decision (same draw) against the sweep's.  The FP64 engine's Verlet list
+    (skin 2 A) is rebuilt every list_every moves, far below the displacement that could let a pair
+    within the cutoff escape it."""
+    from mc_cpp_gb300.engine import FFieldCUDA
+    KCAL = 418.4
+    order = np.argsort([c.natom for c in chains], kind="stable")
+    pick = sorted({int(order[0]), int(order[len(order) // 3]), int(order[2 * len(order) // 3]), int(order[-1])})[:nsample]
+    starts = {k: B.coords(k) for k in pick}
+    recs = B.sweep_logged()
+    errs, ties, moves = [], 0, 0
+    t0 = time.perf_counter()
+    for k in pick:
+        s = chains[k].copy()
+        s.set_coords(starts[k])
+        ff = FFieldCUDA(s, "fp64", moves=False)
+        beta = 1.0 / (0.83144621 / KCAL * s.temp) / KCAL          # physical units, dE in iu
+        apr = 3
+        for i, m in enumerate(recs[k]):
+            if i % list_every == 0:
+                ff.askListUpdate()
+            r = int(m["residue"])
+            d64 = ff.delta_e(np.arange(apr * r, apr * r + apr), m["xyz"][:apr])
+            errs.append(abs(float(m["de"]) - d64) / KCAL)
+            alpha = ((int(m["alpha_hi"]) << 21 ^ int(m["alpha_lo"]) >> 11) + 1) / 2.0 ** 53
+            acc64 = d64 <= np.finfo(float).eps or alpha < math.exp(-beta * d64)
+            acc = bool(m["flags"] & 2)
+            ties += int(acc64 != acc)
+            if acc:
+                ff.commit()
+            moves += 1
+        ff.close()
+    errs = np.array(errs)
+    return {"max_dE_err_kcal_mol": float(errs.max()), "rms_dE_err_kcal_mol": float(np.sqrt((errs ** 2).mean())),
+            "moves_checked": moves, "chains_checked": [int(chains[k].natom // 3) for k in pick],
+            "decisions_differing_from_fp64": ties, "seconds": time.perf_counter() - t0,
+            "how": "one logged sweep after the timed region; FP64 dE of each recorded proposal on the plain engine"}
+
+
+def dropin_rates(w, steps_inc: int = 2000, steps_full: int = 100):
+    """MC_metropolis's unmodified call sequence on one water box, FP64: getE(), move in place,
+    getE(), restore when rejected, askListUpdate every 50 moves.  'incremental' is the drop-in's
+    getE (mcg_energy_host, what FField_CUDA::getE calls); 'full' uploads all coordinates and
+    recomputes the whole energy at every getE (what FField_CUDA did before)."""
+    from mc_cpp_gb300.engine import FFieldCUDA
+    KCAL = 418.4
+    out = {"workload": "%d-molecule water box, FP64, residue translations <= 0.15 A, physical acceptance" % (w.natom // 3)}
+    for mode, steps in (("incremental", steps_inc), ("full", steps_full)):
+        ff = FFieldCUDA(w, "fp64", moves=False)
+        x, y, z = w.x.copy(), w.y.copy(), w.z.copy()
+        L = w.box[0]
+        rng = np.random.default_rng(5)
+        beta = 1.0 / (0.0019872 * w.temp * KCAL)
+
+        def getE():
+            if mode == "incremental":
+                return ff.getE_host(x, y, z)
+            ff.setCoords(np.stack([x, y, z], 1))
+            return ff.getE()
+        getE()
+        nacc = 0
+        t = time.perf_counter()
+        for st in range(1, steps + 1):
+            r = int(rng.integers(0, w.natom // 3))
+            a = slice(3 * r, 3 * r + 3)
+            eold = getE()
+            bx, by, bz = x[a].copy(), y[a].copy(), z[a].copy()
+            d = rng.uniform(-0.15, 0.15, 3)
+            x[a] = bx + d[0]; y[a] = by + d[1]; z[a] = bz + d[2]
+            for v in (x, y, z):
+                v[a] -= L * np.round(v[a] / L)
+            de = getE() - eold
+            if de <= 0 or rng.random() < math.exp(-beta * de):
+                nacc += 1
+            else:
+                x[a], y[a], z[a] = bx, by, bz
+            if st % 50 == 0:
+                if mode == "incremental":
+                    ff.getE_host(x, y, z)
+                ff.askListUpdate(st)
+        dt = time.perf_counter() - t
+        out[mode] = {"moves_per_s": steps / dt, "accepted_moves_per_s": nacc / dt, "steps": steps}
+        ff.close()
+    out["speedup"] = out["incremental"]["moves_per_s"] / out["full"]["moves_per_s"]
+    return out
+
+
+def cpu_config_baselines(budget_s: float):
+    """The reference's algorithm (oracle/ port: FField_MDBAS getE, List_nonBonded update, the
+    MC_metropolis loop with two full getE per move) on the other configurations, on this host:
+    getE ms, Verlet update ms (OpenMP over the host threads, as the reference's list build), and MC
+    moves/s over a bounded run (the 100,002-atom box: extrapolated from getE, two per move)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from mc_cpp_gb300 import systems
+    orc.build()
+    out = {"kind": "port", "threads_list_build": host_threads(), "threads_energy": 1}
+    cases = (("argon864", systems.argon_fcc, True), ("water4096", systems.water_box, True),
+             ("peptide", systems.peptide_in_water, True), ("water100k", lambda: systems.water_box(33334, seed=11), False))
+    for name, make, mc in cases:
+        s = make()
+        o = orc.Oracle(s, moves=mc)
+        t = time.perf_counter()
+        o.energy()
+        ge = time.perf_counter() - t
+        t = time.perf_counter()
+        o.update_verlet()
+        lu = time.perf_counter() - t
+        rec = {"atoms": s.natom, "getE_ms": ge * 1e3, "list_update_ms": lu * 1e3,
+               "pair_interactions_per_s": o.pairs_in_cutoff() / ge}
+        if mc:
+            nmv = int(max(2, min(2000, budget_s / max(1e-6, 2.0 * ge))))
+            t = time.perf_counter()
+            _, _, nacc = o.mc_run(nmv, 1234, trace=False)
+            dt = time.perf_counter() - t
+            rec.update({"mc_moves": nmv, "moves_per_s": nmv / dt, "accepted_moves_per_s": nacc / dt,
+                        "acceptance": "reference units"})
+        else:
+            rec.update({"moves_per_s_extrapolated": 1.0 / (2.0 * ge)})
+        out[name] = rec
+        del o
+    return out
 
 
 # ------------------------------------------------------------------ the other configurations
@@ -540,6 +712,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' figures")
+    ap.add_argument("--no-check", action="store_true", help="skip the untimed FP64 check of a logged sweep")
+    ap.add_argument("--master-port", type=int, default=29517, help="rendezvous port when this script starts the ranks")
     ap.add_argument("--config-only", choices=["argon864", "peptide", "water100k", "argon1024"],
                     help="print only that configuration's figures (one JSON line) and exit")
     args = ap.parse_args()
@@ -552,6 +726,15 @@ def main():
         return 0
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one rank per GPU: start them with torchrun on this node (127.0.0.1 rendezvous)
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+               "--master-addr", "127.0.0.1", "--master-port", str(args.master_port), os.path.abspath(__file__)] + sys.argv[1:]
+        return subprocess.call(cmd)
+    world = env_rank()[1]
+    if world != args.gpus:
+        print(json.dumps({"error": "WORLD_SIZE %d differs from --gpus %d" % (world, args.gpus)}), flush=True)
+        return 2
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

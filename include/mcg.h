@@ -107,6 +107,17 @@ int mcg_get_coords(mcg_system* s, double* x, double* y, double* z);
  * the current list; ener = [tot, pot, kin(=0), elec, vdw, bond, ang, ub, dihe, impr] in iu. */
 int mcg_energy(mcg_system* s, double ener[10]);
 
+/* FField::getE() (src/FField_MDBAS.cpp:53-75) for a caller that moves atoms in place between calls,
+ * as MC_metropolis::run does around every trial move (src/MC_metropolis.cpp:94,122,130-133):
+ * x, y, z are the caller's current coordinates of all atoms and *etot receives their total energy
+ * (iu).  Only what changed since the engine's coordinates is sent to the device: nothing when no
+ * atom moved; a commit of the last proposal when exactly its atoms sit at its coordinates (an
+ * accepted move); the dE of the changed atoms (at most 1024, as mcg_delta_e) when a new move was
+ * made; a full upload and recompute otherwise, and on the first call after mcg_create,
+ * mcg_set_coords, mcg_commit, mcg_update_lists or a Metropolis run.  The total then carries the
+ * dE sums since that recompute (mcg_delta_e's error per move, none in FP64 beyond rounding). */
+int mcg_energy_host(mcg_system* s, const double* x, const double* y, const double* z, double* etot);
+
 /* FField::askListUpdate (src/FField.cpp:222-235): rebuild the Verlet list from the current
  * coordinates with a device cell list.  No-op in full mode. */
 int mcg_update_lists(mcg_system* s);
@@ -175,7 +186,9 @@ int mcg_build_exclusions(const mcg_system_desc* desc, int* counts, int* entries,
  * every 50 steps (MC_metropolis.cpp:151).  trace (may be NULL) receives 12 doubles per step:
  * st, imvtyp, imvatm, r0, r1, r2, rang, eold, enew, de, alpha (-1 if not drawn), accepted.
  * With follow != NULL (nsteps*2 ints: imvtyp, accepted per step), accept decisions are taken from
- * it when they disagree with this engine's (a tie); ties are counted in *n_ties. */
+ * it when they disagree with this engine's and the disagreement is a tie (the draw alpha within
+ * 1e-6 of exp(-beta dE), or, when no alpha was drawn, |dE| <= 1e-6 iu); ties are counted in
+ * *n_ties.  Any other disagreement, or a different move type, ends the run with MCG_EINVAL. */
 int mcg_add_move(mcg_system* s, int type, int mode, const int* sele, double dmax, double target, int each);
 int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
                        const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties);
@@ -230,6 +243,21 @@ int mcg_batch_get_dmax(mcg_batch* b, double* dmax_trn, double* dmax_rot);
 int mcg_batch_energy_fp64(mcg_batch* b, double* e);
 int mcg_batch_get_coords(mcg_batch* b, int chain, double* x, double* y, double* z);
 int mcg_batch_set_coords(mcg_batch* b, int chain, const double* x, const double* y, const double* z);
+/* One trial move of a logged sweep (no counterpart in the reference, whose MC_metropolis keeps no
+ * per-move record): what the sweep proposed and decided, for checking it against an FP64
+ * restatement of the same chain. */
+typedef struct mcg_batch_move {
+    double de;                  /* the move's dE (iu) as the sweep's Metropolis test used it */
+    int residue;                /* moved residue, index within its chain */
+    int flags;                  /* bit 0: rotation (else translation); bit 1: accepted */
+    uint32_t alpha_hi, alpha_lo;/* Philox words of the acceptance draw, alpha = ((hi << 21 ^ lo >> 11) + 1) / 2^53 */
+    double xyz[8][3];           /* proposed positions (A, in [-L/2, L/2)) of the residue's atoms; first apr used */
+} mcg_batch_move;
+/* One sweep with per-move records, host-synchronous: moves[r0(c) + k] receives chain c's k-th trial
+ * move of this sweep (its Philox counter is the chain's trial count before the sweep plus k), where
+ * r0(c) is the number of residues of the chains before c; cap >= the residues of all chains.  The
+ * sweep runs the same kernels as mcg_batch_sweep, launched directly instead of from the graph. */
+int mcg_batch_sweep_logged(mcg_batch* b, mcg_batch_move* moves, int64_t cap);
 /* Run nsweeps sweeps and return their device time in milliseconds (CUDA events on the handle's
  * stream, synchronised on both sides). */
 int mcg_batch_time_sweeps(mcg_batch* b, int nsweeps, float* ms);
@@ -308,8 +336,10 @@ int mcg_probe_fp32_tflops(double* tflops);
  * of partners j > i with nup[natom] entries each; out[2] receives (elec, vdw) in iu.  Launched on
  * `stream` (a cudaStream_t, NULL for the default stream), asynchronous.  natom is limited to
  * MCG_NOALLOC_MAX_ATOMS (the static scratch is 512 KiB on every GPU that loads the library).  The
- * first call on a device looks up the scratch address (cudaGetSymbolAddress) with that device
- * current.  Calls share the scratch: calls that overlap on the GPU race and must be serialised. */
+ * rows are not trusted: counts above cap are clamped to cap and partners outside [0, natom) are
+ * skipped.  The first call on a device looks up the scratch address (cudaGetSymbolAddress) with
+ * that device current and keeps it for the process (stale after a cudaDeviceReset of that device).
+ * Calls share the scratch: calls that overlap on the GPU race and must be serialised. */
 #define MCG_NOALLOC_MAX_ATOMS 262144
 int mcg_energy_switch_fp64_noalloc(int natom, const double* pq, const double* es, const int* nbr, const int* nup,
                                    int cap, int pbc_type, const double box[3], double cutoff, double cuton,

@@ -136,7 +136,11 @@ void FField_CUDA::compute()
 
 double FField_CUDA::getE()
 {
-    compute();
+    ensure();
+    double e = 0.0;
+    check(mcg_energy_host(sys, at_List.getXvect().data(), at_List.getYvect().data(), at_List.getZvect().data(), &e),
+          "energy_host");
+    tot = pot = e;
     return tot;
 }
 
@@ -154,7 +158,9 @@ void FField_CUDA::askListUpdate(int st)
         std::cout << "Verlet list updated at step " << st;
         auto start = std::chrono::system_clock::now();
         ensure();
-        upload();
+        double e = 0.0;   // the device takes the AtomList's coordinates (commits an accepted move)
+        check(mcg_energy_host(sys, at_List.getXvect().data(), at_List.getYvect().data(), at_List.getZvect().data(), &e),
+              "energy_host");
         check(mcg_update_lists(sys), "update_lists");
         auto end = std::chrono::system_clock::now();
         std::cout << " : time required (milliseconds) : "

@@ -8,9 +8,16 @@
 //
 // Like every FField it holds references to the caller's AtomList, PerConditions and Ensemble and
 // reads the coordinates again on every getE(), because MC_metropolis moves atoms in place between
-// calls (Move.hpp:47-48, AtomList.cpp:427).  The device system is created on the first energy
-// call, after IO_MDBAS has filled the bonded lists through the setters; its exclusion and Verlet
-// lists are built on the device with the same rules as List_nonBonded.
+// calls (Move.hpp:47-48, AtomList.cpp:427).  getE() hands the AtomList's coordinate vectors to
+// mcg_energy_host, which sends the device only what changed since the previous call: nothing
+// before a move (or after a rejected one), a commit after an accepted one, the moved atoms' dE
+// after a move.  So the unmodified MC_metropolis loop costs one small dE launch per trial move, not
+// two full energies.  askListUpdate() first brings the device up to the AtomList, then rebuilds
+// the list; the next getE() recomputes the whole energy over the new list.  getE() refreshes the
+// tot and pot members; getE(double ener[10]) recomputes every component.  The device system is
+// created on the first energy call, after IO_MDBAS has filled the bonded lists through the
+// setters; its exclusion and Verlet lists are built on the device with the same rules as
+// List_nonBonded.
 //
 // Errors follow the reference's convention: the reason goes to cerr and the process exits with
 // the engine's negative status (FField_MDBAS.cpp:68-71 does the same for a bad cut mode).

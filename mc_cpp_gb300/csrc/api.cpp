@@ -24,9 +24,22 @@ namespace mcg {
 const char* last_error_cstr();
 }
 
+// What mcg_energy_host knows about the engine's current coordinates (its host mirror host_x/y/z):
+// their total energy with the current list, and the delta_e proposal it made last, if any.  Every
+// other entry point that changes coordinates, lists or the pending proposal updates or drops it.
+struct IncrementalEnergy {
+    bool valid = false;     // e_base is the total energy of host_x/y/z over the current list
+    double e_base = 0.0;
+    bool prop = false;      // the engine's pending proposal is the one mcg_energy_host made
+    double e_prop = 0.0;    // the total energy with that proposal applied
+    std::vector<int> diff;  // scratch: atoms whose caller coordinates differ from the mirror
+    std::vector<double> nx, ny, nz;
+};
+
 struct mcg_system {
     mcg::SingleEngine eng;
     std::vector<mcg::MoveKind> moves;
+    IncrementalEnergy inc;
 };
 
 using namespace mcg;
@@ -66,6 +79,7 @@ int mcg_destroy(mcg_system* s) {
 
 int mcg_set_coords(mcg_system* s, const double* x, const double* y, const double* z) {
     if (!s || !x || !y || !z) return fail(MCG_EINVAL, "null argument");
+    s->inc.valid = s->inc.prop = false;
     return s->eng.set_coords(x, y, z);
 }
 
@@ -76,22 +90,87 @@ int mcg_get_coords(mcg_system* s, double* x, double* y, double* z) {
 
 int mcg_energy(mcg_system* s, double ener[10]) {
     if (!s || !ener) return fail(MCG_EINVAL, "null argument");
-    return s->eng.energy(ener);
+    int rc = s->eng.energy(ener);
+    s->inc.valid = rc == MCG_OK;
+    s->inc.e_base = ener[0];
+    s->inc.prop = false;
+    return rc;
+}
+
+// FField::getE() for a caller that moves atoms in place between calls.  MC_metropolis::run calls
+// getE() before and after every trial move (MC_metropolis.cpp:94,122) and restores the moved atoms
+// of a rejected move (:130-133), so between two calls only the atoms of one move differ.  The
+// caller's coordinates are compared with the engine's mirror of the device coordinates:
+//   none differ                           -> the known energy, no device work;
+//   exactly the last proposal's atoms, at
+//   the proposal's coordinates            -> the proposal is committed (an accepted move);
+//   at most 1024 atoms                    -> their dE over the current list (mcg_delta_e) is added
+//                                            and kept as the new proposal;
+//   more, or no known energy              -> all coordinates are uploaded and the energy recomputed.
+// A list update, mcg_set_coords, mcg_commit or a Metropolis run makes the next call recompute.
+int mcg_energy_host(mcg_system* s, const double* x, const double* y, const double* z, double* etot) {
+    if (!s || !x || !y || !z || !etot) return fail(MCG_EINVAL, "null argument");
+    SingleEngine& E = s->eng;
+    IncrementalEnergy& I = s->inc;
+    const int n = E.n;
+    int rc;
+    if (I.valid) {
+        I.diff.clear();
+        for (int i = 0; i < n; i++)
+            if (!(x[i] == E.host_x[i] && y[i] == E.host_y[i] && z[i] == E.host_z[i])) {
+                I.diff.push_back(i);
+                if ((int)I.diff.size() > 1024) break;
+            }
+        const int m = (int)I.diff.size();
+        if (m == 0) {
+            *etot = I.e_base;
+            return MCG_OK;
+        }
+        if (I.prop && E.pending_matches(m, I.diff.data(), x, y, z)) {
+            if ((rc = E.commit())) { I.valid = I.prop = false; return rc; }
+            I.e_base = I.e_prop;
+            I.prop = false;
+            *etot = I.e_base;
+            return MCG_OK;
+        }
+        if (m <= 1024) {
+            I.nx.resize(m); I.ny.resize(m); I.nz.resize(m);
+            for (int k = 0; k < m; k++) { const int a = I.diff[k]; I.nx[k] = x[a]; I.ny[k] = y[a]; I.nz[k] = z[a]; }
+            double de = 0.0;
+            I.prop = false;
+            if ((rc = E.delta_e(m, I.diff.data(), I.nx.data(), I.ny.data(), I.nz.data(), &de))) return rc;
+            I.prop = true;
+            I.e_prop = I.e_base + de;
+            *etot = I.e_prop;
+            return MCG_OK;
+        }
+    }
+    I.valid = I.prop = false;
+    if ((rc = E.set_coords(x, y, z))) return rc;
+    double ener[10];
+    if ((rc = E.energy(ener))) return rc;
+    I.valid = true;
+    I.e_base = ener[0];
+    *etot = I.e_base;
+    return MCG_OK;
 }
 
 int mcg_update_lists(mcg_system* s) {
     if (!s) return fail(MCG_EINVAL, "null handle");
+    s->inc.valid = s->inc.prop = false;
     return s->eng.update_lists();
 }
 
 int mcg_delta_e(mcg_system* s, int n, const int* atoms, const double* nx, const double* ny, const double* nz,
                 double* de) {
     if (!s || !atoms || !nx || !ny || !nz || !de) return fail(MCG_EINVAL, "null argument");
+    s->inc.prop = false;
     return s->eng.delta_e(n, atoms, nx, ny, nz, de);
 }
 
 int mcg_commit(mcg_system* s) {
     if (!s) return fail(MCG_EINVAL, "null handle");
+    s->inc.valid = s->inc.prop = false;
     return s->eng.commit();
 }
 
@@ -230,6 +309,7 @@ static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int accepta
     if (!s) return fail(MCG_EINVAL, "null handle");
     if (s->moves.empty()) return fail(MCG_EINVAL, "no move types registered");  // MC.cpp:185-189
     if (nsteps < 0) return fail(MCG_EINVAL, "nsteps must be >= 0");
+    s->inc.valid = s->inc.prop = false;
     SingleEngine& E = s->eng;
     const HostSystem& h = E.hs;
     const int nmvtyp = (int)s->moves.size();
@@ -327,7 +407,16 @@ static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int accepta
         if (follow) {
             bool want = follow[2 * (st - 1) + 1] != 0;
             if (follow[2 * (st - 1)] != imvtyp) return fail(MCG_EINVAL, "followed trace diverged at step " + std::to_string(st));
-            if (want != accepted) { ties++; accepted = want; }
+            if (want != accepted) {
+                // only a tie may be overridden: the draw within 1e-6 of the acceptance threshold,
+                // or (no draw) a dE within 1e-6 iu of the DBL_EPSILON bound
+                const double margin = alpha >= 0.0 ? std::fabs(alpha - std::exp(-beta * de)) : std::fabs(de);
+                if (!(margin <= 1e-6))
+                    return fail(MCG_EINVAL, "followed decision differs at step " + std::to_string(st) +
+                                                " and is not a tie (margin " + std::to_string(margin) + ")");
+                ties++;
+                accepted = want;
+            }
         }
         double eold = etot;
         if (accepted) {

@@ -1720,6 +1720,17 @@ int SingleEngine::commit() {
     return MCG_OK;
 }
 
+bool SingleEngine::pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const {
+    if (pending_m != m) return false;
+    for (int k = 0; k < m; k++) {
+        const int a = atoms[k];
+        if (pending_idx[k] != a || pending_xyz[3 * k] != x[a] || pending_xyz[3 * k + 1] != y[a] ||
+            pending_xyz[3 * k + 2] != z[a])
+            return false;
+    }
+    return true;
+}
+
 int SingleEngine::update_lists() {
     if (hs.cut != MCG_CUT_SWITCH) return MCG_OK;
     int rc = build_list();

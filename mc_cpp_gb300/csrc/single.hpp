@@ -24,6 +24,8 @@ public:
     int get_coords(double* x, double* y, double* z);
     int delta_e(int m, const int* atoms, const double* nx, const double* ny, const double* nz, double* de);
     int commit();
+    // true when the pending proposal moves exactly atoms[0..m) (ascending) to x/y/z[atoms[k]]
+    bool pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const;
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
     int time_nonbonded(int reps, float* ms);
     // Pair-kernel variant of the mixed periodic switch energy: -1 = chosen by timing at the first

@@ -70,6 +70,14 @@ class FFieldCUDA:
         native.check(native.lib().mcg_energy(self.h, native.pd(e)))
         return e
 
+    def getE_host(self, x, y, z) -> float:
+        """FField::getE() on caller-owned coordinate arrays (float64, natom each) that the caller
+        moves in place between calls, as MC_metropolis does; only what changed is sent to the device
+        (mcg_energy_host)."""
+        e = C.c_double(0)
+        native.check(native.lib().mcg_energy_host(self.h, native.pd(x), native.pd(y), native.pd(z), C.byref(e)))
+        return e.value
+
     def askListUpdate(self, step: int = 0) -> None:
         native.check(native.lib().mcg_update_lists(self.h))
 
@@ -235,6 +243,14 @@ class BatchChains:
 
     def sweep(self, n: int = 1) -> None:
         native.check(native.lib().mcg_batch_sweep(self.h, n))
+
+    def sweep_logged(self):
+        """One sweep with per-move records: a list with, for each chain, its moves of this sweep in
+        order (structured array of native.MOVE_DTYPE)."""
+        nres = [int(n) // a for n, a in zip(self.sizes, self._apr_of)]
+        rec = np.zeros(sum(nres), native.MOVE_DTYPE)
+        native.check(native.lib().mcg_batch_sweep_logged(self.h, rec.ctypes.data, len(rec)))
+        return np.split(rec, np.cumsum(nres)[:-1])
 
     def time_sweeps(self, n: int) -> float:
         ms = C.c_float(0)

@@ -68,6 +68,11 @@ class BatchTuning(C.Structure):
                 ("ms_per_sweep", C.c_float), ("from_cache", C.c_int), ("clusters", C.c_int)]
 
 
+# one record of a logged sweep (struct mcg_batch_move)
+MOVE_DTYPE = np.dtype([("de", np.float64), ("residue", np.int32), ("flags", np.int32), ("alpha_hi", np.uint32),
+                       ("alpha_lo", np.uint32), ("xyz", np.float64, (8, 3))], align=True)
+assert MOVE_DTYPE.itemsize == 216
+
 _lib = None
 
 
@@ -97,6 +102,7 @@ def lib():
         "mcg_set_coords": (C.c_int, [P, _d, _d, _d]),
         "mcg_get_coords": (C.c_int, [P, _d, _d, _d]),
         "mcg_energy": (C.c_int, [P, _d]),
+        "mcg_energy_host": (C.c_int, [P, _d, _d, _d, _d]),
         "mcg_update_lists": (C.c_int, [P]),
         "mcg_delta_e": (C.c_int, [P, C.c_int, _i, _d, _d, _d, _d]),
         "mcg_commit": (C.c_int, [P]),
@@ -110,6 +116,7 @@ def lib():
         "mcg_batch_create": (C.c_int, [C.POINTER(SystemDesc), C.c_int, C.POINTER(BatchOpts), C.POINTER(P)]),
         "mcg_batch_destroy": (C.c_int, [P]),
         "mcg_batch_sweep": (C.c_int, [P, C.c_int]),
+        "mcg_batch_sweep_logged": (C.c_int, [P, C.c_void_p, C.c_int64]),
         "mcg_batch_stats": (C.c_int, [P, _i64, _i64, _d]),
         "mcg_batch_energy_fp64": (C.c_int, [P, _d]),
         "mcg_batch_get_coords": (C.c_int, [P, C.c_int, _d, _d, _d]),

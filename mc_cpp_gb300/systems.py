@@ -24,7 +24,7 @@ import numpy as np
 from .mdbas import MoveSpec, System
 
 __all__ = ["argon_fcc", "argon_random", "water_box", "peptide_in_water", "water_chains",
-           "argon_chains", "TWO_SIXTH", "WATER"]
+           "water_chain_specs", "argon_chains", "shard_chains", "TWO_SIXTH", "WATER"]
 
 TWO_SIXTH = 2.0 ** (1.0 / 6.0)
 # rigid 3-site water (config "water box"): O-H 0.9572 A, H-O-H 104.52 deg
@@ -253,15 +253,24 @@ def peptide_in_water(nchain: int = 40, nwat: int = 6000, L: float = 56.4, seed: 
                         MoveSpec("rot", "residue", "residue_name", "TIP3", 15.0, 50.0, 0)])
 
 
-def water_chains(nchains: int = 256, nmin: int = 512, nmax: int = 8192, density: float = 0.0334,
-                 tmin: float = 280.0, tmax: float = 360.0, seed: int = 3) -> List[System]:
-    """Independent water boxes of log-uniform molecule counts and uniform temperatures."""
+def water_chain_specs(nchains: int = 256, nmin: int = 512, nmax: int = 8192, tmin: float = 280.0,
+                      tmax: float = 360.0, seed: int = 3):
+    """(molecules, seed, temperature) of each chain of water_chains, without building the boxes."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(math.log(nmin), math.log(nmax), nchains)).astype(np.int64)
     sizes = np.clip(sizes, nmin, nmax)
     temps = _q(rng.uniform(tmin, tmax, nchains))
     seeds = rng.integers(1, 2 ** 31 - 1, nchains)
-    return [water_box(int(n), density, int(s), float(t)) for n, s, t in zip(sizes, seeds, temps)]
+    return [(int(n), int(s), float(t)) for n, s, t in zip(sizes, seeds, temps)]
+
+
+def water_chains(nchains: int = 256, nmin: int = 512, nmax: int = 8192, density: float = 0.0334,
+                 tmin: float = 280.0, tmax: float = 360.0, seed: int = 3, only=None) -> List[System]:
+    """Independent water boxes of log-uniform molecule counts and uniform temperatures; `only`
+    (indices into the nchains specs) builds a subset, in that order."""
+    specs = water_chain_specs(nchains, nmin, nmax, tmin, tmax, seed)
+    pick = range(nchains) if only is None else only
+    return [water_box(specs[i][0], density, specs[i][1], specs[i][2]) for i in pick]
 
 
 def argon_chains(nchains: int = 1024, nmin: int = 500, nmax: int = 2000, rho_min: float = 0.015,
@@ -273,3 +282,21 @@ def argon_chains(nchains: int = 1024, nmin: int = 500, nmax: int = 2000, rho_min
     temps = _q(rng.uniform(tmin, tmax, nchains))
     seeds = rng.integers(1, 2 ** 31 - 1, nchains)
     return [argon_random(int(n), float(r), int(s), float(t)) for n, r, s, t in zip(sizes, rhos, seeds, temps)]
+
+
+def shard_chains(weights, world: int):
+    """Greedy longest-first partition of independent chains over `world` ranks: chains in order
+    of decreasing weight (atoms), each to the rank with the least total so far (lowest rank on a
+    tie).  Returns each rank's chain indices, ascending.  The largest total exceeds the smallest by
+    at most the largest weight."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    w = [float(v) for v in weights]
+    order = sorted(range(len(w)), key=lambda i: (-w[i], i))
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        load[r] += w[i]
+        parts[r].append(i)
+    return [sorted(p) for p in parts]

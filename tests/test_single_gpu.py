@@ -5,6 +5,7 @@ Tolerances (relative to the magnitude of the total; energies in internal units):
                exclusion rows and 1-4 pairs bit-exact as sets.
   mixed:       total energy within 1e-6 relative; each dE within 1e-4 kcal/mol.
 """
+import os
 import numpy as np
 import pytest
 
@@ -240,3 +241,26 @@ def test_invalid_calls_return_status():
         ff.commit()
     # the handle stays usable after rejected calls
     assert np.isfinite(ff.getE())
+
+
+def test_metropolis_1e5_moves_match_the_reference_run():
+    """The small plain configuration at its stated length: 864 argon atoms, 1e5 single-atom moves
+    of the reference's random stream (seed 1234), FP64, recorded from the compiled reference
+    (tests/golden/argon864_long.npz).  Without following, every decision equals the reference's
+    and every dE agrees within 1e-6 kcal/mol; the final running energy agrees within 1e-9."""
+    g = goldens.golden()["mc"]["argon864_long"]
+    ref = np.load(os.path.join(goldens.GOLD_DIR, "argon864_long.npz"))
+    n = g["nsteps"]
+    acc_ref = np.unpackbits(ref["accepted"])[:n].astype(bool)
+    s = goldens.system("argon864")
+    ff = FFieldCUDA(s, "fp64")
+    tr, etot, nacc, nties = ff.metropolis(n, g["seed"])
+    assert nties == 0
+    assert np.array_equal(tr[:, 2].astype(np.int32), ref["imvatm"])        # same moved atoms
+    assert np.array_equal(tr[:, 11] != 0, acc_ref)                         # same decisions, all 1e5
+    assert nacc == g["accepted"][0]
+    drawn = ref["alpha"] >= 0
+    assert np.array_equal(tr[:, 10] >= 0, drawn)
+    assert np.array_equal(tr[drawn, 10], ref["alpha"][drawn])               # the same alpha draws
+    assert (np.abs(tr[:, 9] - ref["de"]) / KCAL).max() <= 1e-6
+    assert abs(etot - g["final_etot"]) <= 1e-9 * abs(g["final_etot"])
