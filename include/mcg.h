@@ -145,9 +145,10 @@ int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
 int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);
 /* Kernel of the mixed-precision periodic switch energy (an addition without a reference
  * counterpart: FField_MDBAS has one scalar loop).  variant -1 (the default) times every variant
- * at the first energy and keeps the fastest; 0..3 are per-atom list kernels; 4 and above are
- * cluster-pair kernels over the cluster form of the same Verlet list (MCG_ENOTSUP when it was
- * not built).  mcg_get_pair_kernel reports the variant in use (-1 before the first energy) and
+ * at the first energy and keeps the fastest; 0..3 are per-atom list kernels; 4 and 5 are
+ * cluster-pair kernels over the cluster form of the same Verlet list; 6 and 7 are group-pair
+ * kernels over the group form of the rows the list kernels read (MCG_ENOTSUP when a form could
+ * not be built).  mcg_get_pair_kernel reports the variant in use (-1 before the first energy) and
  * the number of variants. */
 int mcg_set_pair_kernel(mcg_system* s, int variant);
 int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count);
@@ -157,6 +158,11 @@ int mcg_get_pair_kernel(mcg_system* s, int* variant, int* count);
  * complete).  The engine builds it only for its first energy (to time the cluster kernels) and
  * while a cluster kernel is in use. */
 int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
+/* Group form of the rows the per-atom list kernels read (mixed periodic switch systems with at most
+ * 1,024 distinct atom parameter sets; zeros otherwise), built on demand: groups (runs of at most 4
+ * consecutive atoms of one residue), group pairs in the rows, and the atom pairs their masks encode
+ * (equal to the rows' size: mcg_prune_stats' entries, or the half-list size without pruning). */
+int mcg_group_stats(mcg_system* s, int64_t* groups, int64_t* entries, int64_t* mask_pairs);
 /* Dynamic pruning of the rows the per-atom list kernels of the mixed periodic switch energy read
  * (an addition without a reference counterpart: FField_MDBAS sums its whole Verlet list).  Before
  * a launch, each half Verlet row is pruned on the device to the partners within cutoff + buffer
@@ -303,6 +309,16 @@ int mcg_batch_get_lists(mcg_batch* b, int chain, int* counts, int* entries, int6
 /* Rebuild every chain's neighbour lists now (the batched counterpart of FField::askListUpdate,
  * FField.cpp:222-235).  Sweeps rebuild lists by themselves when atoms have moved enough. */
 int mcg_batch_update_lists(mcg_batch* b);
+/* Exact checkpoint of a batch (no counterpart in the reference: MC::write_traj, src/MC.cpp:93-108,
+ * saves frames and energies, not the random-number state).  mcg_batch_save writes every chain's
+ * 64-bit fixed-point coordinates, the positions its lists were built from, its Philox counter,
+ * running energy, counters, dmax state, and the launch shape, to a file (written whole, then
+ * renamed into place).  mcg_batch_load restores them into a batch created from the same chain
+ * descriptions and options (MCG_EINVAL otherwise; MCG_EIO for an unreadable, truncated or damaged
+ * file), re-applying the saved launch shape: sweeping after a load gives bitwise the chains a run
+ * without the save would have given. */
+int mcg_batch_save(mcg_batch* b, const char* path);
+int mcg_batch_load(mcg_batch* b, const char* path);
 /* Total number of atoms over all chains, and a chain's atom count. */
 int64_t mcg_batch_natoms(mcg_batch* b);
 int mcg_batch_chain_natoms(mcg_batch* b, int chain);

@@ -240,6 +240,11 @@ int mcg_cluster_stats(mcg_system* s, int64_t* clusters, int64_t* cluster_pairs, 
     return s->eng.cluster_stats(clusters, cluster_pairs, mask_pairs);
 }
 
+int mcg_group_stats(mcg_system* s, int64_t* groups, int64_t* entries, int64_t* mask_pairs) {
+    if (!s || !groups || !entries || !mask_pairs) return fail(MCG_EINVAL, "null argument");
+    return s->eng.group_stats(groups, entries, mask_pairs);
+}
+
 int mcg_set_prune_buffer(mcg_system* s, double buffer) {
     if (!s) return fail(MCG_EINVAL, "null argument");
     return s->eng.set_prune_buffer(buffer);

@@ -2054,6 +2054,154 @@ int mcg_batch_get_lists(mcg_batch* b, int chain, int* counts, int* entries, int6
     return MCG_OK;
 }
 
+// ---- exact checkpoint of a batch ----------------------------------------------------------
+// A chain's future is a function of its masters M, its Philox counter and statistics (ChainState:
+// running energy, counters, dmax and the acceptances since the last dmax adjustment, the largest
+// displacement since the last list build), its lists and the launch shape.  The lists are a
+// deterministic function of the mirror positions at their build (FB: cells sorted by residue
+// index), so the file holds FB, not the lists: loading rebuilds every chain's lists from its FB
+// and then restores M, the mirror and the states.  The launch shape matters too (the speculation
+// width sets how a move's pair terms are split over warps, so the FP32 sums' order), so it is saved
+// and re-applied.  Layout: magic, sizes, launch shape, ChainDev[nchains] and BatchGeom (checked
+// against the loading batch: same chains, options and Philox keys), ChainState[nchains],
+// M[natoms], FB[natoms], FNV-1a checksum of all the preceding bytes.
+static const char kCkptMagic[8] = {'M', 'C', 'G', 'B', 'C', 'K', 'P', '1'};
+
+struct CkptHeader {
+    char magic[8];
+    int32_t version, nchains;
+    int64_t natoms, nres;
+    int32_t threads, ctas_per_sm, spec_cap, clusters;
+};
+
+static uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t k = 0; k < n; k++) { h ^= c[k]; h *= 1099511628211ull; }
+    return h;
+}
+
+// the chains' constants without the speculation width (a launch-shape setting)
+static std::vector<ChainDev> chains_for_compare(const std::vector<ChainDev>& v) {
+    std::vector<ChainDev> w(v);
+    for (ChainDev& c : w) c.kspec = 0;
+    return w;
+}
+
+int mcg_batch_save(mcg_batch* b, const char* path) {
+    if (!b || !path) return fail(MCG_EINVAL, "null argument");
+    const int64_t na = b->natoms;
+    std::vector<ChainState> st(b->nchains);
+    std::vector<ulonglong4_32a> M(na);
+    std::vector<uint4> FB(na);
+    BK(cudaMemcpyAsync(st.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaMemcpyAsync(M.data(), b->d_M, sizeof(ulonglong4_32a) * na, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaMemcpyAsync(FB.data(), b->d_FB, sizeof(uint4) * na, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    CkptHeader h;
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, kCkptMagic, 8);
+    h.version = 1;
+    h.nchains = b->nchains;
+    h.natoms = na;
+    h.nres = b->nres;
+    h.threads = b->threads;
+    h.ctas_per_sm = b->ctas_per_sm;
+    h.spec_cap = b->spec_cap;
+    h.clusters = b->clusters;
+    std::string tmp = std::string(path) + ".part";
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return fail(MCG_EIO, std::string("cannot write ") + tmp);
+    uint64_t sum = 1469598103934665603ull;
+    bool ok = true;
+    auto put = [&](const void* p, size_t n) {
+        sum = fnv1a(sum, p, n);
+        ok = ok && fwrite(p, 1, n, f) == n;
+    };
+    put(&h, sizeof h);
+    put(b->chains.data(), sizeof(ChainDev) * b->nchains);
+    put(&b->G, sizeof(BatchGeom));
+    put(st.data(), sizeof(ChainState) * b->nchains);
+    put(M.data(), sizeof(ulonglong4_32a) * na);
+    put(FB.data(), sizeof(uint4) * na);
+    ok = ok && fwrite(&sum, 1, sizeof sum, f) == sizeof sum;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return fail(MCG_EIO, std::string("cannot write ") + path);
+    }
+    return MCG_OK;
+}
+
+int mcg_batch_load(mcg_batch* b, const char* path) {
+    if (!b || !path) return fail(MCG_EINVAL, "null argument");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(MCG_EIO, std::string("cannot read ") + path);
+    std::vector<unsigned char> buf;
+    {
+        unsigned char chunk[1 << 16];
+        size_t n;
+        while ((n = fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + n);
+        fclose(f);
+    }
+    const int64_t na = b->natoms;
+    const size_t need = sizeof(CkptHeader) + sizeof(ChainDev) * b->nchains + sizeof(BatchGeom) +
+                        sizeof(ChainState) * b->nchains + (sizeof(ulonglong4_32a) + sizeof(uint4)) * na + sizeof(uint64_t);
+    CkptHeader h;
+    if (buf.size() < sizeof h) return fail(MCG_EIO, "checkpoint file is truncated");
+    memcpy(&h, buf.data(), sizeof h);
+    if (memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) return fail(MCG_EIO, "not a batch checkpoint file");
+    if (h.nchains != b->nchains || h.natoms != na || h.nres != b->nres)
+        return fail(MCG_EINVAL, "checkpoint is of a batch with other chain or atom counts");
+    if (buf.size() != need) return fail(MCG_EIO, "checkpoint file has the wrong size (truncated or damaged)");
+    uint64_t sum;
+    memcpy(&sum, buf.data() + need - sizeof sum, sizeof sum);
+    if (fnv1a(1469598103934665603ull, buf.data(), need - sizeof sum) != sum) return fail(MCG_EIO, "checkpoint checksum mismatch");
+    size_t o = sizeof h;
+    std::vector<ChainDev> saved(b->nchains);
+    memcpy(saved.data(), buf.data() + o, sizeof(ChainDev) * b->nchains);
+    o += sizeof(ChainDev) * b->nchains;
+    BatchGeom G;
+    memcpy(&G, buf.data() + o, sizeof G);
+    o += sizeof G;
+    {
+        std::vector<ChainDev> a = chains_for_compare(saved), c = chains_for_compare(b->chains);
+        if (memcmp(a.data(), c.data(), sizeof(ChainDev) * b->nchains) != 0 || memcmp(&G, &b->G, sizeof G) != 0)
+            return fail(MCG_EINVAL, "checkpoint is of other chains or options (boxes, temperatures, moves, seed)");
+    }
+    if (h.threads != b->threads || h.ctas_per_sm != b->ctas_per_sm || h.spec_cap != b->spec_cap || h.clusters != b->clusters) {
+        int r = b->reconfigure(h.threads, h.ctas_per_sm, h.spec_cap, h.clusters);
+        if (r) return r;
+    }
+    for (int c = 0; c < b->nchains; c++)
+        if (b->chains[c].kspec != saved[c].kspec) return fail(MCG_EINVAL, "checkpoint launch shape could not be re-applied");
+    const ChainState* st = (const ChainState*)(buf.data() + o);
+    o += sizeof(ChainState) * b->nchains;
+    const ulonglong4_32a* M = (const ulonglong4_32a*)(buf.data() + o);
+    o += sizeof(ulonglong4_32a) * na;
+    const uint4* FB = (const uint4*)(buf.data() + o);
+    // lists from the build positions, then the masters, the mirror and the states
+    BK(cudaMemcpyAsync(b->d_F, FB, sizeof(uint4) * na, cudaMemcpyHostToDevice, b->stream));
+    int r = b->launch_build(b->stream, 1);
+    if (r) return r;
+    std::vector<ChainState> chk(b->nchains);
+    BK(cudaMemcpyAsync(chk.data(), b->d_state, sizeof(ChainState) * b->nchains, cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < b->nchains; c++)
+        if (chk[c].err) return fail(chk[c].err, "neighbour list capacity exceeded (chain " + std::to_string(c) + ")");
+    std::vector<uint4> F(na);
+    for (const ChainDev& C : b->chains)
+        for (int i = 0; i < C.nres * C.apr; i++) {
+            const ulonglong4_32a& m = M[C.atom0 + i];
+            F[C.atom0 + i] = make_uint4((uint32_t)(m.x >> 32), (uint32_t)(m.y >> 32), (uint32_t)(m.z >> 32), (uint32_t)(i % C.apr));
+        }
+    BK(cudaMemcpyAsync(b->d_M, M, sizeof(ulonglong4_32a) * na, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_F, F.data(), sizeof(uint4) * na, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_FB, FB, sizeof(uint4) * na, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_state, st, sizeof(ChainState) * b->nchains, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    return MCG_OK;
+}
+
 int mcg_batch_update_lists(mcg_batch* b) {
     if (!b) return fail(MCG_EINVAL, "null handle");
     int r = b->launch_build();

@@ -220,4 +220,33 @@ __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, 
     return fmaf(qk_sw, fmaf(dinv, pn, ro * dp), d_lj);
 }
 
+// Block sums of two doubles (every thread passes its values; thread 0 of warp 0 writes out[0..1]).
+__device__ __forceinline__ void block_reduce2(double a, double b, double* out) {
+    __shared__ double sa[32], sb[32];
+    a = warp_sum(a); b = warp_sum(b);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { sa[w] = a; sb[w] = b; }
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        a = l < nw ? sa[l] : 0.0; b = l < nw ? sb[l] : 0.0;
+        a = warp_sum(a); b = warp_sum(b);
+        if (l == 0) { out[0] = a; out[1] = b; }
+    }
+    __syncthreads();
+}
+
+// A lane's share of row i of the factored pair sums: q_i (ch + cl) and eps_i vs, into the lane's float-float totals
+__device__ __forceinline__ void mix_row_flush(float4 pi, float ch, float cl, float vs, float& EH, float& EL, float& VH,
+                                              float& VL) {
+    float ph, pl, sm, er;
+    ff_mul(pi.x, pi.y, ch, cl, ph, pl);
+    two_sum(EH, ph, sm, er);
+    EH = sm;
+    EL += er + pl;
+    two_sum(VH, pi.z * vs, sm, er);
+    VH = sm;
+    VL += er;
+}
+
 }  // namespace mcg

@@ -372,21 +372,6 @@ __device__ __forceinline__ void pair_energy(const AtomsDev& A, const PbcDev& pbc
     }
 }
 
-__device__ __forceinline__ void block_reduce2(double a, double b, double* out) {
-    __shared__ double sa[32], sb[32];
-    a = warp_sum(a); b = warp_sum(b);
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) { sa[w] = a; sb[w] = b; }
-    __syncthreads();
-    if (w == 0) {
-        int nw = blockDim.x >> 5;
-        a = l < nw ? sa[l] : 0.0; b = l < nw ? sb[l] : 0.0;
-        a = warp_sum(a); b = warp_sum(b);
-        if (l == 0) { out[0] = a; out[1] = b; }
-    }
-    __syncthreads();
-}
-
 // Switch energy over the half list: a warp per row i, lanes over its j > i entries.
 template <int P>
 __global__ void __launch_bounds__(NB_THREADS) k_energy_list(AtomsDev A, int n, PbcDev pbc, CutDev cut,
@@ -455,19 +440,6 @@ __device__ __forceinline__ void mix_batch(const int (&j)[U], const uint4 (&fj)[U
             vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
         }
     }
-}
-
-// the lane's share of row i: q_i (ch + cl) and eps_i vs, into the lane's float-float totals
-__device__ __forceinline__ void mix_row_flush(float4 pi, float ch, float cl, float vs, float& EH, float& EL, float& VH,
-                                              float& VL) {
-    float ph, pl, sm, er;
-    ff_mul(pi.x, pi.y, ch, cl, ph, pl);
-    two_sum(EH, ph, sm, er);
-    EH = sm;
-    EL += er + pl;
-    two_sum(VH, pi.z * vs, sm, er);
-    VH = sm;
-    VL += er;
 }
 
 // Mixed-precision switched energy over the half list for periodic boxes: the pair kernel.  A warp
@@ -1128,6 +1100,10 @@ int SingleEngine::init(const HostSystem& h) {
         (rc = dupload(&d_fxd, hs.fexclData, stream)))
         return rc;
     if ((rc = dalloc(&d_fx, n))) return rc;
+    if (uses_pair_variants() && ncls > 0) {   // groups of the group-pair kernels (residue runs of <= 4 atoms)
+        if ((rc = grp.setup(hs.resid))) return rc;
+        grp_setup = true;
+    }
     // 1-4 pairs and their per-atom CSR (both directions) for the ΔE kernel
     n14 = (int)hs.pairs14.size() / 2;
     std::vector<int2> p14(n14);
@@ -1197,10 +1173,13 @@ int SingleEngine::launch_nonbonded(double* nbp) {
 }
 
 static const int kListVariants = 4;
+static const int kGroupFirst = kListVariants + ClusterPairs::kVariants;   // first group-pair variant
 
-int SingleEngine::pair_kernel_count() { return kListVariants + ClusterPairs::kVariants; }
+int SingleEngine::pair_kernel_count() { return kGroupFirst + GroupPairs::kVariants; }
 
 int SingleEngine::launch_pair_variant(int v, double* nbp) {
+    if (v >= kGroupFirst)
+        return grp.launch_energy(stream, v - kGroupFirst, d_fx, d_cls, ncls, group_geom(), nbp);
     if (v >= kListVariants) {
         launches += 1;   // the pack kernel in front of the cluster kernel
         return clp.launch_energy(stream, v - kListVariants, d_fx, d_prmf, cluster_geom(), nbp);
@@ -1248,8 +1227,12 @@ void SingleEngine::tune_pair_kernel() {
     if (cudaEventCreate(&a) != cudaSuccess) return;
     if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return; }
     float best = 3.0e38f;
-    const int nv = clp.ok ? pair_kernel_count() : kListVariants;
+    const int nv = pair_kernel_count();
+    int timed = 0;
     for (int v = 0; v < nv; v++) {
+        if (v >= kListVariants && v < kGroupFirst && !clp.ok) continue;
+        if (v >= kGroupFirst && !grp.ok) continue;
+        timed++;
         launch_pair_variant(v, d_part);
         cudaEventRecord(a, stream);
         for (int r = 0; r < 3; r++) launch_pair_variant(v, d_part);
@@ -1258,7 +1241,7 @@ void SingleEngine::tune_pair_kernel() {
         if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) continue;
         if (ms < best) { best = ms; pair_variant = v; }
     }
-    launches += 4 * nv;
+    launches += 4 * timed;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
 }
@@ -1267,12 +1250,59 @@ int SingleEngine::set_pair_kernel(int v) {
     if (v < -1 || v >= pair_kernel_count()) return fail(MCG_EINVAL, "pair-kernel variant out of range");
     if (v >= 0 && !uses_pair_variants())
         return fail(MCG_ENOTSUP, "pair-kernel variants apply to the mixed periodic switch energy");
-    if (v >= kListVariants) {
+    if (v >= kGroupFirst) {
+        if (!grp_setup) return fail(MCG_ENOTSUP, "the group-pair kernels need the parameter-class table");
+        int rc = ensure_pruned();
+        if (!rc) rc = ensure_groups();
+        if (rc) return rc;
+        if (!grp.ok) return fail(MCG_ENOTSUP, "the group-pair rows could not be built for this system");
+    } else if (v >= kListVariants) {
         int rc = ensure_clusters();
         if (rc) return rc;
         if (!clp.ok) return fail(MCG_ENOTSUP, "the cluster-pair list could not be built for this system");
     }
     pair_variant = v;
+    return MCG_OK;
+}
+
+// The group-pair rows of the rows the per-atom list kernels read (pruned rows when pruning is on),
+// rebuilt on first use after those rows changed.  A system whose group rows overflow the build's
+// limits keeps the other kernels.
+int SingleEngine::ensure_groups() {
+    if (!grp_setup || !grp_dirty) return MCG_OK;
+    grp_dirty = false;
+    const bool pr = prune_buf > 0.0 && !prune_dirty && d_prn;
+    const int grc = grp.build(stream, pr ? d_prn : d_nbr, pr ? d_pnup : d_nup, cap);
+    launches += grp.build_launches;
+    grp.build_launches = 0;
+    if (grc == MCG_ECUDA) return grc;
+    if (grc != MCG_OK) set_error("");
+    return MCG_OK;
+}
+
+GroupGeom SingleEngine::group_geom() const {
+    const ClusterGeom C = cluster_geom();
+    GroupGeom G;
+    for (int k = 0; k < 3; k++) { G.Ls[k] = C.Ls[k]; G.Ll[k] = C.Ll[k]; }
+    G.iso = G.Ls[0] == G.Ls[1] && G.Ls[1] == G.Ls[2] && G.Ll[0] == G.Ll[1] && G.Ll[1] == G.Ll[2];
+    const double l2 = (double)G.Ls[0] + (double)G.Ll[0];
+    const double l2sq = l2 * l2;
+    G.L2h = (float)l2sq;
+    G.L2l = (float)(l2sq - (double)G.L2h);
+    G.c2 = C.c2;
+    G.n2 = C.n2;
+    G.k3 = C.k3;
+    G.inv_f1 = C.inv_f1;
+    return G;
+}
+
+int SingleEngine::group_stats(int64_t* groups, int64_t* entries, int64_t* mask_pairs) {
+    *groups = *entries = *mask_pairs = 0;
+    if (!grp_setup) return MCG_OK;
+    int rc = ensure_pruned();
+    if (!rc) rc = ensure_groups();
+    if (rc) return rc;
+    if (grp.ok) { *groups = grp.ngroup; *entries = grp.nentries; *mask_pairs = grp.nbits; }
     return MCG_OK;
 }
 
@@ -1304,9 +1334,13 @@ int SingleEngine::prepare_pair_kernel() {
     if ((rc = ensure_pruned())) return rc;
     if (pair_variant < 0) {
         if ((rc = ensure_clusters())) return rc;
+        if ((rc = ensure_groups())) return rc;
         tune_pair_kernel();
     }
-    if (pair_variant >= kListVariants) {
+    if (pair_variant >= kGroupFirst) {
+        if ((rc = ensure_groups())) return rc;
+        if (!grp.ok) pair_variant = 0;
+    } else if (pair_variant >= kListVariants) {
         if ((rc = ensure_clusters())) return rc;
         if (!clp.ok) pair_variant = 0;
     }
@@ -1346,6 +1380,7 @@ int SingleEngine::ensure_pruned() {
     const double lim = std::max(0.0, 0.5 * prune_buf - 1e-3);
     prune_lim2 = lim * lim;
     prune_dirty = false;
+    grp_dirty = grp_setup;    // the group rows follow the pruned rows
     prunes++;
     launches += 1;
     return MCG_OK;
@@ -1369,6 +1404,7 @@ int SingleEngine::set_prune_buffer(double buffer) {
         return fail(MCG_ENOTSUP, "pruning applies to the mixed periodic switch energy");
     prune_buf = buffer;
     prune_dirty = true;
+    grp_dirty = grp_setup;
     return MCG_OK;
 }
 
@@ -1534,6 +1570,7 @@ int SingleEngine::build_list() {
         if (maxrow <= cap) {
             clp_dirty = uses_pair_variants();   // the cluster form follows on first use
             prune_dirty = true;                 // and so do the pruned rows
+            grp_dirty = grp_setup;              // and the group rows
             return MCG_OK;
         }
         cudaFree(d_nbr);

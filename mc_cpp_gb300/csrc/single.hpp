@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "cluster.hpp"
+#include "groups.hpp"
 #include "dev_types.hpp"
 #include "engine.hpp"
 
@@ -34,11 +35,13 @@ public:
     int pair_kernel() const { return pair_variant; }
     static int pair_kernel_count();
     int cluster_stats(int64_t* clusters, int64_t* cluster_pairs, int64_t* mask_pairs);
+    int group_stats(int64_t* groups, int64_t* entries, int64_t* mask_pairs);
     // Dynamic pruning of the rows the mixed periodic switch energy reads: buffer (A) beyond rc,
     // 0 = the pair kernel reads the Verlet rows themselves.
     int set_prune_buffer(double buffer);
     int prune_stats(int64_t* entries, int64_t* prunes, float* last_ms);
     ClusterPairs clp;
+    GroupPairs grp;
 
     HostSystem hs;
     int n = 0;
@@ -63,6 +66,10 @@ private:
     int ensure_clusters();
     int prepare_pair_kernel();
     bool clp_dirty = false;       // the Verlet list changed since the cluster form was built
+    int ensure_groups();
+    GroupGeom group_geom() const;
+    bool grp_setup = false;       // groups defined (mixed periodic switch systems with a class table)
+    bool grp_dirty = false;       // the rows the pair kernel reads changed since the group rows were built
     int ensure_pruned();
     void note_moved(int atom);
     double prune_buf = 0.5;       // prune radius rc + prune_buf

@@ -8,6 +8,7 @@ change coordinates between calls; ``setCoords`` pushes them to the device.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -122,6 +123,12 @@ class FFieldCUDA:
         """(clusters, cluster pairs, Verlet pairs in the masks) of the cluster form of the list."""
         a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
         native.check(native.lib().mcg_cluster_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def group_stats(self):
+        """(groups, group pairs, atom pairs in their masks) of the group form of the rows."""
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        native.check(native.lib().mcg_group_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
     def set_prune_buffer(self, buffer: float) -> None:
@@ -251,6 +258,14 @@ class BatchChains:
         rec = np.zeros(sum(nres), native.MOVE_DTYPE)
         native.check(native.lib().mcg_batch_sweep_logged(self.h, rec.ctypes.data, len(rec)))
         return np.split(rec, np.cumsum(nres)[:-1])
+
+    def save(self, path: str) -> None:
+        """Exact checkpoint of every chain (mcg_batch_save)."""
+        native.check(native.lib().mcg_batch_save(self.h, os.fsencode(path)))
+
+    def load(self, path: str) -> None:
+        """Restores a checkpoint of a batch made from the same chains and options (mcg_batch_load)."""
+        native.check(native.lib().mcg_batch_load(self.h, os.fsencode(path)))
 
     def time_sweeps(self, n: int) -> float:
         ms = C.c_float(0)

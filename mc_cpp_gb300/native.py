@@ -117,6 +117,8 @@ def lib():
         "mcg_batch_destroy": (C.c_int, [P]),
         "mcg_batch_sweep": (C.c_int, [P, C.c_int]),
         "mcg_batch_sweep_logged": (C.c_int, [P, C.c_void_p, C.c_int64]),
+        "mcg_batch_save": (C.c_int, [P, C.c_char_p]),
+        "mcg_batch_load": (C.c_int, [P, C.c_char_p]),
         "mcg_batch_stats": (C.c_int, [P, _i64, _i64, _d]),
         "mcg_batch_energy_fp64": (C.c_int, [P, _d]),
         "mcg_batch_get_coords": (C.c_int, [P, C.c_int, _d, _d, _d]),
@@ -139,6 +141,7 @@ def lib():
         "mcg_set_pair_kernel": (C.c_int, [P, C.c_int]),
         "mcg_get_pair_kernel": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "mcg_cluster_stats": (C.c_int, [P, _i64, _i64, _i64]),
+        "mcg_group_stats": (C.c_int, [P, _i64, _i64, _i64]),
         "mcg_set_prune_buffer": (C.c_int, [P, C.c_double]),
         "mcg_prune_stats": (C.c_int, [P, _i64, _i64, C.POINTER(C.c_float)]),
         "mcg_mdbas_read": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(P)]),

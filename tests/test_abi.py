@@ -50,6 +50,13 @@ def test_null_handles_rejected_on_host():
     assert L.mcg_prune_stats(None, C.byref(i64), C.byref(i64), C.byref(f32)) == native.MCG_EINVAL
     assert L.mcg_set_pair_kernel(None, 0) == native.MCG_EINVAL
     assert L.mcg_cluster_stats(None, C.byref(i64), C.byref(i64), C.byref(i64)) == native.MCG_EINVAL
+    assert L.mcg_group_stats(None, C.byref(i64), C.byref(i64), C.byref(i64)) == native.MCG_EINVAL
+    d = C.c_double(0)
+    x = (C.c_double * 4)()
+    assert L.mcg_energy_host(None, x, x, x, C.byref(d)) == native.MCG_EINVAL
+    assert L.mcg_batch_save(None, b"/tmp/x.ckpt") == native.MCG_EINVAL
+    assert L.mcg_batch_load(None, b"/tmp/x.ckpt") == native.MCG_EINVAL
+    assert L.mcg_batch_sweep_logged(None, None, 0) == native.MCG_EINVAL
     assert b"null" in L.mcg_last_error()
 
 

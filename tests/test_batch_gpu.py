@@ -349,3 +349,70 @@ def test_phase_timing_adds_up():
     assert lists > 0 and sweep > 0
     assert lists + sweep <= tot * 1.01 + 0.05
     assert np.all(B.stats()[0] == 4 * (B.sizes // 3))
+
+
+def _snapshot(B):
+    t, a, e = B.stats()
+    dt, dr = B.dmax()
+    return t, a, e, dt, dr, [B.coords(k) for k in range(B.nchains)], B.pairs()
+
+
+@pytest.mark.parametrize("shape", ["same", "other"])
+def test_checkpoint_resume_is_bit_exact(tmp_path, shape):
+    """Sweeping 4, saving, loading into a fresh batch of the same chains and sweeping 4 more gives
+    bitwise the chains of 8 sweeps without the save: coordinates, running energies, counters,
+    pair counts and adjusted dmax.  With shape 'other' the fresh batch starts with another launch
+    shape, and the load re-applies the saved one."""
+    chains = _waters((600, 1500, 900))
+    kw = dict(dmax_trn=0.15, dmax_rot=15.0, seed=9, dmax_each=(30, 30), dmax_target=(40.0, 40.0),
+              threads_per_chain=256, speculation=4, clusters=-1)
+    A = BatchChains(chains, **kw)
+    A.sweep(4)
+    ck = str(tmp_path / "batch.ckpt")
+    A.save(ck)
+    A.sweep(4)
+    want = _snapshot(A)
+    kw2 = dict(kw) if shape == "same" else dict(kw, threads_per_chain=512, speculation=0, clusters=0)
+    B = BatchChains(chains, **kw2)
+    B.sweep(1)                                  # state to be overwritten by the load
+    B.load(ck)
+    assert B.tuning()["threads_per_chain"] == 256
+    B.sweep(4)
+    got = _snapshot(B)
+    for w, g in zip(want[:5], got[:5]):
+        assert np.array_equal(w, g), (w, g)
+    for w, g in zip(want[5], got[5]):
+        assert np.array_equal(w, g)
+    # a checkpoint restores the pair counters too (statistics of the chain, not of the batch)
+    assert np.array_equal(want[6], got[6])
+    A.close()
+    B.close()
+
+
+def test_checkpoint_rejects_other_batches_and_damaged_files(tmp_path):
+    chains = _waters((600, 900))
+    A = BatchChains(chains, seed=9)
+    A.sweep(1)
+    ck = tmp_path / "a.ckpt"
+    A.save(str(ck))
+    other = BatchChains(chains, seed=10)                       # another Philox key
+    with pytest.raises(native.McgError) as ei:
+        other.load(str(ck))
+    assert ei.value.code == native.MCG_EINVAL
+    fewer = BatchChains(chains[:1], seed=9)
+    with pytest.raises(native.McgError) as ei:
+        fewer.load(str(ck))
+    assert ei.value.code == native.MCG_EINVAL
+    raw = ck.read_bytes()
+    (tmp_path / "short.ckpt").write_bytes(raw[:-100])
+    bad = bytearray(raw)
+    bad[len(raw) // 2] ^= 0x40
+    (tmp_path / "flip.ckpt").write_bytes(bytes(bad))
+    for name in ("short.ckpt", "flip.ckpt", "missing.ckpt"):
+        with pytest.raises(native.McgError) as ei:
+            A.load(str(tmp_path / name))
+        assert ei.value.code == native.MCG_EIO
+    # the batch is unchanged by the failed loads and still sweeps
+    t0 = A.stats()[0]
+    A.sweep(1)
+    assert (A.stats()[0] > t0).all()

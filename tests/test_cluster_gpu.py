@@ -18,6 +18,7 @@ pytestmark = pytest.mark.gpu
 KCAL = 418.4
 MIX_REL = 1e-6
 N_LIST_VARIANTS = 4
+N_CLUSTER_END = 6          # variants 4 and 5 are the cluster-pair kernels
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -34,7 +35,13 @@ def _check_variants(s, ff, want, tol=MIX_REL):
     scale = max(1.0, abs(want[3]), abs(want[4]))
     got = {}
     for v in range(nv):
-        ff.set_pair_kernel(v)
+        try:
+            ff.set_pair_kernel(v)
+        except native.McgError as err:
+            # the group-pair variants (tests/test_group_kernel_gpu.py) need the class table
+            if v >= N_CLUSTER_END and err.code == native.MCG_ENOTSUP:
+                continue
+            raise
         e = ff.getE10()
         rel = abs(e[0] - want[0]) / max(1.0, abs(want[0]))
         assert rel <= tol, (v, rel, e[0], want[0])
