@@ -294,9 +294,12 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
 /* Current launch shape (ms_per_sweep = 0). */
 int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out);
 /* Host-buffer run: when xyz_in != NULL, copy all chains' coordinates in (3*natoms doubles: x for
- * every atom of every chain, then y, then z), rebuild the lists and recompute the running
- * energies; run nsweeps sweeps; when xyz_out != NULL copy the coordinates back; fill accepted and
- * etot (nchains entries each, may be NULL).  Host-synchronous. */
+ * every atom of every chain, then y, then z); a chain whose coordinates differ from the device's
+ * takes them, has its lists rebuilt when an atom moved beyond the rebuild threshold and its running
+ * energy recomputed, while a chain given back exactly the coordinates of the last export is left
+ * as it is (the FP64 view of a 64-bit fixed-point coordinate converts back to a different one, so
+ * this keeps the chain's state exact); run nsweeps sweeps; when xyz_out != NULL copy the
+ * coordinates back; fill accepted and etot (nchains entries each, may be NULL).  Host-synchronous. */
 int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* xyz_out, int64_t* accepted,
                        double* etot);
 /* Mixed-precision recompute of every chain's energy over its neighbour lists (iu). */

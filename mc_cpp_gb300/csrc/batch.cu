@@ -904,7 +904,7 @@ template <int APR>
 __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __restrict__ chains, BatchGeom G,
                                                           const uint4* __restrict__ F, const int* __restrict__ res_chain,
                                                           const uint16_t* __restrict__ LST, const int* __restrict__ NL,
-                                                          double* e_res, int64_t nres_total) {
+                                                          double* e_res, int64_t nres_total, const int* __restrict__ only) {
     // A warp per residue r.  Lanes scan r's list 32 entries at a time; the entries q > r whose
     // first atom lies within rc + 2 extents of r's are compacted into the warp's ring in shared
     // memory, and each time 32 are pending every lane evaluates one residue pair: all atom pairs
@@ -925,6 +925,7 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t gr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gr < nres_total; gr += warps) {
         const int c = res_chain[gr];
+        if (only && !only[c]) continue;    // a chain whose energy is not asked for
         const ChainDev& C = chains[c];
         if (APR && C.apr != APR) continue;
         const int apr = APR ? APR : C.apr;
@@ -1031,10 +1032,10 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
 }
 
 __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const double* __restrict__ e_res,
-                                   ChainState* state, int nchains) {
+                                   ChainState* state, int nchains, const int* __restrict__ only) {
     __shared__ double sh[256];
     const int c = blockIdx.x;
-    if (c >= nchains) return;
+    if (c >= nchains || (only && !only[c])) return;
     const ChainDev& C = chains[c];
     double s = 0.0;
     for (int r = threadIdx.x; r < C.nres; r += blockDim.x) s += e_res[C.res0 + r];
@@ -1051,20 +1052,32 @@ __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const do
 // The chain's largest squared displacement from its list-build positions FB enters state.maxd2, so
 // the next list build (k_batch_bin) rebuilds exactly the chains whose imported atoms moved beyond
 // the rebuild threshold.  Launched with 256 threads per chain.
+// An atom whose three input coordinates equal the FP64 view of its current master (what
+// k_batch_export gave out) keeps its master: a chain whose atoms all come back unchanged is left
+// exactly as it was (changed[c] = 0), and its running energy stands.
 __global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz,
                                                       int64_t natoms, ulonglong4_32a* M, uint4* F,
-                                                      const uint4* __restrict__ FB, ChainState* state, int nchains) {
+                                                      const uint4* __restrict__ FB, ChainState* state, int* changed,
+                                                      int nchains) {
     __shared__ float s_max[8];
+    __shared__ int s_changed;
     const int c = blockIdx.x;
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     const int n = C.nres * C.apr;
+    if (threadIdx.x == 0) s_changed = 0;
+    __syncthreads();
     float dmax = 0.0f;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int64_t a = C.atom0 + i;
+        const ulonglong4_32a mo = M[a];
+        const double v[3] = {xyz[a], xyz[natoms + a], xyz[2 * natoms + a]};
+        if (v[0] == master_to_f64(mo.x, C.L[0]) && v[1] == master_to_f64(mo.y, C.L[1]) && v[2] == master_to_f64(mo.z, C.L[2]))
+            continue;
+        s_changed = 1;
         unsigned long long m[3];
         for (int k = 0; k < 3; k++) {
-            double u = xyz[k * natoms + a] * C.rL[k];
+            double u = v[k] * C.rL[k];
             u -= rint(u);
             if (u >= 0.5) u -= 1.0;
             m[k] = (unsigned long long)__double2ll_rn(u * TWO64);
@@ -1083,6 +1096,7 @@ __global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict
     if (threadIdx.x == 0) {
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) dmax = fmaxf(dmax, s_max[w]);
         state[c].maxd2 = fmaxf(state[c].maxd2, dmax);
+        changed[c] = s_changed;
     }
 }
 
@@ -1164,6 +1178,7 @@ struct mcg_batch {
     MoveLogDev* d_mlog = nullptr; // per-move records the next direct sweep launch writes (null: none)
     MoveLogDev* d_log = nullptr;  // their buffer (one record per residue of all chains), on first use
     double* d_eres = nullptr;     // per-residue energy shares (mixed recompute)
+    int* d_changed = nullptr;     // chains whose coordinates the last host import changed
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int threads = 256;
     int64_t rebuilds_seen = 0, launches = 0;
@@ -1178,7 +1193,7 @@ struct mcg_batch {
         if (d_cl_start) cudaFree(d_cl_start);
         void* p[] = {d_chains, d_state, d_order, d_M, d_F, d_FB, d_LST, d_NL, d_gorder, d_gcell, d_prm, d_tile_chain,
                      d_tile_first, d_part, d_xyz, d_gstarts, d_res_chain, d_eres, d_cta_start, d_gpos, d_item_chain,
-                     d_chain_item0, d_build, d_log};
+                     d_chain_item0, d_build, d_log, d_changed};
         for (void* q : p) if (q) cudaFree(q);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -1204,17 +1219,18 @@ struct mcg_batch {
         return MCG_OK;
     }
     int launch_build() { return launch_build(stream, 1); }
-    int launch_energy_list() {
+    // mixed recompute of the running energies: every chain, or the chains flagged in `only`
+    int launch_energy_list(const int* only = nullptr) {
         int r;
         if (!d_eres && (r = balloc_d(&d_eres, (size_t)nres))) return r;
         const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_energy_res<3><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
+            k_batch_energy_res<3><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
         else if (apr_all == 1)
-            k_batch_energy_res<1><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
+            k_batch_energy_res<1><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
         else
-            k_batch_energy_res<0><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres);
-        k_batch_energy_sum<<<nchains, 256, 0, stream>>>(d_chains, d_eres, d_state, nchains);
+            k_batch_energy_res<0><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
+        k_batch_energy_sum<<<nchains, 256, 0, stream>>>(d_chains, d_eres, d_state, nchains, only);
         BK(cudaGetLastError());
         launches += 2;
         return MCG_OK;
@@ -1910,14 +1926,16 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
     const size_t bytes = sizeof(double) * 3 * (size_t)b->natoms;
     int r;
     if ((xyz_in || xyz_out) && !b->d_xyz) { if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r; }
+    if (xyz_in && !b->d_changed && (r = balloc(&b->d_changed, (size_t)b->nchains))) return r;
     if (xyz_in) {
         BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
         k_batch_import<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M, b->d_F, b->d_FB,
-                                                          b->d_state, b->nchains);
+                                                          b->d_state, b->d_changed, b->nchains);
         BK(cudaGetLastError());
         b->launches++;
-        // lists of the chains whose atoms moved beyond the rebuild threshold, then the energies
-        if ((r = b->launch_build(b->stream, 0)) || (r = b->launch_energy_list())) return r;
+        // lists of the chains whose atoms moved beyond the rebuild threshold, then the energies of
+        // the chains whose coordinates changed
+        if ((r = b->launch_build(b->stream, 0)) || (r = b->launch_energy_list(b->d_changed))) return r;
     }
     if ((r = mcg_batch_sweep(b, nsweeps))) return r;
     if (xyz_out) {

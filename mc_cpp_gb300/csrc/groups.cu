@@ -130,50 +130,21 @@ __global__ void __launch_bounds__(GB_WARPS * 32) k_group_rows(const int* __restr
     }
 }
 
-// The pair terms of one masked atom pair (the terms of k_energy_list_mix's mix_batch, factored by
-// the row atom): ch + cl += q_j g (float-float), vs += eps_j (x^12 - x^6) f, with f the unscaled
-// switch polynomial and g = f / r.
-template <bool ISO>
-__device__ __forceinline__ void group_pair(uint4 fi, float sig_i, uint4 fj, const float4 pj, const GroupGeom& G,
-                                           float& ch, float& cl, float& vs) {
-    float r2;
-    if (ISO) {
-        const float ux = __int2float_rn((int)(fj.x - fi.x)), uy = __int2float_rn((int)(fj.y - fi.y)),
-                    uz = __int2float_rn((int)(fj.z - fi.z));
-        const float r2u = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-        r2 = fmaf(r2u, G.L2h, r2u * G.L2l);
-    } else {
-        const float dx = fixed_delta(fi.x, fj.x, G.Ls[0], G.Ll[0]), dy = fixed_delta(fi.y, fj.y, G.Ls[1], G.Ll[1]),
-                    dz = fixed_delta(fi.z, fj.z, G.Ls[2], G.Ll[2]);
-        r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    }
-    if (r2 <= G.c2) {
-        float rinv = rsqrtf(r2);
-        rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
-        const float uu = fmaxf(r2, G.n2);
-        const float a = G.c2 - uu;
-        const float f = a * a * fmaf(2.0f, uu, G.k3);
-        const float g = rinv * f;
-        float sm, er;
-        two_sum(ch, pj.x * g, sm, er);
-        ch = sm;
-        cl = fmaf(pj.y, g, cl + er);
-        const float y = (sig_i + pj.w) * rinv;
-        const float x2 = y * y;
-        const float x6 = x2 * x2 * x2;
-        vs = fmaf(pj.z, fmaf(x6, x6, -x6) * f, vs);
-    }
-}
-
-// The mixed-precision switched energy over the group rows: a warp per group row (the group's up
-// to 4 atoms in registers), a lane per entry (the partner group's atoms gathered as one run of
-// consecutive positions), the entry's masked atom pairs evaluated in turn.  Atom parameters come
-// from the class table in shared memory, indexed by the class the fixed-point mirror carries in w.
-template <bool ISO, int MINB>
+// The mixed-precision switched energy over the group rows: a warp per group row (the group's atoms
+// in registers), a lane per entry (the partner group's atoms gathered as one run of consecutive
+// fixed-point positions), the entry's G x G atom pairs evaluated without branches: a pair whose
+// mask bit is clear or that lies beyond the cutoff takes r^2 = rc^2, where the switch polynomial is
+// exactly 0.  Per entry and row atom the pair terms are summed in FP32 over the entry's (at most G)
+// partners, then added to the row atom's float-float Coulomb sum (TwoSum) and FP32 LJ sum, which
+// are multiplied by q_i and eps_i at the row's end (factored as in k_energy_list_mix).  Atom
+// parameters come from the class table in shared memory, indexed by the class the fixed-point
+// mirror carries in w.  G: the largest group size of the system (3 or 4); the next entry's
+// positions are loaded while the current one is evaluated.
+template <int G, bool ISO, int MINB, bool PF>
 __global__ void __launch_bounds__(GE_THREADS, MINB) k_energy_groups(const uint4* __restrict__ fx, const float4* __restrict__ cls,
                                                                     int ncls, const int* __restrict__ gstart, int ngroup,
                                                                     const int2* __restrict__ grow,
-                                                                    const int* __restrict__ glen, int gcap, GroupGeom G,
+                                                                    const int* __restrict__ glen, int gcap, GroupGeom Gm,
                                                                     double* part) {
     extern __shared__ float4 s_cls[];
     for (int c = threadIdx.x; c < ncls; c += blockDim.x) s_cls[c] = cls[c];
@@ -181,41 +152,94 @@ __global__ void __launch_bounds__(GE_THREADS, MINB) k_energy_groups(const uint4*
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const float c2 = Gm.c2, n2 = Gm.n2, k3 = Gm.k3;
     float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;
     for (int g = warp; g < ngroup; g += nwarps) {
-        const int a0 = gstart[g], ni = gstart[g + 1] - a0;   // 1..4, the same in every lane
-        uint4 fi[4];
-        float si[4];
+        const int a0 = gstart[g], ni = gstart[g + 1] - a0;   // 1..G, the same in every lane
+        uint4 fi[G];
+        float si[G];
 #pragma unroll
-        for (int a = 0; a < 4; a++) {
+        for (int a = 0; a < G; a++) {
             fi[a] = fx[a0 + (a < ni ? a : 0)];
             si[a] = s_cls[fi[a].w].w;
         }
-        float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f}, vs[4] = {0.f, 0.f, 0.f, 0.f};
+        float ch[G], cl[G], vs[G];
+#pragma unroll
+        for (int a = 0; a < G; a++) { ch[a] = 0.f; cl[a] = 0.f; vs[a] = 0.f; }
         const int m = glen[g];
         const int2* row = grow + (size_t)g * gcap;
+        // an entry is (first atom of the partner group, pair mask | (its size - 1) << 16); positions
+        // past the partner group's size repeat its first atom (their mask bits are clear)
+        int2 e = lane < m ? row[lane] : make_int2(a0, 0);
+        uint4 fj[G];
+#pragma unroll
+        for (int b = 0; b < G; b++) fj[b] = fx[e.x + (b <= (e.y >> 16) ? b : 0)];
         for (int k = lane; k < m; k += 32) {
-            const int2 e = row[k];
-            const int nj = (e.y >> 16) + 1;
-            uint4 fj[4];
-            float4 pj[4];
+            const int2 ec = e;
+            uint4 fc[G];
 #pragma unroll
-            for (int b = 0; b < 4; b++) fj[b] = fx[e.x + (b < nj ? b : 0)];
+            for (int b = 0; b < G; b++) fc[b] = fj[b];
+            // PF: the next entry's gathers are issued here, in flight while this one is evaluated;
+            // otherwise at the end of the iteration
+            if (PF) {
+                e = k + 32 < m ? row[k + 32] : make_int2(a0, 0);
 #pragma unroll
-            for (int b = 0; b < 4; b++) pj[b] = s_cls[fj[b].w];
+                for (int b = 0; b < G; b++) fj[b] = fx[e.x + (b <= (e.y >> 16) ? b : 0)];
+            }
+            const int mask = ec.y;
+            float4 pj[G];
 #pragma unroll
-            for (int a = 0; a < 4; a++) {
+            for (int b = 0; b < G; b++) pj[b] = s_cls[fc[b].w];
+#pragma unroll
+            for (int a = 0; a < G; a++) {
                 if (a >= ni) break;
+                float th = 0.f, tl = 0.f, tv = 0.f;
 #pragma unroll
-                for (int b = 0; b < 4; b++)
-                    if ((e.y >> (a * 4 + b)) & 1) group_pair<ISO>(fi[a], si[a], fj[b], pj[b], G, ch[a], cl[a], vs[a]);
+                for (int b = 0; b < G; b++) {
+                    float r2;
+                    if (ISO) {
+                        const float ux = __int2float_rn((int)(fc[b].x - fi[a].x)), uy = __int2float_rn((int)(fc[b].y - fi[a].y)),
+                                    uz = __int2float_rn((int)(fc[b].z - fi[a].z));
+                        const float r2u = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+                        r2 = fmaf(r2u, Gm.L2h, r2u * Gm.L2l);
+                    } else {
+                        const float dx = fixed_delta(fi[a].x, fc[b].x, Gm.Ls[0], Gm.Ll[0]);
+                        const float dy = fixed_delta(fi[a].y, fc[b].y, Gm.Ls[1], Gm.Ll[1]);
+                        const float dz = fixed_delta(fi[a].z, fc[b].z, Gm.Ls[2], Gm.Ll[2]);
+                        r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    }
+                    // masked out or beyond rc: r^2 = rc^2, where the switch polynomial is 0
+                    r2 = (((mask >> (a * 4 + b)) & 1) && r2 <= c2) ? r2 : c2;
+                    float rinv = rsqrtf(r2);
+                    rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
+                    const float uu = fmaxf(r2, n2);
+                    const float aa = c2 - uu;
+                    const float f = aa * aa * fmaf(2.0f, uu, k3);
+                    const float gg = rinv * f;
+                    th = fmaf(pj[b].x, gg, th);
+                    tl = fmaf(pj[b].y, gg, tl);
+                    const float y = (si[a] + pj[b].w) * rinv;
+                    const float x2 = y * y;
+                    const float x6 = x2 * x2 * x2;
+                    tv = fmaf(pj[b].z, fmaf(x6, x6, -x6) * f, tv);
+                }
+                float sm, er;
+                two_sum(ch[a], th, sm, er);
+                ch[a] = sm;
+                cl[a] += tl + er;
+                vs[a] += tv;
+            }
+            if (!PF) {
+                e = k + 32 < m ? row[k + 32] : make_int2(a0, 0);
+#pragma unroll
+                for (int b = 0; b < G; b++) fj[b] = fx[e.x + (b <= (e.y >> 16) ? b : 0)];
             }
         }
 #pragma unroll
-        for (int a = 0; a < 4; a++)
+        for (int a = 0; a < G; a++)
             if (a < ni) mix_row_flush(s_cls[fi[a].w], ch[a], cl[a], vs[a], EH, EL, VH, VL);
     }
-    block_reduce2(((double)EH + (double)EL) * G.inv_f1, ((double)VH + (double)VL) * G.inv_f1, part + 2 * blockIdx.x);
+    block_reduce2(((double)EH + (double)EL) * Gm.inv_f1, ((double)VH + (double)VL) * Gm.inv_f1, part + 2 * blockIdx.x);
 }
 
 template <typename T>
@@ -245,6 +269,8 @@ int GroupPairs::setup(const std::vector<int>& resid) {
     }
     ngroup = (int)gs.size();
     gs.push_back(n);
+    gmax = 1;
+    for (int g = 0; g < ngroup; g++) gmax = std::max(gmax, gs[g + 1] - gs[g]);
     int rc;
     if ((rc = galloc(&d_gstart, gs.size())) || (rc = galloc(&d_gof, (size_t)n)) || (rc = galloc(&d_glen, (size_t)ngroup)) ||
         (rc = galloc(&d_misc, 3)))
@@ -286,14 +312,15 @@ int GroupPairs::launch_energy(cudaStream_t st, int v, const uint4* fx, const flo
                               double* part) {
     const size_t smem = sizeof(float4) * (size_t)ncls;
     int blocks = 0;
-#define MCG_GROUP_ONE(ISO_, B_)                                                                                  \
+#define MCG_GROUP_ONE(GS_, ISO_, B_, PF_)                                                                        \
     blocks = 152 * B_;                                                                                            \
-    k_energy_groups<ISO_, B_><<<blocks, GE_THREADS, smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, gcap, G, part);
-    if (v == 0) {
-        if (G.iso) { MCG_GROUP_ONE(true, 2) } else { MCG_GROUP_ONE(false, 2) }
-    } else {
-        if (G.iso) { MCG_GROUP_ONE(true, 3) } else { MCG_GROUP_ONE(false, 3) }
-    }
+    k_energy_groups<GS_, ISO_, B_, PF_><<<blocks, GE_THREADS, smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, \
+                                                                          gcap, G, part);
+#define MCG_GROUP_G(GS_)                                                                                          \
+    if (v == 0) { if (G.iso) { MCG_GROUP_ONE(GS_, true, 2, true) } else { MCG_GROUP_ONE(GS_, false, 2, true) } }   \
+    else { if (G.iso) { MCG_GROUP_ONE(GS_, true, 3, false) } else { MCG_GROUP_ONE(GS_, false, 3, false) } }
+    if (gmax <= 3) { MCG_GROUP_G(3) } else { MCG_GROUP_G(4) }
+#undef MCG_GROUP_G
 #undef MCG_GROUP_ONE
     return blocks;
 }

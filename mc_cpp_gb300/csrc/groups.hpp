@@ -46,6 +46,7 @@ public:
 
     bool ok = false;
     int n = 0, ngroup = 0, gcap = 0;
+    int gmax = 1;                // largest group (atoms)
     int64_t nentries = 0;        // group pairs in the rows
     int64_t nbits = 0;           // atom pairs their masks encode (the source rows' size)
     int64_t build_launches = 0;

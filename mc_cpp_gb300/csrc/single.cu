@@ -408,6 +408,9 @@ __device__ __forceinline__ void mix_batch(const int (&j)[U], const uint4 (&fj)[U
                                           int i, uint4 fi, float4 pi, int k0, int m, float Ls0, float Ls1, float Ls2,
                                           float Ll0, float Ll1, float Ll2, float L2h, float L2l, float c2, float n2,
                                           float k3, float& ch, float& cl, float& vs) {
+    // the batch's terms are summed in FP32 (at most U per lane), then added to the row sums once;
+    // a slot past the row's end or beyond rc takes r^2 = rc^2, where the switch polynomial is 0
+    float th = 0.f, tl = 0.f;
 #pragma unroll
     for (int u = 0; u < U; u++) {
         if (k0 + u * 32 >= m) break;   // warp-uniform: this and later slots are past the row
@@ -423,23 +426,24 @@ __device__ __forceinline__ void mix_batch(const int (&j)[U], const uint4 (&fj)[U
                         dz = fixed_delta(fi.z, fj[u].z, Ls2, Ll2);
             r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         }
-        if (j[u] != i && r2 <= c2) {
-            float rinv = rsqrtf(r2);
-            rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
-            const float uu = fmaxf(r2, n2);
-            const float a = c2 - uu;
-            const float f = a * a * fmaf(2.0f, uu, k3);
-            const float g = rinv * f;
-            float sm, er;
-            two_sum(ch, pj[u].x * g, sm, er);
-            ch = sm;
-            cl = fmaf(pj[u].y, g, cl + er);
-            const float y = (pi.w + pj[u].w) * rinv;
-            const float x2 = y * y;
-            const float x6 = x2 * x2 * x2;
-            vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
-        }
+        r2 = (j[u] != i && r2 <= c2) ? r2 : c2;
+        float rinv = rsqrtf(r2);
+        rinv = rinv * fmaf(-0.5f * r2 * rinv, rinv, 1.5f);   // one Newton step
+        const float uu = fmaxf(r2, n2);
+        const float a = c2 - uu;
+        const float f = a * a * fmaf(2.0f, uu, k3);
+        const float g = rinv * f;
+        th = fmaf(pj[u].x, g, th);
+        tl = fmaf(pj[u].y, g, tl);
+        const float y = (pi.w + pj[u].w) * rinv;
+        const float x2 = y * y;
+        const float x6 = x2 * x2 * x2;
+        vs = fmaf(pj[u].z, fmaf(x6, x6, -x6) * f, vs);
     }
+    float sm, er;
+    two_sum(ch, th, sm, er);
+    ch = sm;
+    cl += tl + er;
 }
 
 // Mixed-precision switched energy over the half list for periodic boxes: the pair kernel.  A warp

@@ -207,9 +207,28 @@ def test_host_buffer_run_roundtrip():
     assert np.array_equal(got, out)
 
 
+def test_host_import_of_exported_coordinates_changes_nothing():
+    """Coordinates given back exactly as exported leave every chain as it was: a host-buffer run
+    of one sweep is bitwise one plain sweep (coordinates, running energies, counters)."""
+    ch = _waters((600, 900, 700), seed=35)
+    A = BatchChains(ch, seed=16)
+    B = BatchChains(ch, seed=16)
+    out = np.zeros((3, B.natoms))
+    for _ in range(2):
+        B.run_host(None, 0, out)
+        B.run_host(out.copy(), 1, out)
+        A.sweep(1)
+    for k in range(len(ch)):
+        assert np.array_equal(A.coords(k), B.coords(k))
+    for a, b in zip(A.stats(), B.stats()):
+        assert np.array_equal(a, b)
+    assert np.array_equal(np.concatenate([A.coords(k) for k in range(len(ch))]).T, out)
+
+
 def test_host_import_rebuilds_only_chains_that_moved():
     """Importing coordinates rebuilds the lists of exactly the chains whose atoms moved beyond the
-    rebuild threshold from their list-build positions; the energies are recomputed either way."""
+    rebuild threshold from their list-build positions, and recomputes the energies of the chains
+    whose coordinates changed."""
     ch = _waters((600, 900), seed=33)
     B = BatchChains(ch, seed=15)
     out = np.zeros((3, B.natoms))
