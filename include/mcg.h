@@ -221,7 +221,7 @@ typedef struct mcg_batch_opts {
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
-    int speculation;          /* moves evaluated together per chain: 0 = from box size, 1 = off, 2, 4, 8 */
+    int speculation;          /* moves evaluated together per chain: 0 = the widest the chain's size allows, 1 = off, 2, 4, 8 */
     int clusters;             /* 0 = automatic (on with 512-thread CTAs): the largest chains each run on a
                                  cluster of two CTAs (two SMs); -1 = off */
     /* dmax adjustment per move type (index 0 = TRN, 1 = ROT), as MC_metropolis::run does it
@@ -277,7 +277,7 @@ int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_
 typedef struct mcg_batch_tuning {
     int threads_per_chain;    /* 128, 256 or 512 */
     int ctas_per_sm;          /* persistent CTAs per SM (1, 2 or 4) */
-    int speculation;          /* cap on moves evaluated together per CTA (0 = box-size heuristic) */
+    int speculation;          /* cap on moves evaluated together per chain (0 = the widest the chain's size allows) */
     float ms_per_sweep;       /* device time of one sweep at that shape (0 if not measured) */
     int from_cache;           /* 1 when taken from the cache without trial sweeps */
     int clusters;             /* 1: the largest chains run on two-CTA clusters */

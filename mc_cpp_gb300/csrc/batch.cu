@@ -370,10 +370,11 @@ constexpr int KMAX = 8;                  // moves evaluated together, at most
 constexpr int RING = 64;                 // per-warp ring of compacted neighbour atoms (power of two)
 
 // What every warp needs of a move after the iteration's barrier (written by the first warp of the
-// move's group): residue, old first-atom position (conflicts), new and build positions of its
-// atoms (commit substitutes, far check) and the Metropolis draw.
+// move's group): residue, old and new positions of its atoms (interaction test, dE corrections,
+// commit substitutes), build positions (far check) and the Metropolis draw.
 struct MoveRec {
     uint4 fn[MAX_APR];                   // new mirror positions (w = slot)
+    uint4 fo[MAX_APR];                   // old mirror positions
     unsigned long long mn[MAX_APR][3];   // new master coordinates
     uint4 fb[MAX_APR];                   // build positions of the moved atoms
     uint4 fo0;                           // old position of the first atom
@@ -382,6 +383,49 @@ struct MoveRec {
     float lna;                           // -ln(alpha), FP32 estimate (NaN: decide in FP64)
     uint32_t ahi, alo;                   // Philox words of alpha in (0, 1] (u01d_open0)
 };
+
+// Metropolis test (MC_metropolis.cpp:175-204): accept when dE <= DBL_EPSILON, else when
+// alpha < exp(-beta dE).  dE = deh + del (float-float, iu).  Decided in FP32 when the margin is
+// clear (FP32 dE and beta are within 1e-6 relative, lna within 2e-5), in FP64 otherwise.
+__device__ __forceinline__ bool metropolis_accept(float deh, float del, const MoveRec& Q, float beta_f, double beta) {
+    const float hf = deh + del;
+    if (hf <= 0.0f) return true;
+    if (hf >= 1e-12f) {
+        const float tf = beta_f * hf, lna = Q.lna;
+        if (tf < lna - 1e-4f * fmaxf(1.0f, lna)) return true;
+        if (tf > lna + 1e-4f * fmaxf(1.0f, lna)) return false;
+        // inside the margin, or lna is NaN: FP64
+    }
+    const double de = (double)deh + (double)del;
+    return de <= 2.220446049250313e-16 || u01d_open0(Q.ahi, Q.alo) < exp(-beta * de);
+}
+
+// This lane's share of the change in move g's dE when the earlier move h of the same iteration is
+// accepted: the pair terms between the two residues, as differences between g's new and old
+// positions, with h at its new positions minus with h at its old ones.  The 2 apr^2 atom-pair terms
+// are spread over the warp's lanes; a pair out of range in both positions of g contributes exactly 0.
+// The displacements come straight from the fixed-point mirrors (exact minimum images); g's new
+// displacement is the old one less g's atom move, the minimum image for every pair within rc since
+// rc + the largest move <= L/2.
+__device__ __forceinline__ float pair_correction(const MoveRec& Qg, const MoveRec& Qh, int apr, int lane,
+                                                 const float4 (*tab)[MAX_APR], float Ls0, float Ls1, float Ls2,
+                                                 float Ll0, float Ll1, float Ll2, float c2, float n2, float k3) {
+    float s = 0.0f;
+    const int npr = apr * apr;
+    for (int t = lane; t < 2 * npr; t += 32) {
+        const int side = t >= npr ? 1 : 0;                 // 0: h new (+), 1: h old (-)
+        const int r = t - side * npr, j = r / apr, b = r - j * apr;
+        const uint4 a = Qg.fo[j], an = Qg.fn[j];
+        const uint4 hb = side ? Qh.fo[b] : Qh.fn[b];
+        const float dx = fdelta(a.x, hb.x, Ls0, Ll0), dy = fdelta(a.y, hb.y, Ls1, Ll1), dz = fdelta(a.z, hb.z, Ls2, Ll2);
+        const float mx = fdelta(a.x, an.x, Ls0, Ll0), my = fdelta(a.y, an.y, Ls1, Ll1), mz = fdelta(a.z, an.z, Ls2, Ll2);
+        const float4 tb = tab[j][hb.w];
+        int np = 0;
+        const float v = mixed_pair_delta_clamped(dx, dy, dz, mx, my, mz, tb.x, tb.y, tb.z, c2, n2, k3, np);
+        s += side ? -v : v;
+    }
+    return s;
+}
 
 // Per-move record of a logged sweep (mcg_batch_sweep_logged): the layout of mcg_batch_move, with
 // the proposed positions as raw 64-bit masters (the host converts them to Angstrom in place).
@@ -407,11 +451,13 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4 or 8
 // per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
 // before the iteration.  After the iteration's only block barrier every warp decides the moves in
-// order with the same data: move g stands while no earlier ACCEPTED move of the iteration can
-// interact with it (same residue, or first atoms within rc + 2 extents + 2 largest moves for old
-// and new positions), so its dE is the one the sequential chain computes and the chain equals the
-// sequential Metropolis chain.  The first move that fails the test and all later ones are
-// re-proposed next iteration from the same Philox counters.
+// order with the same data.  For each earlier ACCEPTED move h of the iteration that can interact
+// with move g (first atoms within rc + 2 extents + 2 largest moves), g's dE is corrected by the
+// change of the pair terms between the two residues (h's new minus h's old positions), so it is
+// the dE the sequential chain computes, and the test is taken on it: the chain equals the
+// sequential Metropolis chain up to FP32 summation order.  A move whose residue an earlier
+// accepted move of the iteration moved, and all later ones, are re-proposed next iteration from
+// the same Philox counters.
 //
 // Per iteration and warp: the warp draws its group's move from the Philox stream and applies it to
 // its residue (lanes = atoms; every warp of a group does this redundantly, so no barrier is needed
@@ -593,6 +639,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                         MoveRec& Q = cp ? *peer(&P[buf][grp]) : P[buf][grp];
                         if (lane < apr) {
                             Q.fn[lane] = fn;
+                            Q.fo[lane] = fo;
                             Q.mn[lane][0] = nx; Q.mn[lane][1] = ny; Q.mn[lane][2] = nz;
                             Q.fb[lane] = fb;
                         }
@@ -708,6 +755,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             float deh = 0.0f, del = 0.0f;           // dE of move `lane` as a float-float pair
             bool acc_raw = false;
             unsigned cm = 0;                        // earlier moves of the iteration move g may interact with
+            unsigned sr = 0;                        // earlier moves of the iteration that move g's residue
             {
                 // lane = g * WPG + w holds warp w's partial of move g; segmented butterfly over w
                 float2 v = lane < CL * NW ? s_red[buf][lane] : make_float2(0.0f, 0.0f);
@@ -723,36 +771,50 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 del = __shfl_sync(0xffffffffu, v.y, src);
             }
             if (lane < kk) {
-                // Metropolis test (MC_metropolis.cpp:175-204): accept when dE <= DBL_EPSILON, else
-                // when alpha < exp(-beta dE).  Decided in FP32 when the margin is clear (FP32 dE and
-                // beta are within 1e-6 relative), in FP64 otherwise.
-                const float hf = deh + del;
-                bool exact = false;
-                if (hf <= 0.0f) acc_raw = true;
-                else if (hf < 1e-12f) exact = true;
-                else {
-                    const float tf = C.beta_f * hf, lna = Q[lane].lna;
-                    if (tf < lna - 1e-4f * fmaxf(1.0f, lna)) acc_raw = true;
-                    else if (tf > lna + 1e-4f * fmaxf(1.0f, lna)) acc_raw = false;
-                    else exact = true;              // also when lna is NaN
-                }
-                if (exact) {
-                    const double de = (double)deh + (double)del;
-                    acc_raw = de <= 2.220446049250313e-16 || u01d_open0(Q[lane].ahi, Q[lane].alo) < exp(-C.beta * de);
-                }
+                acc_raw = metropolis_accept(deh, del, Q[lane], C.beta_f, C.beta);
                 for (int h = 0; h < lane; h++) {
+                    if (Q[h].res == Q[lane].res) { sr |= 1u << h; continue; }
                     const float dx = fdelta(Q[h].fo0.x, Q[lane].fo0.x, Ls0, Ll0);
                     const float dy = fdelta(Q[h].fo0.y, Q[lane].fo0.y, Ls1, Ll1);
                     const float dz = fdelta(Q[h].fo0.z, Q[lane].fo0.z, Ls2, Ll2);
-                    if (Q[h].res == Q[lane].res || dx * dx + dy * dy + dz * dz <= G.indep2) cm |= 1u << h;
+                    if (dx * dx + dy * dy + dz * dz <= G.indep2) cm |= 1u << h;
                 }
             }
-            const unsigned araw = __ballot_sync(0xffffffffu, acc_raw);
+            // In move order: move g stands unless an earlier accepted move of the iteration moved
+            // its residue.  Its dE was evaluated against the chain before the iteration; each
+            // earlier accepted move h that may interact with it changes only the pair terms
+            // between the two residues, so dE is corrected by those terms (pair_correction) and
+            // the test is taken again on the corrected value: the dE and decision of the
+            // sequential chain, up to FP32 summation order.
+            unsigned araw = __ballot_sync(0xffffffffu, acc_raw);
             unsigned accmask = 0;
             int ng = kk;
             for (int g = 0; g < kk; g++) {
-                const unsigned cmg = __shfl_sync(0xffffffffu, cm, g);
-                if (cmg & accmask) { ng = g; break; }
+                if (__shfl_sync(0xffffffffu, sr, g) & accmask) { ng = g; break; }
+                const unsigned cset = __shfl_sync(0xffffffffu, cm, g) & accmask;
+                if (cset) {                          // warp-uniform
+                    float ch = 0.0f;
+                    for (unsigned hm = cset; hm; hm &= hm - 1)
+                        ch += pair_correction(Q[g], Q[__ffs(hm) - 1], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f,
+                                              n2f, k3f);
+                    float cl = 0.0f;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float oh = __shfl_xor_sync(0xffffffffu, ch, o), ol = __shfl_xor_sync(0xffffffffu, cl, o);
+                        float sm, e;
+                        two_sum(ch, oh, sm, e);
+                        ch = sm;
+                        cl = cl + ol + e;
+                    }
+                    if (lane == g) {
+                        float sm, e;
+                        two_sum(deh, ch, sm, e);
+                        deh = sm;
+                        del = del + cl + e;
+                        acc_raw = metropolis_accept(deh, del, Q[g], C.beta_f, C.beta);
+                    }
+                    araw = __ballot_sync(0xffffffffu, acc_raw);
+                }
                 accmask |= araw & (1u << g);
             }
             // far check of the accepted moves (lane = g * apr + j) and the commits
@@ -1581,23 +1643,16 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         C.use_cells = (C.nc[0] >= 5 && C.nc[1] >= 5 && C.nc[2] >= 5 && C.nc[0] * C.nc[1] * C.nc[2] <= MAX_CELLS) ? 1 : 0;
         for (int k = 0; k < 3; k++) { C.Lf[k] = (float)C.L[k]; C.Lhalf[k] = (float)(0.5 * C.L[k]); }
         C.wrap_offsets = (rc + rext + mmax + span > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]))) ? 1 : 0;
-        // speculation width from the chance that two random residues are out of interaction range
+        // speculation width: a move is re-proposed only when an earlier accepted move of its
+        // iteration picked the same residue (interacting moves are corrected, not re-proposed);
+        // take the widest group in which that happens in under ~5% of the iterations (~0.5
+        // acceptance assumed)
         {
-            const double vol = C.L[0] * C.L[1] * C.L[2];
-            const double frac = 4.0 / 3.0 * PI * rind * rind * rind / vol;
-            const bool any_half = rind > 0.5 * std::min(C.L[0], std::min(C.L[1], C.L[2]));
-            // a move is re-proposed when an earlier accepted move of its group may interact with
-            // it (probability ~ frac * acceptance, ~0.45 assumed); take the widest group whose
-            // expected number of standing moves is >= 0.7 of its width
-            const double pc = std::min(1.0, frac * 0.45);
             int kh = 1;
-            for (int kw : {2, 4, 8}) {
-                double e = 0.0, surv = 1.0;
-                for (int g = 0; g < kw; g++) { e += surv; surv *= std::pow(1.0 - pc, g + 1); }
-                if (e >= 0.7 * kw) kh = kw;
-            }
-            B->kgeom.push_back(any_half ? 1 : KMAX);
-            B->kheur.push_back(any_half ? 1 : kh);
+            for (int kw : {2, 4, 8})
+                if (0.5 * 0.5 * kw * (kw - 1) / (double)C.nres <= 0.05) kh = kw;
+            B->kgeom.push_back(KMAX);
+            B->kheur.push_back(kh);
         }
         if (!C.use_cells) C.nc[0] = C.nc[1] = C.nc[2] = 1;
     }
@@ -1856,7 +1911,7 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     // (threads per CTA, CTAs per SM): one chain per SM at 512 threads (also as two waves), two
     // co-resident chains at 256, four at 128
     static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}};
-    static const int kSpec[] = {1, 2, 4, 8, 0};
+    static const int kSpec[] = {1, 2, 4, 0};   // 0: the widest width the chain's size allows (8 from 140 residues)
     struct Cand { int th, cp, sp, cl; float ms; };
     std::vector<Cand> cand;
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }
