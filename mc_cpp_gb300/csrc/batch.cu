@@ -90,7 +90,7 @@ struct ChainDev {
     float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
-    int kspec;            // moves evaluated together by the sweep (1, 2, 4 or 8)
+    int kspec;            // moves evaluated together by the sweep (1, 2, 4, 8 or 16)
     int wrap_offsets;     // box small enough that (b - a_0) - (a_k - a_0) may leave the minimum image
     float Lf[3], Lhalf[3];
     float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
@@ -366,17 +366,19 @@ __device__ void chain_rebuild(const ChainDev& C, const BatchGeom& G, const uint4
 }
 
 // ---- the sweep ------------------------------------------------------------------------------
-constexpr int KMAX = 8;                  // moves evaluated together, at most
+constexpr int KMAX = 16;                 // moves evaluated together, at most (8 for residues of more than 4 atoms)
 constexpr int RING = 64;                 // per-warp ring of compacted neighbour atoms (power of two)
 
 // What every warp needs of a move after the iteration's barrier (written by the first warp of the
 // move's group): residue, old and new positions of its atoms (interaction test, dE corrections,
 // commit substitutes), build positions (far check) and the Metropolis draw.
+// A: atoms per residue the kernel is compiled for (the record is sized for them).
+template <int A>
 struct MoveRec {
-    uint4 fn[MAX_APR];                   // new mirror positions (w = slot)
-    uint4 fo[MAX_APR];                   // old mirror positions
-    unsigned long long mn[MAX_APR][3];   // new master coordinates
-    uint4 fb[MAX_APR];                   // build positions of the moved atoms
+    uint4 fn[A];                         // new mirror positions (w = slot)
+    uint4 fo[A];                         // old mirror positions
+    unsigned long long mn[A][3];         // new master coordinates
+    uint4 fb[A];                         // build positions of the moved atoms
     uint4 fo0;                           // old position of the first atom
     int res;
     int rot;                             // move type: 0 translation, 1 rotation
@@ -387,7 +389,8 @@ struct MoveRec {
 // Metropolis test (MC_metropolis.cpp:175-204): accept when dE <= DBL_EPSILON, else when
 // alpha < exp(-beta dE).  dE = deh + del (float-float, iu).  Decided in FP32 when the margin is
 // clear (FP32 dE and beta are within 1e-6 relative, lna within 2e-5), in FP64 otherwise.
-__device__ __forceinline__ bool metropolis_accept(float deh, float del, const MoveRec& Q, float beta_f, double beta) {
+template <int A>
+__device__ __forceinline__ bool metropolis_accept(float deh, float del, const MoveRec<A>& Q, float beta_f, double beta) {
     const float hf = deh + del;
     if (hf <= 0.0f) return true;
     if (hf >= 1e-12f) {
@@ -407,7 +410,8 @@ __device__ __forceinline__ bool metropolis_accept(float deh, float del, const Mo
 // The displacements come straight from the fixed-point mirrors (exact minimum images); g's new
 // displacement is the old one less g's atom move, the minimum image for every pair within rc since
 // rc + the largest move <= L/2.
-__device__ __forceinline__ float pair_correction(const MoveRec& Qg, const MoveRec& Qh, int apr, int lane,
+template <int A>
+__device__ __forceinline__ float pair_correction(const MoveRec<A>& Qg, const MoveRec<A>& Qh, int apr, int lane,
                                                  const float4 (*tab)[MAX_APR], float Ls0, float Ls1, float Ls2,
                                                  float Ll0, float Ll1, float Ll2, float c2, float n2, float k3) {
     float s = 0.0f;
@@ -448,8 +452,8 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
     return ((unsigned long long)(long long)hi << 32) + lo;
 }
 
-// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4 or 8
-// per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
+// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4, 8 or
+// 16 per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
 // before the iteration.  After the iteration's only block barrier every warp decides the moves in
 // order with the same data.  For each earlier ACCEPTED move h of the iteration that can interact
 // with move g (first atoms within rc + 2 extents + 2 largest moves), g's dE is corrected by the
@@ -483,7 +487,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
     constexpr int NW = NT / 32;
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
     static_assert(CL == 1 || CL == 2, "clusters of one or two CTAs");
-    __shared__ MoveRec P[2][KMAX];
+    constexpr int KM = A <= 4 ? KMAX : 8;         // moves per iteration, at most (shared-memory records)
+    __shared__ MoveRec<A> P[2][KM];
     __shared__ float2 s_red[2][CL * NW];
     __shared__ float4 s_ring[NW][RING];
     __shared__ int s_cell[MAX_CELLS + 1];
@@ -517,7 +522,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         __syncthreads();
         const ChainDev& C = s_chain;
         const int apr = APR ? APR : C.apr;
-        const int K = C.kspec;                 // 1, 2, 4 or 8; K * apr <= 32 and CL * NT / K >= 32
+        const int K = C.kspec;                 // 1, 2, 4, 8 or 16 (<= KM); CL * NT / K >= 32
         const int KL = K / CL;                 // moves of this CTA
         const int GS = NT / KL;                // threads per move
         const int WPG = GS >> 5;               // warps per move
@@ -552,7 +557,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 for (int t = 0; t < 2; t++) if (to_adj[t] > 0) kk = min(kk, to_adj[t]);
             }
             const bool gact = grp < kk;
-            MoveRec* R = P[buf ^ 1];
+            MoveRec<A>* R = P[buf ^ 1];
             float acc = 0.0f;
             int np = 0;
             if (gact) {
@@ -636,7 +641,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     const float lna = q1.z >= 65536u ? -__logf(__uint2float_rn(q1.z) * 2.3283064365386963e-10f)
                                                      : __int_as_float(0x7fc00000);
                     for (int cp = 0; cp < CL; cp++) {
-                        MoveRec& Q = cp ? *peer(&P[buf][grp]) : P[buf][grp];
+                        MoveRec<A>& Q = cp ? *peer(&P[buf][grp]) : P[buf][grp];
                         if (lane < apr) {
                             Q.fn[lane] = fn;
                             Q.fo[lane] = fo;
@@ -751,7 +756,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             }
             unit_sync();
             // ---- decisions, identical in every warp: lane g < kk holds move g
-            const MoveRec* Q = P[buf];
+            const MoveRec<A>* Q = P[buf];
             float deh = 0.0f, del = 0.0f;           // dE of move `lane` as a float-float pair
             bool acc_raw = false;
             unsigned cm = 0;                        // earlier moves of the iteration move g may interact with
@@ -817,17 +822,20 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 }
                 accmask |= araw & (1u << g);
             }
-            // far check of the accepted moves (lane = g * apr + j) and the commits
+            // far check of the accepted moves (t = g * apr + j over the lanes) and the commits
             bool far = false;
             {
-                const int g = lane / apr, j = lane - g * apr;
                 float e2 = 0.0f;
-                if (g < ng && ((accmask >> g) & 1u)) {
-                    const float ex = fdelta(Q[g].fb[j].x, Q[g].fn[j].x, Ls0, Ll0);
-                    const float ey = fdelta(Q[g].fb[j].y, Q[g].fn[j].y, Ls1, Ll1);
-                    const float ez = fdelta(Q[g].fb[j].z, Q[g].fn[j].z, Ls2, Ll2);
-                    e2 = ex * ex + ey * ey + ez * ez;
-                    far = e2 > G.half_skin2;
+                for (int t = lane; t < ng * apr; t += 32) {
+                    const int g = t / apr, j = t - g * apr;
+                    if ((accmask >> g) & 1u) {
+                        const float ex = fdelta(Q[g].fb[j].x, Q[g].fn[j].x, Ls0, Ll0);
+                        const float ey = fdelta(Q[g].fb[j].y, Q[g].fn[j].y, Ls1, Ll1);
+                        const float ez = fdelta(Q[g].fb[j].z, Q[g].fn[j].z, Ls2, Ll2);
+                        const float d2 = ex * ex + ey * ey + ez * ez;
+                        e2 = fmaxf(e2, d2);
+                        far = far || d2 > G.half_skin2;
+                    }
                 }
                 if (warp == 0) {
                     for (int o = 16; o > 0; o >>= 1) e2 = fmaxf(e2, __shfl_xor_sync(0xffffffffu, e2, o));
@@ -841,8 +849,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             }
             if (mlog && rank == 0 && warp == 0) {   // logged sweep: the standing moves in chain order
                 MoveLogDev* lg = mlog + C.res0 + mv;
-                const int g = lane / apr, j = lane - g * apr;
-                if (g < ng) {
+                for (int t = lane; t < ng * apr; t += 32) {
+                    const int g = t / apr, j = t - g * apr;
                     lg[g].pos[j][0] = Q[g].mn[j][0];
                     lg[g].pos[j][1] = Q[g].mn[j][1];
                     lg[g].pos[j][2] = Q[g].mn[j][2];
@@ -1414,7 +1422,9 @@ struct mcg_batch {
             const int cl = (c < (int)clustered.size() && clustered[c]) ? 2 : 1;
             int k = cap <= 0 ? kheur[c] : std::min(cap, kgeom[c]);
             // a group is whole warps, and one warp holds the atoms of all moves of an iteration
-            while (k > 1 && (k > cl * threads / 32 || k * chains[c].apr > 32)) k >>= 1;
+            // a group is whole warps; the kernel for residues of more than 4 atoms holds 8 records
+            const int kcap = (apr_all == 1 || apr_all == 3) ? KMAX : 8;
+            while (k > 1 && (k > cl * threads / 32 || k > kcap)) k >>= 1;
             chains[c].kspec = std::max(k, cl);
         }
         spec_cap = cap;
@@ -1646,10 +1656,10 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         // speculation width: a move is re-proposed only when an earlier accepted move of its
         // iteration picked the same residue (interacting moves are corrected, not re-proposed);
         // take the widest group in which that happens in under ~5% of the iterations (~0.5
-        // acceptance assumed)
+        // acceptance assumed): 8 from 140 residues, 16 from 1,200
         {
             int kh = 1;
-            for (int kw : {2, 4, 8})
+            for (int kw : {2, 4, 8, 16})
                 if (0.5 * 0.5 * kw * (kw - 1) / (double)C.nres <= 0.05) kh = kw;
             B->kgeom.push_back(KMAX);
             B->kheur.push_back(kh);
@@ -1670,7 +1680,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if (B->threads != 128 && B->threads != 256 && B->threads != 512)
         return fail(MCG_EINVAL, "threads_per_chain must be 128, 256 or 512");
     if (opts->speculation < 0 || (opts->speculation & (opts->speculation - 1)) || opts->speculation > KMAX)
-        return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4 or 8");
+        return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4, 8 or 16");
     if (opts->ctas_per_sm < 0 || opts->ctas_per_sm > 8) return fail(MCG_EINVAL, "ctas_per_sm must be in [0, 8]");
     int dev = 0;
     cudaGetDevice(&dev);
@@ -1911,7 +1921,7 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
     // (threads per CTA, CTAs per SM): one chain per SM at 512 threads (also as two waves), two
     // co-resident chains at 256, four at 128
     static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}};
-    static const int kSpec[] = {1, 2, 4, 0};   // 0: the widest width the chain's size allows (8 from 140 residues)
+    static const int kSpec[] = {1, 2, 4, 8, 0};   // 0: the widest width the chain's size allows
     struct Cand { int th, cp, sp, cl; float ms; };
     std::vector<Cand> cand;
     if (!b->ev0) { BK(cudaEventCreate(&b->ev0)); BK(cudaEventCreate(&b->ev1)); }

@@ -267,9 +267,9 @@ def test_invalid_batches_rejected():
     assert ei.value.code == native.MCG_EINVAL
 
 
-@pytest.mark.parametrize("speculation,clusters", [(4, -1), (4, 0), (8, 0), (2, 0)])
+@pytest.mark.parametrize("speculation,clusters", [(4, -1), (4, 0), (8, 0), (2, 0), (16, -1), (16, 0)])
 def test_speculative_sweep_reproduces_sequential_chain(speculation, clusters):
-    """Moves evaluated together (up to 8, on one CTA or a two-CTA cluster) must give the
+    """Moves evaluated together (up to 16, on one CTA or a two-CTA cluster) must give the
     sequential chain: same random numbers, same decisions, same coordinates.  dE sums differ only
     in float summation order, so a decision could flip only at an exact tie (~1e-7 per move)."""
     ch = _waters((4000, 2600, 1500), seed=31)
@@ -313,7 +313,7 @@ def test_dmax_adjustment_follows_the_reference_rule():
         BatchChains(ch, dmax_each=(10, 0), dmax_max=(0.1, 0.0))      # cap below the initial dmax
 
 
-@pytest.mark.parametrize("speculation", [4, 8])
+@pytest.mark.parametrize("speculation", [4, 8, 16])
 def test_speculative_sweep_with_dmax_adjustment_is_sequential(speculation):
     """Iterations end at the move after which dmax is adjusted, so moves evaluated together share
     one dmax and the chain equals the sequential one, dmax included."""
@@ -341,7 +341,7 @@ def test_autotune_picks_a_shape_and_keeps_the_chain_exact(tmp_path, monkeypatch)
     B = BatchChains(ch, seed=8)
     t = B.autotune(trial_sweeps=1, use_cache=False)
     assert (t["threads_per_chain"], t["ctas_per_sm"]) in ((512, 1), (512, 2), (256, 2), (128, 4)) and t["clusters"] in (0, 1)
-    assert t["speculation"] in (0, 1, 2, 4) and t["ms_per_sweep"] > 0 and not t["from_cache"]
+    assert t["speculation"] in (0, 1, 2, 4, 8) and t["ms_per_sweep"] > 0 and not t["from_cache"]
     assert {k: t[k] for k in ("threads_per_chain", "ctas_per_sm", "speculation", "clusters")} == B.tuning()
     tr, a, etot = B.stats()
     sweeps = tr // (B.sizes // 3)                      # every shape: 1 warm-up + 1 timed sweep

@@ -18,8 +18,8 @@ and nothing else), the running energy equals the FP64 start energy plus the FP64
 accepted moves, and the device's FP64 recompute equals the restatement's total.
 
 Cases: the tuner's launch shape on water chains of 512-8192 molecules (the largest on a two-CTA
-cluster), one-CTA chains with speculation 8 and dmax adjustment, and argon chains (translations
-only).
+cluster), one-CTA chains with speculation 8 and dmax adjustment, chains with speculation 16 (one
+of them on a two-CTA cluster), and argon chains (translations only).
 """
 import json
 import os
@@ -51,6 +51,13 @@ CASES = {
                                              systems.water_box(3000, seed=46, temp=360.0)],
                              opts=dict(dmax_trn=0.15, dmax_rot=15.0, clusters=-1, speculation=8, threads_per_chain=256,
                                        dmax_each=(40, 40), dmax_target=(40.0, 40.0)), tune=False, sweeps=2),
+    # 16 moves per iteration: one warp per move on one CTA, two warps per move on a two-CTA cluster;
+    # in the 600-molecule box every pair of moves of an iteration may interact
+    "water_spec16": dict(chains=lambda: [systems.water_box(600, seed=47, temp=300.0),
+                                         systems.water_box(1300, seed=48, temp=330.0),
+                                         systems.water_box(4000, seed=49, temp=290.0)],
+                         opts=dict(dmax_trn=0.15, dmax_rot=15.0, clusters=0, speculation=16, threads_per_chain=512),
+                         tune=False, sweeps=2),
     "argon": dict(chains=lambda: [systems.argon_random(700, 0.02, 51, temp=120.0),
                                   systems.argon_random(1900, 0.016, 52, temp=95.0)],
                   opts=dict(dmax_trn=0.2, dmax_rot=0.0, clusters=-1), tune=False, sweeps=2),
