@@ -570,18 +570,19 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 const int piv = (int)(((uint64_t)q0.z * (uint64_t)apr) >> 32);
                 const int k = lane < apr ? lane : 0;
                 const int a = res * apr + k;
-                // the first neighbour indices of the list row, loaded before the move is formed so
-                // their latency overlaps the moved residue's loads and the move arithmetic
                 // lanes take list entries (neighbour residues), CH per lane in flight, each with all
-                // of its atoms
+                // of its atoms.  The neighbour indices of each chunk are loaded one chunk ahead (the
+                // first ones before the move is formed, so their latency overlaps the moved
+                // residue's loads and the move arithmetic): a chunk waits for its position loads
+                // only, not for an index load and then the positions.
                 constexpr int CH = A >= 3 ? 1 : (A == 2 ? 2 : 4);
                 const uint16_t* row = LST + (size_t)(C.res0 + res) * G.cap;
                 const int nent = NL[C.res0 + res];
-                int q_first[CH];
+                int qn[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
                     const int e = gw * 32 + u * GS + lane;
-                    q_first[u] = e < G.cap ? row[e] : 0;
+                    qn[u] = e < G.cap ? row[e] : 0;
                 }
                 uint4 fo = Fc[a];
                 ulonglong4_32a mo = Mc[a];
@@ -693,15 +694,17 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     int q[CH];
                     uint4 pb[CH][A];
 #pragma unroll
-                    for (int u = 0; u < CH; u++) {
-                        const int e = base + u * GS + lane;
-                        q[u] = e < nent ? (base == gw * 32 ? q_first[u] : (int)row[e]) : -1;
-                    }
+                    for (int u = 0; u < CH; u++) q[u] = base + u * GS + lane < nent ? qn[u] : -1;
 #pragma unroll
                     for (int u = 0; u < CH; u++)
 #pragma unroll
                         for (int b = 0; b < A; b++)
                             pb[u][b] = (q[u] >= 0 && b < apr) ? Fc[q[u] * apr + b] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+                    for (int u = 0; u < CH; u++) {   // the next chunk's indices
+                        const int e = base + CH * GS + u * GS + lane;
+                        qn[u] = e < nent ? (int)row[e] : 0;
+                    }
 #pragma unroll
                     for (int u = 0; u < CH; u++) {
                         if (base + u * GS >= nent) break;
