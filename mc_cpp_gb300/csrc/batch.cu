@@ -144,7 +144,7 @@ __device__ __forceinline__ int cell_coord(uint32_t v, int nc) {
 // 5x5x5 stencil is scanned; boxes with fewer than 5 cells per edge scan every residue.  A residue
 // q enters the list of r when their first atoms are within rc + skin + 2 extents (a superset of the
 // residues with an atom pair within rc + skin).  Before a sweep, a grid-wide pass (k_batch_bin +
-// k_batch_lists) rebuilds the lists of the chains whose atoms have moved more than ~0.55 half-skins
+// k_batch_lists) rebuilds the lists of the chains whose atoms have moved more than 0.7 half-skins
 // since their last build; inside a sweep, a chain whose atom has moved more than half the skin
 // rebuilds its own lists with its CTA (chain_rebuild) before the next move.  Lists are built a home
 // cell per warp: lane = home residue, candidates staged 32 at a time in shared memory.
@@ -1641,7 +1641,10 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
     const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
     G.indep2 = (float)(rind * rind);
-    G.pre2 = (float)((0.55 * 0.5 * skin) * (0.55 * 0.5 * skin));
+    // pre-sweep rebuild threshold: lower rebuilds more chains before each sweep, higher leaves more
+    // rebuilds to the chains' own CTAs inside the sweep; on the 256-chain water workload (steady
+    // state) 0.55, 0.75, 0.9 and 1.0 half-skins took 15.1, 14.7, 16.7 and 17.1 ms per sweep
+    G.pre2 = (float)((0.7 * 0.5 * skin) * (0.7 * 0.5 * skin));
     G.pair2 = (float)((rc + 2.0 * rext + 1e-3) * (rc + 2.0 * rext + 1e-3));
     {
         const double rs = rlist + 2 * rext + skin + 0.01;
