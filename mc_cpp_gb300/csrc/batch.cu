@@ -125,7 +125,6 @@ struct BatchGeom {
     float rcent2;      // (rc + skin + 2 rext)^2, residue-centre prefilter
     float half_skin2;  // (skin/2)^2
     float cellmin;     // cell edge for the 5-stencil
-    float skip2;       // (rc + extent from the first atom + largest move)^2: dE prefilter
     float indep2;      // (rc + 2 extents + 2 largest moves)^2: two moves cannot interact beyond it
     float subst2;      // (list centre radius + skin)^2: a residue farther than this is in no list of the other
     float pre2;        // a chain whose atoms moved less than this (squared) since the build keeps its lists
@@ -534,7 +533,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 (float)((double)C.tab[k / MAX_APR][k % MAX_APR][0] * (double)G.sw2f),
                 (float)((double)C.tab[k / MAX_APR][k % MAX_APR][1] * (double)G.sw2f), C.tab[k / MAX_APR][k % MAX_APR][2],
                 C.tab[k / MAX_APR][k % MAX_APR][3]);
-        const float c2f = G.c2f, n2f = G.n2f, k3f = G.c2f - 3.0f * G.n2f;
+        const float c2f = G.c2f, n2f = G.n2f, k3f = G.c2f - 3.0f * G.n2f, rcf = sqrtf(G.c2f);
         ChainState S = state[c];
         if (tid == 0) { s_err = 0; s_pairs = 0ull; }
         __syncthreads();
@@ -667,8 +666,32 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                     off[j][0] = __shfl_sync(0xffffffffu, ofx, j); off[j][1] = __shfl_sync(0xffffffffu, ofy, j);
                     off[j][2] = __shfl_sync(0xffffffffu, ofz, j);
                 }
-                // ---- neighbour atoms: compaction into the ring, evaluation 32 at a time
                 const bool wrap = C.wrap_offsets != 0;
+                // prefilter radius of this move: a neighbour atom b has a pair within rc of atom j,
+                // before or after the move, only if |b - c| <= rc + max_j |a_j - c| + max_j |m_j|
+                // (c: the residue's centroid before the move; its first atom in small boxes, where
+                // only displacements from the first atom are minimum images)
+                float cx = 0.0f, cy = 0.0f, cz = 0.0f, skip2;
+                {
+                    if (!wrap) {
+#pragma unroll
+                        for (int j = 1; j < A; j++)
+                            if (j < apr) { cx += off[j][0]; cy += off[j][1]; cz += off[j][2]; }
+                        const float ia = 1.0f / (float)apr;
+                        cx *= ia; cy *= ia; cz *= ia;
+                    }
+                    float ext2 = 0.0f, mv2 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < A; j++)
+                        if (j < apr) {
+                            const float dx = off[j][0] - cx, dy = off[j][1] - cy, dz = off[j][2] - cz;
+                            ext2 = fmaxf(ext2, dx * dx + dy * dy + dz * dz);
+                            mv2 = fmaxf(mv2, m[j][0] * m[j][0] + m[j][1] * m[j][1] + m[j][2] * m[j][2]);
+                        }
+                    const float rs = rcf + sqrtf(ext2) + sqrtf(mv2) + 1e-3f;
+                    skip2 = rs * rs;
+                }
+                // ---- neighbour atoms: compaction into the ring, evaluation 32 at a time
                 auto eval = [&](const float4 v) {
                     const uint32_t w = __float_as_uint(v.w);
 #pragma unroll
@@ -725,7 +748,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                             if (b >= apr) break;
                             const float ex = fdelta(fo0.x, pb[u][b].x, Ls0, Ll0), ey = fdelta(fo0.y, pb[u][b].y, Ls1, Ll1),
                                         ez = fdelta(fo0.z, pb[u][b].z, Ls2, Ll2);
-                            const bool keep = q[u] >= 0 && ex * ex + ey * ey + ez * ez <= G.skip2;
+                            const float ux = ex - cx, uy = ey - cy, uz = ez - cz;
+                            const bool keep = q[u] >= 0 && ux * ux + uy * uy + uz * uz <= skip2;
                             const unsigned bal = __ballot_sync(0xffffffffu, keep);
                             if (keep)
                                 ring[(head + __popc(bal & lt_mask)) & (RING - 1)] = make_float4(ex, ey, ez, __uint_as_float(pb[u][b].w));
@@ -1638,7 +1662,6 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     // the cutoff only while rc + |m| <= L/2 (m: the largest move of one atom)
     const double span = span_max + 0.01;   // rigid residues keep their intra-residue distances
     const double mmax = std::max(dmax_cap[0], 2.0 * span * std::sin(0.5 * dmax_cap[1] * PI / 180.0)) + 1e-6;
-    G.skip2 = (float)((rc + rext + mmax + 1e-3) * (rc + rext + mmax + 1e-3));
     const double rind = rc + 2.0 * rext + 2.0 * mmax + 1e-3;
     G.indep2 = (float)(rind * rind);
     // pre-sweep rebuild threshold: lower rebuilds more chains before each sweep, higher leaves more
