@@ -221,7 +221,7 @@ typedef struct mcg_batch_opts {
     int list_capacity;        /* 0 = automatic: maximum list entries per residue */
     uint64_t seed;            /* base seed; chain c uses (seed, c) as its Philox key */
     int ctas_per_sm;          /* persistent CTAs per SM the chains are packed onto (0 = 1) */
-    int speculation;          /* moves evaluated together per chain: 0 = the widest the chain's size allows, 1 = off, 2, 4, 8, 16 */
+    int speculation;          /* moves evaluated together per chain: 0 = the widest the chain's size allows, 1 = off, 2, 4, 8, 16, 32 */
     int clusters;             /* 0 = automatic (on with 512-thread CTAs): the largest chains each run on a
                                  cluster of two CTAs (two SMs); -1 = off */
     /* dmax adjustment per move type (index 0 = TRN, 1 = ROT), as MC_metropolis::run does it

@@ -90,7 +90,7 @@ struct ChainDev {
     float tofix32[3];     // 2^32 / L : Angstrom -> mirror units (master increments, master_step)
     int nc[3];            // cell grid for list builds
     int use_cells;        // 0: boxes too small for a 5-cell stencil; every residue is scanned
-    int kspec;            // moves evaluated together by the sweep (1, 2, 4, 8 or 16)
+    int kspec;            // moves evaluated together by the sweep (1, 2, 4, 8, 16 or 32)
     int wrap_offsets;     // box small enough that (b - a_0) - (a_k - a_0) may leave the minimum image
     float Lf[3], Lhalf[3];
     float Ls[3], Lsl[3];  // L / 2^32 as float-float: mirror units -> Angstrom
@@ -365,7 +365,7 @@ __device__ void chain_rebuild(const ChainDev& C, const BatchGeom& G, const uint4
 }
 
 // ---- the sweep ------------------------------------------------------------------------------
-constexpr int KMAX = 16;                 // moves evaluated together, at most (8 for residues of more than 4 atoms)
+constexpr int KMAX = 32;                 // moves evaluated together, at most (8 for residues of more than 4 atoms)
 constexpr int RING = 64;                 // per-warp ring of compacted neighbour atoms (power of two)
 
 // What every warp needs of a move after the iteration's barrier (written by the first warp of the
@@ -451,8 +451,8 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
     return ((unsigned long long)(long long)hi << 32) + lo;
 }
 
-// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4, 8 or
-// 16 per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
+// Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4, 8, 16
+// or 32 per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
 // before the iteration.  After the iteration's only block barrier every warp decides the moves in
 // order with the same data.  For each earlier ACCEPTED move h of the iteration that can interact
 // with move g (first atoms within rc + 2 extents + 2 largest moves), g's dE is corrected by the
@@ -487,10 +487,18 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
     static_assert(CL == 1 || CL == 2, "clusters of one or two CTAs");
     constexpr int KM = A <= 4 ? KMAX : 8;         // moves per iteration, at most (shared-memory records)
-    __shared__ MoveRec<A> P[2][KM];
+    // The move records and the cell starts of an in-sweep list rebuild share their memory: a
+    // rebuild runs after the iteration's decisions and commits, and the iteration after it reads
+    // no record of the one before (its commits have landed).
+    union SweepShared {
+        MoveRec<A> P[2][KM];
+        int cell[MAX_CELLS + 1];
+    };
+    __shared__ SweepShared s_u;
+    auto& P = s_u.P;
+    int* s_cell = s_u.cell;
     __shared__ float2 s_red[2][CL * NW];
     __shared__ float4 s_ring[NW][RING];
-    __shared__ int s_cell[MAX_CELLS + 1];
     __shared__ int s_err;
     __shared__ float4 s_tab[MAX_APR][MAX_APR];        // 16-byte aligned: read as float4
     __shared__ unsigned long long s_pairs;
@@ -521,7 +529,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
         __syncthreads();
         const ChainDev& C = s_chain;
         const int apr = APR ? APR : C.apr;
-        const int K = C.kspec;                 // 1, 2, 4, 8 or 16 (<= KM); CL * NT / K >= 32
+        const int K = C.kspec;                 // 1, 2, 4, 8, 16 or 32 (<= KM); CL * NT / K >= 32
         const int KL = K / CL;                 // moves of this CTA
         const int GS = NT / KL;                // threads per move
         const int WPG = GS >> 5;               // warps per move
@@ -1685,10 +1693,10 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
         // speculation width: a move is re-proposed only when an earlier accepted move of its
         // iteration picked the same residue (interacting moves are corrected, not re-proposed);
         // take the widest group in which that happens in under ~5% of the iterations (~0.5
-        // acceptance assumed): 8 from 140 residues, 16 from 1,200
+        // acceptance assumed): 8 from 140 residues, 16 from 1,200, 32 (two-CTA clusters) from 4,960
         {
             int kh = 1;
-            for (int kw : {2, 4, 8, 16})
+            for (int kw : {2, 4, 8, 16, 32})
                 if (0.5 * 0.5 * kw * (kw - 1) / (double)C.nres <= 0.05) kh = kw;
             B->kgeom.push_back(KMAX);
             B->kheur.push_back(kh);
@@ -1709,7 +1717,7 @@ int mcg_batch_create(const mcg_system_desc* descs, int nchains, const mcg_batch_
     if (B->threads != 128 && B->threads != 256 && B->threads != 512)
         return fail(MCG_EINVAL, "threads_per_chain must be 128, 256 or 512");
     if (opts->speculation < 0 || (opts->speculation & (opts->speculation - 1)) || opts->speculation > KMAX)
-        return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4, 8 or 16");
+        return fail(MCG_EINVAL, "speculation must be 0, 1, 2, 4, 8, 16 or 32");
     if (opts->ctas_per_sm < 0 || opts->ctas_per_sm > 8) return fail(MCG_EINVAL, "ctas_per_sm must be in [0, 8]");
     int dev = 0;
     cudaGetDevice(&dev);

@@ -267,9 +267,9 @@ def test_invalid_batches_rejected():
     assert ei.value.code == native.MCG_EINVAL
 
 
-@pytest.mark.parametrize("speculation,clusters", [(4, -1), (4, 0), (8, 0), (2, 0), (16, -1), (16, 0)])
+@pytest.mark.parametrize("speculation,clusters", [(4, -1), (4, 0), (8, 0), (2, 0), (16, -1), (16, 0), (32, 0)])
 def test_speculative_sweep_reproduces_sequential_chain(speculation, clusters):
-    """Moves evaluated together (up to 16, on one CTA or a two-CTA cluster) must give the
+    """Moves evaluated together (up to 16 on one CTA, 32 on a two-CTA cluster) must give the
     sequential chain: same random numbers, same decisions, same coordinates.  dE sums differ only
     in float summation order, so a decision could flip only at an exact tie (~1e-7 per move)."""
     ch = _waters((4000, 2600, 1500), seed=31)
