@@ -1009,7 +1009,9 @@ template <int APR>
 __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __restrict__ chains, BatchGeom G,
                                                           const uint4* __restrict__ F, const int* __restrict__ res_chain,
                                                           const uint16_t* __restrict__ LST, const int* __restrict__ NL,
-                                                          double* e_res, int64_t nres_total, const int* __restrict__ only) {
+                                                          double* e_res, int64_t nres_total, const int* __restrict__ only,
+                                                          const int* __restrict__ any) {
+    if (any && !*any) return;   // a masked recompute with no chain to recompute
     // A warp per residue r.  Lanes scan r's list 32 entries at a time; the entries q > r whose
     // first atom lies within rc + 2 extents of r's are compacted into the warp's ring in shared
     // memory, and each time 32 are pending every lane evaluates one residue pair: all atom pairs
@@ -1137,8 +1139,10 @@ __global__ void __launch_bounds__(256) k_batch_energy_res(const ChainDev* __rest
 }
 
 __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const double* __restrict__ e_res,
-                                   ChainState* state, int nchains, const int* __restrict__ only) {
+                                   ChainState* state, int nchains, const int* __restrict__ only,
+                                   const int* __restrict__ any) {
     __shared__ double sh[256];
+    if (any && !*any) return;
     const int c = blockIdx.x;
     if (c >= nchains || (only && !only[c])) return;
     const ChainDev& C = chains[c];
@@ -1159,7 +1163,9 @@ __global__ void k_batch_energy_sum(const ChainDev* __restrict__ chains, const do
 // the rebuild threshold.  Launched with 256 threads per chain.
 // An atom whose three input coordinates equal the FP64 view of its current master (what
 // k_batch_export gave out) keeps its master: a chain whose atoms all come back unchanged is left
-// exactly as it was (changed[c] = 0), and its running energy stands.
+// exactly as it was (changed[c] = 0), and its running energy stands.  changed[nchains] becomes 1
+// when any chain changed; changed[] is zeroed before the launch.  Grid: chains x slices of 256
+// atoms (a chain's slices stride over its atoms).
 __global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict__ chains, const double* __restrict__ xyz,
                                                       int64_t natoms, ulonglong4_32a* M, uint4* F,
                                                       const uint4* __restrict__ FB, ChainState* state, int* changed,
@@ -1170,10 +1176,11 @@ __global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     const int n = C.nres * C.apr;
+    if ((int)(blockIdx.y * blockDim.x) >= n) return;   // a slice past the chain's atoms (block-uniform)
     if (threadIdx.x == 0) s_changed = 0;
     __syncthreads();
     float dmax = 0.0f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x) {
         const int64_t a = C.atom0 + i;
         const ulonglong4_32a mo = M[a];
         const double v[3] = {xyz[a], xyz[natoms + a], xyz[2 * natoms + a]};
@@ -1200,8 +1207,12 @@ __global__ void __launch_bounds__(256) k_batch_import(const ChainDev* __restrict
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) dmax = fmaxf(dmax, s_max[w]);
-        state[c].maxd2 = fmaxf(state[c].maxd2, dmax);
-        changed[c] = s_changed;
+        // non-negative floats order as their bit patterns
+        atomicMax(reinterpret_cast<int*>(&state[c].maxd2), __float_as_int(dmax));
+        if (s_changed) {
+            atomicOr(&changed[c], 1);
+            atomicOr(&changed[nchains], 1);
+        }
     }
 }
 
@@ -1211,7 +1222,7 @@ __global__ void k_batch_export(const ChainDev* __restrict__ chains, const ulongl
     if (c >= nchains) return;
     const ChainDev& C = chains[c];
     const int n = C.nres * C.apr;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x) {
         const int64_t a = C.atom0 + i;
         const ulonglong4_32a m = M[a];
         xyz[a] = master_to_f64(m.x, C.L[0]);
@@ -1324,18 +1335,30 @@ struct mcg_batch {
         return MCG_OK;
     }
     int launch_build() { return launch_build(stream, 1); }
+    // slices of 256 atoms per chain for the per-atom host-buffer kernels: enough for the largest
+    // chain to take about 8 atoms per thread
+    int atom_slices() const {
+        int mx = 1;
+        for (const ChainDev& C : chains) mx = std::max(mx, C.nres * C.apr);
+        return std::max(1, std::min(64, (mx + 8 * 256 - 1) / (8 * 256)));
+    }
     // mixed recompute of the running energies: every chain, or the chains flagged in `only`
+    // (only[nchains] != 0 when any is: the kernels return at once when none is)
     int launch_energy_list(const int* only = nullptr) {
+        const int* any = only ? only + nchains : nullptr;
         int r;
         if (!d_eres && (r = balloc_d(&d_eres, (size_t)nres))) return r;
         const int blocks = (int)std::min<int64_t>((nres + 7) / 8, 152 * 16);
         if (apr_all == 3)
-            k_batch_energy_res<3><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
+            k_batch_energy_res<3><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only,
+                                                              any);
         else if (apr_all == 1)
-            k_batch_energy_res<1><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
+            k_batch_energy_res<1><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only,
+                                                              any);
         else
-            k_batch_energy_res<0><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only);
-        k_batch_energy_sum<<<nchains, 256, 0, stream>>>(d_chains, d_eres, d_state, nchains, only);
+            k_batch_energy_res<0><<<blocks, 256, 0, stream>>>(d_chains, G, d_F, d_res_chain, d_LST, d_NL, d_eres, nres, only,
+                                                              any);
+        k_batch_energy_sum<<<nchains, 256, 0, stream>>>(d_chains, d_eres, d_state, nchains, only, any);
         BK(cudaGetLastError());
         launches += 2;
         return MCG_OK;
@@ -2028,11 +2051,13 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
     const size_t bytes = sizeof(double) * 3 * (size_t)b->natoms;
     int r;
     if ((xyz_in || xyz_out) && !b->d_xyz) { if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r; }
-    if (xyz_in && !b->d_changed && (r = balloc(&b->d_changed, (size_t)b->nchains))) return r;
+    if (xyz_in && !b->d_changed && (r = balloc(&b->d_changed, (size_t)b->nchains + 1))) return r;
     if (xyz_in) {
         BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
-        k_batch_import<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M, b->d_F, b->d_FB,
-                                                          b->d_state, b->d_changed, b->nchains);
+        BK(cudaMemsetAsync(b->d_changed, 0, sizeof(int) * ((size_t)b->nchains + 1), b->stream));
+        k_batch_import<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M,
+                                                                                  b->d_F, b->d_FB, b->d_state,
+                                                                                  b->d_changed, b->nchains);
         BK(cudaGetLastError());
         b->launches++;
         // lists of the chains whose atoms moved beyond the rebuild threshold, then the energies of
@@ -2041,7 +2066,8 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
     }
     if ((r = mcg_batch_sweep(b, nsweeps))) return r;
     if (xyz_out) {
-        k_batch_export<<<b->nchains, 256, 0, b->stream>>>(b->d_chains, b->d_M, b->natoms, b->d_xyz, b->nchains);
+        k_batch_export<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, b->d_M, b->natoms, b->d_xyz,
+                                                                                  b->nchains);
         BK(cudaGetLastError());
         b->launches++;
         BK(cudaMemcpyAsync(xyz_out, b->d_xyz, bytes, cudaMemcpyDeviceToHost, b->stream));
