@@ -498,6 +498,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
     auto& P = s_u.P;
     int* s_cell = s_u.cell;
     __shared__ float2 s_red[2][CL * NW];
+    __shared__ unsigned s_cm[KM], s_sr[KM];       // per move: earlier moves that may interact / moved its residue
+    __shared__ float2 s_corr[KM][KM];             // [g][h]: dE correction of move g if move h is accepted
     __shared__ float4 s_ring[NW][RING];
     __shared__ int s_err;
     __shared__ float4 s_tab[MAX_APR][MAX_APR];        // 16-byte aligned: read as float4
@@ -794,8 +796,6 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             const MoveRec<A>* Q = P[buf];
             float deh = 0.0f, del = 0.0f;           // dE of move `lane` as a float-float pair
             bool acc_raw = false;
-            unsigned cm = 0;                        // earlier moves of the iteration move g may interact with
-            unsigned sr = 0;                        // earlier moves of the iteration that move g's residue
             {
                 // lane = g * WPG + w holds warp w's partial of move g; segmented butterfly over w
                 float2 v = lane < CL * NW ? s_red[buf][lane] : make_float2(0.0f, 0.0f);
@@ -810,33 +810,26 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 deh = __shfl_sync(0xffffffffu, v.x, src);
                 del = __shfl_sync(0xffffffffu, v.y, src);
             }
-            if (lane < kk) {
-                acc_raw = metropolis_accept(deh, del, Q[lane], C.beta_f, C.beta);
-                for (int h = 0; h < lane; h++) {
-                    if (Q[h].res == Q[lane].res) { sr |= 1u << h; continue; }
-                    const float dx = fdelta(Q[h].fo0.x, Q[lane].fo0.x, Ls0, Ll0);
-                    const float dy = fdelta(Q[h].fo0.y, Q[lane].fo0.y, Ls1, Ll1);
-                    const float dz = fdelta(Q[h].fo0.z, Q[lane].fo0.z, Ls2, Ll2);
-                    if (dx * dx + dy * dy + dz * dz <= G.indep2) cm |= 1u << h;
+            // Interaction masks and dE corrections of the iteration's moves, one warp per move (warp
+            // w takes moves w, w + NW, ...; the records are in this CTA's shared memory): for move g,
+            // the earlier moves h that moved its residue (s_sr) or may interact with it (first atoms
+            // within rc + 2 extents + 2 largest moves, s_cm), and for each of the latter the change
+            // of the pair terms between the two residues (pair_correction), needed if h is accepted.
+            for (int g = warp; g < kk; g += NW) {
+                bool same = false, near = false;
+                if (lane < g) {
+                    same = Q[lane].res == Q[g].res;
+                    if (!same) {
+                        const float dx = fdelta(Q[lane].fo0.x, Q[g].fo0.x, Ls0, Ll0);
+                        const float dy = fdelta(Q[lane].fo0.y, Q[g].fo0.y, Ls1, Ll1);
+                        const float dz = fdelta(Q[lane].fo0.z, Q[g].fo0.z, Ls2, Ll2);
+                        near = dx * dx + dy * dy + dz * dz <= G.indep2;
+                    }
                 }
-            }
-            // In move order: move g stands unless an earlier accepted move of the iteration moved
-            // its residue.  Its dE was evaluated against the chain before the iteration; each
-            // earlier accepted move h that may interact with it changes only the pair terms
-            // between the two residues, so dE is corrected by those terms (pair_correction) and
-            // the test is taken again on the corrected value: the dE and decision of the
-            // sequential chain, up to FP32 summation order.
-            unsigned araw = __ballot_sync(0xffffffffu, acc_raw);
-            unsigned accmask = 0;
-            int ng = kk;
-            for (int g = 0; g < kk; g++) {
-                if (__shfl_sync(0xffffffffu, sr, g) & accmask) { ng = g; break; }
-                const unsigned cset = __shfl_sync(0xffffffffu, cm, g) & accmask;
-                if (cset) {                          // warp-uniform
-                    float ch = 0.0f;
-                    for (unsigned hm = cset; hm; hm &= hm - 1)
-                        ch += pair_correction(Q[g], Q[__ffs(hm) - 1], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f,
-                                              n2f, k3f);
+                const unsigned srg = __ballot_sync(0xffffffffu, same), cmg = __ballot_sync(0xffffffffu, near);
+                for (unsigned hm = cmg; hm; hm &= hm - 1) {
+                    const int h = __ffs(hm) - 1;
+                    float ch = pair_correction(Q[g], Q[h], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f, n2f, k3f);
                     float cl = 0.0f;
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) {
@@ -846,11 +839,33 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                         ch = sm;
                         cl = cl + ol + e;
                     }
+                    if (lane == 0) s_corr[g][h] = make_float2(ch, cl);
+                }
+                if (lane == 0) { s_cm[g] = cmg; s_sr[g] = srg; }
+            }
+            __syncthreads();
+            if (lane < kk) acc_raw = metropolis_accept(deh, del, Q[lane], C.beta_f, C.beta);
+            // In move order: move g stands unless an earlier accepted move of the iteration moved
+            // its residue.  Its dE was evaluated against the chain before the iteration; each
+            // earlier accepted move h that may interact with it changes only the pair terms
+            // between the two residues, so dE is corrected by those terms and the test is taken
+            // again on the corrected value: the dE and decision of the sequential chain, up to FP32
+            // summation order.
+            unsigned araw = __ballot_sync(0xffffffffu, acc_raw);
+            unsigned accmask = 0;
+            int ng = kk;
+            for (int g = 0; g < kk; g++) {
+                if (s_sr[g] & accmask) { ng = g; break; }
+                const unsigned cset = s_cm[g] & accmask;
+                if (cset) {                          // warp-uniform
                     if (lane == g) {
-                        float sm, e;
-                        two_sum(deh, ch, sm, e);
-                        deh = sm;
-                        del = del + cl + e;
+                        for (unsigned hm = cset; hm; hm &= hm - 1) {
+                            const float2 c = s_corr[g][__ffs(hm) - 1];
+                            float sm, e;
+                            two_sum(deh, c.x, sm, e);
+                            deh = sm;
+                            del = del + c.y + e;
+                        }
                         acc_raw = metropolis_accept(deh, del, Q[g], C.beta_f, C.beta);
                     }
                     araw = __ballot_sync(0xffffffffu, acc_raw);
