@@ -238,9 +238,12 @@ __device__ __forceinline__ void stencil_ranges(const ChainDev& C, const int* __r
 }
 
 // Lists of the residues of one work item of chain C (all 32 lanes of the calling warp): a home
-// cell when the chain uses cells, else 32 consecutive residues scanning every residue.  Lane =
-// home residue; each chunk of 32 candidates is staged in `stage` (32 entries, shared memory) and
-// tested by every lane, so a candidate costs one broadcast load and one distance per home residue.
+// cell when the chain uses cells, else 32 consecutive residues scanning every residue.  Lanes take
+// the candidates 32 at a time (the stencil's merged cell rows, at most two per (dz, dy) row of
+// the stencil, kept in `stage`, a per-warp shared-memory buffer of at least 50 int2); each chunk
+// is tested against the home residues in turn (lane h holds home residue h and its row's count),
+// and the candidates within range are appended to that residue's row by a ballot, in candidate
+// order.
 template <int APR>
 __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int item,
                            const int* __restrict__ starts, const int* __restrict__ g_order,
@@ -248,63 +251,69 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
     (void)g_order;
     const int apr = APR ? APR : C.apr;
     const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
     const bool cells = C.use_cells != 0;
     const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
     const float rc2 = G.rcent2;
     const int cap = G.cap;
-    int hb, he, hx = 0, hy = 0, hz = 0;
+    int hb, he;
+    int2* rng = reinterpret_cast<int2*>(stage);
+    int nr = 0;
     if (cells) {
         hb = starts[item];
         he = starts[item + 1];
-        hx = item % C.nc[0];
-        hy = (item / C.nc[0]) % C.nc[1];
-        hz = item / (C.nc[0] * C.nc[1]);
+        const int hx = item % C.nc[0], hy = (item / C.nc[0]) % C.nc[1], hz = item / (C.nc[0] * C.nc[1]);
+        stencil_ranges(C, starts, hx, hy, hz, [&](int b, int e) {
+            if (lane == 0) rng[nr] = make_int2(b, e);
+            nr++;
+        });
     } else {
         hb = item * 32;
         he = min(C.nres, hb + 32);
+        if (lane == 0) rng[0] = make_int2(0, C.nres);
+        nr = 1;
     }
+    __syncwarp();
     for (int h0 = hb; h0 < he; h0 += 32) {
-        const int hs = h0 + lane;
-        const bool act = hs < he;
-        int r = -1;
-        uint4 pa = make_uint4(0, 0, 0, 0);
-        if (act) {
-            if (cells) { pa = g_pos[hs]; r = (int)pa.w; }
-            else { r = hs; pa = Fc[(size_t)r * apr]; }
+        // up to 32 home residues at a time: lane h holds home residue h0 + h, its position and its
+        // row's entry count
+        const int nh = min(32, he - h0);
+        uint4 ph = make_uint4(0, 0, 0, 0);
+        int rh = 0;
+        if (lane < nh) {
+            if (cells) { ph = g_pos[h0 + lane]; rh = (int)ph.w; }
+            else { rh = h0 + lane; ph = Fc[(size_t)rh * apr]; }
         }
-        uint16_t* row = LST + (size_t)(C.res0 + (act ? r : 0)) * cap;
         int cnt = 0;
-        auto scan = [&](int b, int e) {
-            for (int k = b; k < e; k += 32) {
+        for (int q = 0; q < nr; q++) {
+            const int2 be = rng[q];
+            for (int k = be.x; k < be.y; k += 32) {
                 const int t = k + lane;
-                if (t < e) {
-                    uint4 v;
+                const bool valid = t < be.y;
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (valid) {
                     if (cells) v = g_pos[t];            // w = residue index
                     else { v = Fc[(size_t)t * apr]; v.w = (uint32_t)t; }
-                    stage[lane] = v;
                 }
-                __syncwarp();
-                const int m = min(32, e - k);
-                if (act) {
-                    for (int j = 0; j < m; j++) {
-                        const uint4 v = stage[j];
-                        const float dx = fdelta(pa.x, v.x, Ls0, Ll0), dy = fdelta(pa.y, v.y, Ls1, Ll1), dz = fdelta(pa.z, v.z, Ls2, Ll2);
-                        if ((int)v.w != r && dx * dx + dy * dy + dz * dz <= rc2) {
-                            if (cnt < cap) row[cnt] = (uint16_t)v.w;
-                            cnt++;
-                        }
-                    }
+                for (int h = 0; h < nh; h++) {
+                    const uint32_t hx = __shfl_sync(0xffffffffu, ph.x, h), hy = __shfl_sync(0xffffffffu, ph.y, h),
+                                   hz = __shfl_sync(0xffffffffu, ph.z, h);
+                    const int r = __shfl_sync(0xffffffffu, rh, h);
+                    const float dx = fdelta(hx, v.x, Ls0, Ll0), dy = fdelta(hy, v.y, Ls1, Ll1), dz = fdelta(hz, v.z, Ls2, Ll2);
+                    const bool keep = valid && (int)v.w != r && dx * dx + dy * dy + dz * dz <= rc2;
+                    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                    const int pos = __shfl_sync(0xffffffffu, cnt, h) + __popc(bal & lt_mask);
+                    if (keep && pos < cap) LST[(size_t)(C.res0 + r) * cap + pos] = (uint16_t)v.w;
+                    if (lane == h) cnt += __popc(bal);
                 }
-                __syncwarp();
             }
-        };
-        if (cells) stencil_ranges(C, starts, hx, hy, hz, scan);
-        else scan(0, C.nres);
-        if (act) {
-            NL[C.res0 + r] = min(cnt, cap);
+        }
+        if (lane < nh) {
+            NL[C.res0 + rh] = min(cnt, cap);
             if (cnt > cap) atomicExch(err_out, MCG_ECAPACITY);
         }
     }
+    __syncwarp();   // the range buffer is free for the warp's next item
 }
 
 __device__ __forceinline__ int chain_items(const ChainDev& C) {
