@@ -507,7 +507,9 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
     auto& P = s_u.P;
     int* s_cell = s_u.cell;
     __shared__ float2 s_red[2][CL * NW];
-    __shared__ unsigned s_cm[KM], s_sr[KM];       // per move: earlier moves that may interact / moved its residue
+    // per move: earlier moves of the iteration that may interact with it / moved its residue; two
+    // buffers by iteration parity (an iteration clears its buffer before its first barrier)
+    __shared__ unsigned s_cm[2][KM], s_sr[2][KM];
     __shared__ float2 s_corr[KM][KM];             // [g][h]: dE correction of move g if move h is accepted
     __shared__ float4 s_ring[NW][RING];
     __shared__ int s_err;
@@ -576,6 +578,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             }
             const bool gact = grp < kk;
             MoveRec<A>* R = P[buf ^ 1];
+            if (tid < KM) { s_cm[buf][tid] = 0u; s_sr[buf][tid] = 0u; }
             float acc = 0.0f;
             int np = 0;
             if (gact) {
@@ -819,38 +822,50 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
                 deh = __shfl_sync(0xffffffffu, v.x, src);
                 del = __shfl_sync(0xffffffffu, v.y, src);
             }
-            // Interaction masks and dE corrections of the iteration's moves, one warp per move (warp
-            // w takes moves w, w + NW, ...; the records are in this CTA's shared memory): for move g,
-            // the earlier moves h that moved its residue (s_sr) or may interact with it (first atoms
-            // within rc + 2 extents + 2 largest moves, s_cm), and for each of the latter the change
-            // of the pair terms between the two residues (pair_correction), needed if h is accepted.
-            for (int g = warp; g < kk; g += NW) {
-                bool same = false, near = false;
-                if (lane < g) {
-                    same = Q[lane].res == Q[g].res;
-                    if (!same) {
-                        const float dx = fdelta(Q[lane].fo0.x, Q[g].fo0.x, Ls0, Ll0);
-                        const float dy = fdelta(Q[lane].fo0.y, Q[g].fo0.y, Ls1, Ll1);
-                        const float dz = fdelta(Q[lane].fo0.z, Q[g].fo0.z, Ls2, Ll2);
-                        near = dx * dx + dy * dy + dz * dz <= G.indep2;
+            // Interaction masks and dE corrections of the iteration's moves (the records are in this
+            // CTA's shared memory): for move g, the earlier moves h that moved its residue (s_sr) or
+            // may interact with it (first atoms within rc + 2 extents + 2 largest moves, s_cm), and
+            // for each of the latter the change of the pair terms between the two residues
+            // (pair_correction), needed if h is accepted.  Pair (g, h < g), p = g (g - 1) / 2 + h, is
+            // tested by lane p / NW of warp p % NW, so the tests and the corrections of the near
+            // pairs (computed by the whole warp, one at a time) spread evenly over the warps.
+            {
+                const int npr = kk * (kk - 1) / 2;
+                for (int p0 = 0; p0 < npr; p0 += 32 * NW) {
+                    const int p = p0 + lane * NW + warp;
+                    int g = 0, h = 0;
+                    bool same = false, near = false;
+                    if (p < npr) {
+                        g = (int)(0.5f * (1.0f + sqrtf(1.0f + 8.0f * (float)p)));
+                        if (g * (g - 1) / 2 > p) g--;
+                        else if ((g + 1) * g / 2 <= p) g++;
+                        h = p - g * (g - 1) / 2;
+                        same = Q[h].res == Q[g].res;
+                        if (!same) {
+                            const float dx = fdelta(Q[h].fo0.x, Q[g].fo0.x, Ls0, Ll0);
+                            const float dy = fdelta(Q[h].fo0.y, Q[g].fo0.y, Ls1, Ll1);
+                            const float dz = fdelta(Q[h].fo0.z, Q[g].fo0.z, Ls2, Ll2);
+                            near = dx * dx + dy * dy + dz * dz <= G.indep2;
+                        }
                     }
-                }
-                const unsigned srg = __ballot_sync(0xffffffffu, same), cmg = __ballot_sync(0xffffffffu, near);
-                for (unsigned hm = cmg; hm; hm &= hm - 1) {
-                    const int h = __ffs(hm) - 1;
-                    float ch = pair_correction(Q[g], Q[h], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f, n2f, k3f);
-                    float cl = 0.0f;
+                    if (same) atomicOr(&s_sr[buf][g], 1u << h);
+                    if (near) atomicOr(&s_cm[buf][g], 1u << h);
+                    for (unsigned nb = __ballot_sync(0xffffffffu, near); nb; nb &= nb - 1) {
+                        const int l = __ffs(nb) - 1;
+                        const int gg = __shfl_sync(0xffffffffu, g, l), hh = __shfl_sync(0xffffffffu, h, l);
+                        float ch = pair_correction(Q[gg], Q[hh], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f, n2f, k3f);
+                        float cl = 0.0f;
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        const float oh = __shfl_xor_sync(0xffffffffu, ch, o), ol = __shfl_xor_sync(0xffffffffu, cl, o);
-                        float sm, e;
-                        two_sum(ch, oh, sm, e);
-                        ch = sm;
-                        cl = cl + ol + e;
+                        for (int o = 16; o > 0; o >>= 1) {
+                            const float oh = __shfl_xor_sync(0xffffffffu, ch, o), ol = __shfl_xor_sync(0xffffffffu, cl, o);
+                            float sm, e;
+                            two_sum(ch, oh, sm, e);
+                            ch = sm;
+                            cl = cl + ol + e;
+                        }
+                        if (lane == 0) s_corr[gg][hh] = make_float2(ch, cl);
                     }
-                    if (lane == 0) s_corr[g][h] = make_float2(ch, cl);
                 }
-                if (lane == 0) { s_cm[g] = cmg; s_sr[g] = srg; }
             }
             __syncthreads();
             if (lane < kk) acc_raw = metropolis_accept(deh, del, Q[lane], C.beta_f, C.beta);
@@ -864,8 +879,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
             unsigned accmask = 0;
             int ng = kk;
             for (int g = 0; g < kk; g++) {
-                if (s_sr[g] & accmask) { ng = g; break; }
-                const unsigned cset = s_cm[g] & accmask;
+                if (s_sr[buf][g] & accmask) { ng = g; break; }
+                const unsigned cset = s_cm[buf][g] & accmask;
                 if (cset) {                          // warp-uniform
                     if (lane == g) {
                         for (unsigned hm = cset; hm; hm &= hm - 1) {
