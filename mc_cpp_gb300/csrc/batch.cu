@@ -239,11 +239,11 @@ __device__ __forceinline__ void stencil_ranges(const ChainDev& C, const int* __r
 
 // Lists of the residues of one work item of chain C (all 32 lanes of the calling warp): a home
 // cell when the chain uses cells, else 32 consecutive residues scanning every residue.  Lanes take
-// the candidates 32 at a time (the stencil's merged cell rows, at most two per (dz, dy) row of
-// the stencil, kept in `stage`, a per-warp shared-memory buffer of at least 50 int2); each chunk
-// is tested against the home residues in turn (lane h holds home residue h and its row's count),
-// and the candidates within range are appended to that residue's row by a ballot, in candidate
-// order.
+// the candidates 32 at a time (the stencil's merged cell rows, at most two per (dz, dy) row of the
+// stencil); each chunk is tested against the home residues in turn (positions read from shared
+// memory; lane h holds home residue h's row count), and the candidates within range are appended
+// to that residue's row by a ballot, in candidate order.  `stage`: a per-warp shared-memory buffer
+// of 64 uint4, the ranges in its first half and the home residues in its second.
 template <int APR>
 __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* __restrict__ Fc, int item,
                            const int* __restrict__ starts, const int* __restrict__ g_order,
@@ -257,7 +257,8 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
     const float rc2 = G.rcent2;
     const int cap = G.cap;
     int hb, he;
-    int2* rng = reinterpret_cast<int2*>(stage);
+    int2* rng = reinterpret_cast<int2*>(stage);      // up to 50 ranges (400 bytes)
+    uint4* home = stage + 32;                          // the home residues of the current pass
     int nr = 0;
     if (cells) {
         hb = starts[item];
@@ -283,7 +284,10 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
         if (lane < nh) {
             if (cells) { ph = g_pos[h0 + lane]; rh = (int)ph.w; }
             else { rh = h0 + lane; ph = Fc[(size_t)rh * apr]; }
+            ph.w = (uint32_t)rh;
+            home[lane] = ph;
         }
+        __syncwarp();
         int cnt = 0;
         for (int q = 0; q < nr; q++) {
             const int2 be = rng[q];
@@ -296,10 +300,9 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
                     else { v = Fc[(size_t)t * apr]; v.w = (uint32_t)t; }
                 }
                 for (int h = 0; h < nh; h++) {
-                    const uint32_t hx = __shfl_sync(0xffffffffu, ph.x, h), hy = __shfl_sync(0xffffffffu, ph.y, h),
-                                   hz = __shfl_sync(0xffffffffu, ph.z, h);
-                    const int r = __shfl_sync(0xffffffffu, rh, h);
-                    const float dx = fdelta(hx, v.x, Ls0, Ll0), dy = fdelta(hy, v.y, Ls1, Ll1), dz = fdelta(hz, v.z, Ls2, Ll2);
+                    const uint4 hp = home[h];           // broadcast: position and residue index of home h
+                    const int r = (int)hp.w;
+                    const float dx = fdelta(hp.x, v.x, Ls0, Ll0), dy = fdelta(hp.y, v.y, Ls1, Ll1), dz = fdelta(hp.z, v.z, Ls2, Ll2);
                     const bool keep = valid && (int)v.w != r && dx * dx + dy * dy + dz * dz <= rc2;
                     const unsigned bal = __ballot_sync(0xffffffffu, keep);
                     const int pos = __shfl_sync(0xffffffffu, cnt, h) + __popc(bal & lt_mask);
@@ -312,6 +315,7 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
             NL[C.res0 + rh] = min(cnt, cap);
             if (cnt > cap) atomicExch(err_out, MCG_ECAPACITY);
         }
+        __syncwarp();   // home[] is rewritten for the next home residues
     }
     __syncwarp();   // the range buffer is free for the warp's next item
 }
@@ -346,7 +350,7 @@ __global__ void __launch_bounds__(256) k_batch_lists(const ChainDev* __restrict_
                                                      const int* __restrict__ g_order, const uint4* __restrict__ g_pos,
                                                      uint16_t* LST, int* NL, ChainState* state,
                                                      const int* __restrict__ build, int nitems) {
-    __shared__ uint4 s_stage[8][32];
+    __shared__ uint4 s_stage[8][64];   // per warp: the stencil's cell ranges and the home residues
     const int warp = threadIdx.x >> 5;
     const int warps = gridDim.x * 8;
     for (int it = blockIdx.x * 8 + warp; it < nitems; it += warps) {
