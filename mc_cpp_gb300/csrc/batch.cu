@@ -253,7 +253,7 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     const bool cells = C.use_cells != 0;
-    const float Ls0 = C.Ls[0], Ls1 = C.Ls[1], Ls2 = C.Ls[2], Ll0 = C.Lsl[0], Ll1 = C.Lsl[1], Ll2 = C.Lsl[2];
+    const float Lf0 = C.Ls[0] + C.Lsl[0], Lf1 = C.Ls[1] + C.Lsl[1], Lf2 = C.Ls[2] + C.Lsl[2];
     const float rc2 = G.rcent2;
     const int cap = G.cap;
     int hb, he;
@@ -302,7 +302,10 @@ __device__ void item_lists(const ChainDev& C, const BatchGeom& G, const uint4* _
                 for (int h = 0; h < nh; h++) {
                     const uint4 hp = home[h];           // broadcast: position and residue index of home h
                     const int r = (int)hp.w;
-                    const float dx = fdelta(hp.x, v.x, Ls0, Ll0), dy = fdelta(hp.y, v.y, Ls1, Ll1), dz = fdelta(hp.z, v.z, Ls2, Ll2);
+                    // displacements with the FP32 scale L / 2^32 (rounded): the list radius carries a
+                    // 0.01 A margin, far above the ~1e-6 A this rounding moves a distance
+                    const float dx = __int2float_rn((int)(v.x - hp.x)) * Lf0, dy = __int2float_rn((int)(v.y - hp.y)) * Lf1,
+                                dz = __int2float_rn((int)(v.z - hp.z)) * Lf2;
                     const bool keep = valid && (int)v.w != r && dx * dx + dy * dy + dz * dz <= rc2;
                     const unsigned bal = __ballot_sync(0xffffffffu, keep);
                     const int pos = __shfl_sync(0xffffffffu, cnt, h) + __popc(bal & lt_mask);
