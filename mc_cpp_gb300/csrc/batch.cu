@@ -338,7 +338,15 @@ __global__ void k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __
     if (threadIdx.x == 0) build[c] = need ? 1 : 0;
     if (!need) return;
     const ChainDev& C = chains[c];
-    chain_bin(C, F, FB, g_starts + (size_t)c * (MAX_CELLS + 1), g_order + C.res0, g_cell + C.res0, g_pos + C.res0);
+    // the cell starts are counted, summed and used as fill cursors in shared memory, then copied
+    // out for k_batch_lists
+    __shared__ int s_starts[MAX_CELLS + 1];
+    chain_bin(C, F, FB, s_starts, g_order + C.res0, g_cell + C.res0, g_pos + C.res0);
+    if (C.use_cells) {
+        int* gs = g_starts + (size_t)c * (MAX_CELLS + 1);
+        const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
+        for (int k = threadIdx.x; k <= ncell; k += blockDim.x) gs[k] = s_starts[k];
+    }
     if (threadIdx.x == 0) {
         state[c].maxd2 = 0.0f;
         state[c].rebuilds++;
