@@ -327,9 +327,11 @@ __device__ __forceinline__ int chain_items(const ChainDev& C) {
     return C.use_cells ? C.nc[0] * C.nc[1] * C.nc[2] : (C.nres + 31) / 32;
 }
 
-// Per-chain binning before a sweep, one CTA per chain: only chains that were asked to (force) or
-// whose atoms moved more than sqrt(pre2) since their last build; build[c] tells k_batch_lists.
-__global__ void k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __restrict__ F, uint4* FB, int* g_starts,
+// Per-chain binning before a sweep, one CTA of 1024 threads per chain: only chains that were asked
+// to (force) or whose atoms moved more than sqrt(pre2) since their last build; build[c] tells
+// k_batch_lists.
+__global__ void __launch_bounds__(1024) k_batch_bin(const ChainDev* __restrict__ chains, const uint4* __restrict__ F, uint4* FB,
+                                                    int* g_starts,
                             int* g_order, int* g_cell, uint4* g_pos, ChainState* state, int* build, float pre2, int force,
                             int nchains) {
     const int c = blockIdx.x;
@@ -1372,7 +1374,7 @@ struct mcg_batch {
     // list build: per-chain binning (every chain when force, else the chains that moved enough),
     // then one warp per home cell of the binned chains over the GPU
     int launch_build(cudaStream_t st, int force) {
-        k_batch_bin<<<nchains, 256, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, d_gpos, d_state, d_build,
+        k_batch_bin<<<nchains, 1024, 0, st>>>(d_chains, d_F, d_FB, d_gstarts, d_gorder, d_gcell, d_gpos, d_state, d_build,
                                              G.pre2, force, nchains);
         const int blocks = (int)std::min<int64_t>((nitems + 7) / 8, 152 * 16);
         if (apr_all == 3)
