@@ -479,19 +479,21 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 
 // Speculative exact sweep.  Each iteration takes the next K moves of the chain (K = 1, 2, 4, 8, 16
 // or 32 per chain); the NT/K threads of group g (whole warps) evaluate move mv+g against the state
-// before the iteration.  After the iteration's only block barrier every warp decides the moves in
-// order with the same data.  For each earlier ACCEPTED move h of the iteration that can interact
-// with move g (first atoms within rc + 2 extents + 2 largest moves), g's dE is corrected by the
-// change of the pair terms between the two residues (h's new minus h's old positions), so it is
-// the dE the sequential chain computes, and the test is taken on it: the chain equals the
-// sequential Metropolis chain up to FP32 summation order.  A move whose residue an earlier
-// accepted move of the iteration moved, and all later ones, are re-proposed next iteration from
-// the same Philox counters.
+// before the iteration.  After the iteration barrier the CTA tests every pair of moves (g, h < g)
+// for a shared residue or possible interaction (first atoms within rc + 2 extents + 2 largest
+// moves) and computes, for each interacting pair, the change of the pair terms between the two
+// residues that h's move makes (h's new minus h's old positions); after a second, CTA-local
+// barrier every warp decides the moves in order with the same data: g's dE is corrected by the
+// terms of the earlier ACCEPTED moves that interact with it, so it is the dE the sequential chain
+// computes, and the test is taken on it: the chain equals the sequential Metropolis chain up to
+// FP32 summation order.  A move whose residue an earlier accepted move of the iteration moved, and
+// all later ones, are re-proposed next iteration from the same Philox counters.
 //
 // Per iteration and warp: the warp draws its group's move from the Philox stream and applies it to
 // its residue (lanes = atoms; every warp of a group does this redundantly, so no barrier is needed
 // before the pair loop).  It then scans its share of the residue's neighbour list: neighbour atoms
-// within rc + extent + largest move of the first atom are compacted, as displacements, into the
+// within rc + the residue's extent about its centroid + this move's largest atom displacement of
+// the centroid are compacted, as displacements from the first atom, into the
 // warp's ring in shared memory, and each time 32 are pending they are evaluated with all lanes busy
 // (old and new pair terms, mixed_pair_delta).  Commits are written by the first warp of each group
 // after the barrier; positions that a warp may read before they land come from the previous
