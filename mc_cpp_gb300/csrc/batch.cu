@@ -491,11 +491,12 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 //
 // Per iteration and warp: the warp draws its group's move from the Philox stream and applies it to
 // its residue (lanes = atoms; every warp of a group does this redundantly, so no barrier is needed
-// before the pair loop).  It then scans its share of the residue's neighbour list: neighbour atoms
-// within rc + the residue's extent about its centroid + this move's largest atom displacement of
-// the centroid are compacted, as displacements from the first atom, into the
-// warp's ring in shared memory, and each time 32 are pending they are evaluated with all lanes busy
-// (old and new pair terms, mixed_pair_delta).  Commits are written by the first warp of each group
+// before the pair loop).  It then scans its share of the residue's neighbour list: the neighbour
+// atoms whose distance from the residue's centroid is within rc + the residue's extent about the
+// centroid + this move's largest atom displacement are compacted, as displacements from the first
+// atom, into the warp's ring in shared memory, and each time 32 are pending they are evaluated
+// with all lanes busy (old and new pair terms, mixed_pair_delta).  Commits are written by the
+// first warp of each group
 // after the barrier; positions that a warp may read before they land come from the previous
 // iteration's move records instead.
 //
