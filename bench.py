@@ -20,8 +20,11 @@ host-buffer API (coordinates copied in and out every step, wall clock); `rooflin
 throughput of the sweep kernel alone (its launches timed by event-record nodes inside the sweep
 graph; 68 flops per pair interaction: distance + minimum image 23, square root and inverse 5,
 Coulomb + LJ 30, accumulation 2, switch polynomial 8) against an FFMA probe measured in the same
-run; `cpu_baseline` = the reference's algorithm (oracle/ port, two full energies per move, one
-chain per host thread) on a bounded stratified sample of the same chains.
+run; `issue` = the sweep's warp-instruction issue rate (ncu instructions per move from
+profiles/k_batch_sweep_water256.md times the live trial rate) against four issue slots per SM per
+cycle at the sampled clock, the bound the sweep actually meets; `cpu_baseline` = the reference's
+algorithm (oracle/ port, two full energies per move, one chain per host thread) on a bounded
+stratified sample of the same chains.
 
 N GPUs (`--gpus N`, one rank per GPU; launched with torchrun by the driver, or by this script when
 started without it): the job's chains are the first 256*N of the same seeded generator, split
@@ -273,17 +276,38 @@ def hbm_rate(traffic, ms_per_sweep):
                                                   "profiles/k_batch_sweep_water256.md"}
 
 
-def traffic_from_profiles():
+def profile_figure(key):
+    """A figure recorded in profiles/k_batch_sweep_water256.md as a `key: value ...` line."""
     p = os.path.join(ROOT, "profiles", "k_batch_sweep_water256.md")
     if not os.path.exists(p):
         return None
     for ln in open(p):
-        if ln.startswith("dram_bytes_per_launch:"):
+        if ln.startswith(key + ":"):
             try:
                 return float(ln.split(":")[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def traffic_from_profiles():
+    return profile_figure("dram_bytes_per_launch")
+
+
+def issue_rate(trials_per_s, sm_mhz, nsm):
+    """The sweep's warp-instruction issue rate (ncu warp instructions per move, from the sweep's
+    profile, times the live trial rate) against the SMs' issue peak at the sampled clock: four
+    schedulers per SM, one warp instruction each per cycle.  The sweep is bound by issue, not by
+    FP32 throughput or DRAM, so this is its own roofline."""
+    per_move = profile_figure("warp_instructions_per_move")
+    if not per_move or not sm_mhz or not nsm:
+        return None
+    achieved = per_move * trials_per_s / 1e9
+    peak = 4.0 * nsm * sm_mhz * 1e6 / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "G warp instructions/s", "frac": achieved / peak,
+            "warp_instructions_per_move": per_move,
+            "source": "ncu smsp__inst_executed.sum per move of the sweep kernels (profiles/k_batch_sweep_water256.md), "
+                      "live trials/s, sampled SM clock, 4 issue slots per SM per cycle"}
 
 
 def run_ours(args):
@@ -321,6 +345,7 @@ def run_ours(args):
         barrier()
         ms, ms_lists, ms_sweep = B.time_phases(args.steps)
         barrier()
+    clk_summary = clk.summary()
     _, nl1 = B.counters()
     t1, a1, e1 = B.stats()
     p1 = B.pairs()
@@ -407,10 +432,12 @@ def run_ours(args):
                          "peak_source": "FFMA-chain probe kernel measured in this run (no FP32 figure in MEASURED_PEAKS.json)",
                          "kernel": "k_batch_sweep<3>", "flops_per_pair": FLOPS_PER_PAIR},
             "hbm": hbm_rate(traffic, ms_sweep / args.steps),
+            "issue": issue_rate(agg["trials_per_s"] * ms_max / max(ms_sweep, 1e-9), clk_summary.get("sm_mhz"),
+                                torch.cuda.get_device_properties(0).multi_processor_count),
             "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(nl1 - nl0),
             "list_rebuilds_total": int(rb),
-            "clocks": clk.summary(),
+            "clocks": clk_summary,
             "plain_fp64": plain,
             "batched_vs_plain_accepted": (value / plain["accepted_moves_per_s"]) if plain else None,
             "cpu_baseline": cpu,
