@@ -276,7 +276,7 @@ int mcg_batch_time_phases(mcg_batch* b, int nsweeps, float* ms_total, float* ms_
 /* Launch shape of the sweep kernel chosen by the autotuner. */
 typedef struct mcg_batch_tuning {
     int threads_per_chain;    /* 128, 256 or 512 */
-    int ctas_per_sm;          /* persistent CTAs per SM (1, 2 or 4) */
+    int ctas_per_sm;          /* persistent CTAs per SM (1, 2, 4 or 8) */
     int speculation;          /* cap on moves evaluated together per chain (0 = the widest the chain's size allows) */
     float ms_per_sweep;       /* device time of one sweep at that shape (0 if not measured) */
     int from_cache;           /* 1 when taken from the cache without trial sweeps */

@@ -505,7 +505,7 @@ __device__ __forceinline__ unsigned long long master_step(float d, float tofix32
 // shared memory (distributed shared memory), and the iteration's barrier is the cluster barrier.
 // In-sweep list rebuilds are done by CTA 0 while CTA 1 waits at the cluster barrier.
 template <int APR, int NT, int CL>
-__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4_32a* M,
+__global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : (APR == 1 ? 8 : 4))) k_batch_sweep(const ChainDev* __restrict__ chains, BatchGeom G, ulonglong4_32a* M,
                                                        uint4* F, uint4* FB, uint16_t* LST, int* NL, int* g_order,
                                                        int* g_cell, uint4* g_pos, ChainState* state,
                                                        const int* __restrict__ cta_start,
@@ -515,7 +515,8 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : 4)) k_bat
     constexpr int NW = NT / 32;
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
     static_assert(CL == 1 || CL == 2, "clusters of one or two CTAs");
-    constexpr int KM = A <= 4 ? KMAX : 8;         // moves per iteration, at most (shared-memory records)
+    // moves per iteration, at most (shared-memory records): a warp per move at the least
+    constexpr int KM = (A <= 4 ? KMAX : 8) < NT * CL / 32 ? (A <= 4 ? KMAX : 8) : NT * CL / 32;
     // The move records and the cell starts of an in-sweep list rebuild share their memory: a
     // rebuild runs after the iteration's decisions and commits, and the iteration after it reads
     // no record of the one before (its commits have landed).
@@ -2038,8 +2039,9 @@ int mcg_batch_autotune(mcg_batch* b, int trial_sweeps, int use_cache, mcg_batch_
         return MCG_OK;
     }
     // (threads per CTA, CTAs per SM): one chain per SM at 512 threads (also as two waves), two
-    // co-resident chains at 256, four at 128
-    static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}};
+    // co-resident chains at 256, four at 128, and eight at 128 (co-resident for one-atom residues,
+    // whose kernel fits 64 registers)
+    static const int kShape[][2] = {{512, 1}, {512, 2}, {256, 2}, {128, 4}, {128, 8}};
     static const int kSpec[] = {1, 2, 4, 8, 0};   // 0: the widest width the chain's size allows
     struct Cand { int th, cp, sp, cl; float ms; };
     std::vector<Cand> cand;
