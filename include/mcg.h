@@ -194,7 +194,11 @@ int mcg_build_exclusions(const mcg_system_desc* desc, int* counts, int* entries,
  * With follow != NULL (nsteps*2 ints: imvtyp, accepted per step), accept decisions are taken from
  * it when they disagree with this engine's and the disagreement is a tie (the draw alpha within
  * 1e-6 of exp(-beta dE), or, when no alpha was drawn, |dE| <= 1e-6 iu); ties are counted in
- * *n_ties.  Any other disagreement, or a different move type, ends the run with MCG_EINVAL. */
+ * *n_ties.  Any other disagreement, or a different move type, ends the run with MCG_EINVAL.
+ * A run with neither trace nor follow, FP64, switched cutoff, periodic box, no bonded terms and
+ * translation moves only (at most 8 types, 64 atoms a move) runs on the device: one kernel
+ * launch per 50 steps draws, moves, decides and commits from the same mt19937 words, with the
+ * same draws, decisions and coordinates as the host loop. */
 int mcg_add_move(mcg_system* s, int type, int mode, const int* sele, double dmax, double target, int each);
 int mcg_metropolis_run(mcg_system* s, int nsteps, uint64_t seed, int acceptance_units, double* trace,
                        const int* follow, double* final_etot, int64_t* n_accepted, int64_t* n_ties);

@@ -331,6 +331,20 @@ static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int accepta
     if (rc) return rc;
     double etot = ener[0];
     int64_t acc = 0, ties = 0;
+    // Without per-step output, translation moves of atom sets that carry no bonded term in a
+    // periodic switched FP64 system run on the device, a launch per list-update period, on the same
+    // random words (SingleEngine::metropolis_device); every other run takes the host loop below.
+    bool all_trn = true;
+    for (const MoveKind& mk : s->moves) all_trn = all_trn && mk.type == MCG_MOVE_TRN;
+    if (!trace && !follow && save_each == 0 && all_trn && h.cut == MCG_CUT_SWITCH && h.pbc != MCG_PBC_NONE &&
+        h.prec == MCG_PREC_FP64 && !E.has_bonded_terms() && nmvtyp <= 8) {
+        rc = E.metropolis_device(gen, s->moves, beta, nsteps, &etot, &acc);
+        if (rc) return rc;
+        if (final_etot) *final_etot = etot;
+        if (n_accepted) *n_accepted = acc;
+        if (n_ties) *n_ties = 0;
+        return MCG_OK;
+    }
     std::vector<int> atoms;
     std::vector<double> nx, ny, nz;
     std::vector<double>& X = E.host_x;

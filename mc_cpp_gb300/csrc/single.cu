@@ -1735,6 +1735,289 @@ int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const do
     return MCG_OK;
 }
 
+// ---- device-resident Metropolis run (MC_metropolis::run, src/MC_metropolis.cpp:80-165) ---------
+// For translation moves of atom sets without bonded terms in a periodic switched system, with no
+// per-step output: the whole step runs on the device, a launch covering the steps up to the next
+// list update (MC_metropolis.cpp:151).  The random numbers are the reference's: the raw 32-bit words of
+// the host's std::mt19937, turned into doubles as libstdc++'s generate_canonical<double, 53> does
+// (two words, w0 + w1 2^32 rounded once, times 2^-64; a result of 1 becomes the largest double
+// below 1) and into uniform_real_distribution values as (b - a) u + a, every operation rounded on
+// its own as the reference's uncontracted host code rounds it.
+constexpr int RP_MAXT = 8;       // move types
+constexpr int RP_MAXM = 64;      // atoms of one move
+struct ReplayTables {
+    int nmvtyp;
+    int ninst[RP_MAXT];           // instances of each move type
+    int ibase[RP_MAXT];           // first global instance of each type
+    int each[RP_MAXT];            // dmax adjustment period (0: never), MC::adjust_dmax (MC.cpp:165-173)
+    double target[RP_MAXT];       // target acceptance, percent
+    const int* inst_first;        // per global instance: its first (first, last) atom range; one past the end last
+    const int* ranges;            // (first, last) atom pairs
+};
+struct ReplayState {
+    double etot;
+    long long acc;
+    long long cursor;             // random words consumed from the launch's buffer
+    int steps_done;               // the last step completed
+    int status;                   // 0 ok; 1 out of random words (resume after steps_done); 2 move too large
+    double dmax[RP_MAXT];
+    int acc_tmp[RP_MAXT];
+};
+
+__device__ __forceinline__ double rp_canonical(const uint32_t* __restrict__ w, long long& cur) {
+    const double sum = __dadd_rn((double)w[cur], __dmul_rn((double)w[cur + 1], 4294967296.0));
+    cur += 2;
+    const double r = __dmul_rn(sum, 5.421010862427522170037264e-20);   // 2^-64
+    return r >= 1.0 ? 0.99999999999999988898 : r;                       // nextafter(1, 0)
+}
+
+// Tools::rint wrap of one coordinate (PerConditions::applyPBC, PerConditions.cpp:244-285)
+__device__ __forceinline__ double rp_wrap(double v, double L, double rL) {
+    const double t = __dmul_rn(rL, v);
+    const double r = (double)(t >= 0.0 ? __double2int_rz(__dadd_rn(t, 0.5)) : __double2int_rz(__dsub_rn(t, 0.5)));
+    return __dsub_rn(v, __dmul_rn(L, r));
+}
+
+// One CTA runs the steps: GB300's FP64 pipe issues a warp's FP64 instruction over many cycles, so
+// a step is bound by the dependent FP64 operations of a pair evaluation, not by the number of SMs
+// (an 8-CTA cluster sharing the partners took 21.5 against 20.1 us per step on the 864-atom argon
+// box).
+__global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uint4* fx, PbcDev pbc, CutDev cut,
+                                                const int* __restrict__ nbr, const int* __restrict__ nup,
+                                                const int* __restrict__ nlo, int cap, const int* __restrict__ c14s,
+                                                const int* __restrict__ c14d, ReplayTables T,
+                                                const uint32_t* __restrict__ words, long long nwords, ReplayState* st,
+                                                int s0, int s1, double beta) {
+    __shared__ ReplayState S;
+    __shared__ int s_idx[RP_MAXM];
+    __shared__ double s_xyz[3 * RP_MAXM];
+    __shared__ int s_m, s_type, s_stop, s_acc;
+    __shared__ long long s_cur;
+    __shared__ double s_part[2][8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) S = *st;
+    __syncthreads();
+    for (int step = s0 + 1; step <= s1; step++) {
+        if (tid == 0) {
+            // the proposal: move type, instance, displacement in the unit ball times dmax (MC.cpp:142-156)
+            long long cur = S.cursor;
+            s_stop = 0;
+            if (cur + 256 > nwords) {            // 2 words per uniform: 4 for type and instance, 6 per ball draw, 2 to accept
+                s_stop = 1;
+                S.status = 1;
+            } else {
+                const int t = (int)__dmul_rn((double)T.nmvtyp, rp_canonical(words, cur));
+                const int g = T.ibase[t] + (int)__dmul_rn((double)T.ninst[t], rp_canonical(words, cur));
+                int m = 0;
+                for (int r = T.inst_first[g]; r < T.inst_first[g + 1]; r++)
+                    for (int a = T.ranges[2 * r]; a <= T.ranges[2 * r + 1]; a++) {
+                        if (m < RP_MAXM) s_idx[m] = a;
+                        m++;
+                    }
+                double rx, ry, rz, q;
+                bool out = false;
+                do {
+                    if (cur + 8 > nwords) { out = true; break; }
+                    rx = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
+                    ry = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
+                    rz = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
+                    q = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+                } while (q > 1.0);
+                if (out) {
+                    s_stop = 1;
+                    S.status = 1;
+                } else if (m > RP_MAXM) {
+                    s_stop = 1;
+                    S.status = 2;
+                } else {
+                    const double dm = S.dmax[t];
+                    rx = __dmul_rn(rx, dm); ry = __dmul_rn(ry, dm); rz = __dmul_rn(rz, dm);
+                    for (int i = 1; i < m; i++) {        // ascending atom order (the partner lookup bisects)
+                        const int v = s_idx[i];
+                        int k = i - 1;
+                        while (k >= 0 && s_idx[k] > v) { s_idx[k + 1] = s_idx[k]; k--; }
+                        s_idx[k + 1] = v;
+                    }
+                    for (int k = 0; k < m; k++) {
+                        const double4_32a p = pq[s_idx[k]];
+                        s_xyz[3 * k] = rp_wrap(__dadd_rn(p.x, rx), pbc.L[0], pbc.rL[0]);
+                        s_xyz[3 * k + 1] = rp_wrap(__dadd_rn(p.y, ry), pbc.L[1], pbc.rL[1]);
+                        s_xyz[3 * k + 2] = rp_wrap(__dadd_rn(p.z, rz), pbc.L[2], pbc.rL[2]);
+                    }
+                    s_m = m;
+                    s_type = t;
+                    s_cur = cur;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_stop) break;
+        // dE of the moved set over its Verlet partners and 1-4 pairs, FP64 (as k_delta_e)
+        const int m = s_m;
+        auto slot = [&](int j) -> int {
+            int lo = 0, hi = m - 1;
+            while (lo <= hi) {
+                const int mid = (lo + hi) >> 1, v = s_idx[mid];
+                if (v == j) return mid;
+                if (v < j) lo = mid + 1; else hi = mid - 1;
+            }
+            return -1;
+        };
+        double del = 0.0, dvd = 0.0;
+        const uint4 f0 = make_uint4(0, 0, 0, 0);
+        for (int k = 0; k < m; k++) {
+            const int a = s_idx[k];
+            const double4_32a ao = pq[a];
+            const double4_32a an = make_double4_32a(s_xyz[3 * k], s_xyz[3 * k + 1], s_xyz[3 * k + 2], ao.w);
+            auto visit = [&](int j, bool fourteen) {
+                const int sj = slot(j);
+                if (sj >= 0 && j < a) return;   // a pair of moved atoms, counted at its lower atom
+                const double4_32a jo = pq[j];
+                double4_32a jn = jo;
+                if (sj >= 0) { jn.x = s_xyz[3 * sj]; jn.y = s_xyz[3 * sj + 1]; jn.z = s_xyz[3 * sj + 2]; }
+                double e0, v0, e1, v1;
+                pair_energy<PREC_F64>(A, pbc, cut, fourteen, ao, f0, a, jo, f0, j, true, e0, v0);
+                pair_energy<PREC_F64>(A, pbc, cut, fourteen, an, f0, a, jn, f0, j, true, e1, v1);
+                del += e1 - e0;
+                dvd += v1 - v0;
+            };
+            const int* row = nbr + (size_t)a * cap;
+            const int u = nup[a], l = nlo[a];
+            for (int t = tid; t < u + l; t += blockDim.x) visit(t < u ? row[t] : row[cap - 1 - (t - u)], false);
+            for (int t = c14s[a] + tid; t < c14s[a + 1]; t += blockDim.x) visit(c14d[t], true);
+        }
+        del = warp_sum(del);
+        dvd = warp_sum(dvd);
+        if (lane == 0) { s_part[0][warp] = del; s_part[1][warp] = dvd; }
+        __syncthreads();
+        if (tid == 0) {
+            double se = 0.0, sv = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) { se += s_part[0][w]; sv += s_part[1][w]; }
+            const double de = CHGCHARMM * KCALTOIU * se + 4.0 * sv;
+            // MC_metropolis::apply_criterion (MC_metropolis.cpp:175-204)
+            long long cur = s_cur;
+            bool accepted;
+            // exp is CUDA's (at most 1 ulp from the exact value) where the host loop calls glibc's: the
+            // two runs can part only on a uniform within an ulp of the threshold
+            if (de <= 2.220446049250313e-16) accepted = true;
+            else accepted = rp_canonical(words, cur) < exp(-beta * de);
+            S.cursor = cur;
+            const int t = s_type;
+            if (accepted) {
+                S.acc_tmp[t]++;
+                S.etot += de;
+                S.acc++;
+            }
+            for (int tt = 0; tt < T.nmvtyp; tt++) {
+                if (T.each[tt] != 0 && (step % T.each[tt]) == 0) {
+                    const double ratio = (double)S.acc_tmp[tt] / (double)T.each[tt];
+                    S.dmax[tt] = ratio > T.target[tt] / 100 ? S.dmax[tt] * 1.10 : S.dmax[tt] * 0.9;
+                    S.acc_tmp[tt] = 0;
+                }
+            }
+            S.steps_done = step;
+            s_acc = accepted ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_acc) {
+            for (int k = tid; k < m; k += blockDim.x) {
+                const int a = s_idx[k];
+                double4_32a p = pq[a];
+                p.x = s_xyz[3 * k]; p.y = s_xyz[3 * k + 1]; p.z = s_xyz[3 * k + 2];
+                pq[a] = p;
+                uint4 f = fx[a];
+                f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]);
+                fx[a] = f;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) *st = S;
+}
+
+int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKind>& moves, double beta, int nsteps,
+                                    double* etot, int64_t* n_accepted) {
+    const int nt = (int)moves.size();
+    if (nt < 1 || nt > RP_MAXT) return fail(MCG_ENOTSUP, "device run: 1 to 8 move types");
+    ReplayTables T{};
+    ReplayState S{};
+    std::vector<int> first, ranges;
+    T.nmvtyp = nt;
+    for (int t = 0; t < nt; t++) {
+        const MoveKind& mk = moves[t];
+        T.ninst[t] = mk.ninst();
+        T.ibase[t] = (int)first.size();
+        T.each[t] = mk.each;
+        T.target[t] = mk.target;
+        S.dmax[t] = mk.dmax;
+        const int rb = (int)ranges.size() / 2;
+        for (int k = 0; k < mk.ninst(); k++) first.push_back(rb + mk.rstart[k]);
+        ranges.insert(ranges.end(), mk.ranges.begin(), mk.ranges.end());
+    }
+    first.push_back((int)ranges.size() / 2);
+    S.etot = *etot;
+    constexpr long long W = 8192;            // random words per launch
+    int* d_first = nullptr;
+    int* d_ranges = nullptr;
+    uint32_t* d_words = nullptr;
+    ReplayState* d_st = nullptr;
+    int rc = MCG_OK;
+    auto done = [&](int r) {
+        if (d_first) cudaFree(d_first);
+        if (d_ranges) cudaFree(d_ranges);
+        if (d_words) cudaFree(d_words);
+        if (d_st) cudaFree(d_st);
+        return r;
+    };
+    if ((rc = dalloc(&d_first, first.size())) || (rc = dalloc(&d_ranges, std::max<size_t>(1, ranges.size()))) ||
+        (rc = dalloc(&d_words, (size_t)W)) || (rc = dalloc(&d_st, 1)))
+        return done(rc);
+    if (cudaMemcpyAsync(d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        (!ranges.empty() &&
+         cudaMemcpyAsync(d_ranges, ranges.data(), sizeof(int) * ranges.size(), cudaMemcpyHostToDevice, stream) != cudaSuccess))
+        return done(fail(MCG_ECUDA, "device run: table upload"));
+    T.inst_first = d_first;
+    T.ranges = d_ranges;
+    std::vector<uint32_t> w((size_t)W);
+    long long filled = 0;
+    int step = 0;
+    while (step < nsteps) {
+        // the words not consumed yet, then fresh ones from the generator
+        const long long keep = filled - S.cursor;
+        if (keep > 0 && S.cursor > 0) std::memmove(w.data(), w.data() + S.cursor, sizeof(uint32_t) * (size_t)keep);
+        filled = std::max(0LL, keep);
+        while (filled < W) w[(size_t)filled++] = gen();
+        S.cursor = 0;
+        S.status = 0;
+        const int s1 = std::min(nsteps, (step / 50 + 1) * 50);     // up to the next list update
+        if (cudaMemcpyAsync(d_words, w.data(), sizeof(uint32_t) * (size_t)W, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+            cudaMemcpyAsync(d_st, &S, sizeof S, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+            return done(fail(MCG_ECUDA, "device run: upload"));
+        k_replay<<<1, 256, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
+                                        d_words, W, d_st, step, s1, beta);
+        launches++;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(&S, d_st, sizeof S, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            return done(fail(MCG_ECUDA, "device run: replay kernel"));
+        if (S.status == 2) return done(fail(MCG_ENOTSUP, "device run: a move of more than 64 atoms"));
+        step = S.steps_done;
+        if (S.status == 0 && step % 50 == 0) {
+            if ((rc = update_lists())) return done(rc);
+        }
+    }
+    // host mirror of the coordinates
+    std::vector<double4_32a> pqh((size_t)n);
+    if (cudaMemcpy(pqh.data(), d_pq, sizeof(double4_32a) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return done(fail(MCG_ECUDA, "device run: coordinates"));
+    for (int a = 0; a < n; a++) { host_x[a] = pqh[a].x; host_y[a] = pqh[a].y; host_z[a] = pqh[a].z; }
+    prune_dirty = true;
+    pending_m = 0;
+    *etot = S.etot;
+    *n_accepted = S.acc;
+    return done(MCG_OK);
+}
+
 int SingleEngine::commit() {
     if (pending_m <= 0) return fail(MCG_EINVAL, "no pending proposal to commit");
     // the pending proposal is still staged on the device: only delta_e writes d_stage, and each

@@ -1,6 +1,7 @@
 // Single-system engine (host object owning the device state of one FField_CUDA).
 #pragma once
 #include <cstdint>
+#include <random>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -25,6 +26,12 @@ public:
     int get_coords(double* x, double* y, double* z);
     int delta_e(int m, const int* atoms, const double* nx, const double* ny, const double* nz, double* de);
     int commit();
+    // MC_metropolis::run steps on the device (translation moves of atom sets without bonded terms,
+    // periodic switched FP64 systems, no per-step output): random words from gen, as the host loop
+    // draws them; etot in and out (iu), accepted moves out.
+    int metropolis_device(std::mt19937& gen, const std::vector<MoveKind>& moves, double beta, int nsteps, double* etot,
+                          int64_t* n_accepted);
+    bool has_bonded_terms() const { return !term_data.empty(); }
     // true when the pending proposal moves exactly atoms[0..m) (ascending) to x/y/z[atoms[k]]
     bool pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const;
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);

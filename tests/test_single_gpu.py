@@ -264,3 +264,32 @@ def test_metropolis_1e5_moves_match_the_reference_run():
     assert np.array_equal(tr[drawn, 10], ref["alpha"][drawn])               # the same alpha draws
     assert (np.abs(tr[:, 9] - ref["de"]) / KCAL).max() <= 1e-6
     assert abs(etot - g["final_etot"]) <= 1e-9 * abs(g["final_etot"])
+
+
+def test_device_metropolis_run_matches_the_reference_run():
+    """Without per-step output, the 864-atom argon run (translation moves, no bonded terms) runs on
+    the device, a launch per list-update period, on the reference's random words: over the 1e5
+    recorded moves it accepts exactly the reference's count and ends at its running energy."""
+    g = goldens.golden()["mc"]["argon864_long"]
+    s = goldens.system("argon864")
+    ff = FFieldCUDA(s, "fp64")
+    _, etot, nacc, nties = ff.metropolis(g["nsteps"], g["seed"], trace=False)
+    assert nties == 0
+    assert nacc == g["accepted"][0]
+    assert abs(etot - g["final_etot"]) <= 1e-9 * abs(g["final_etot"])
+
+
+def test_device_metropolis_run_equals_the_host_loop():
+    """The device run and the host loop (taken when a trace is asked for) make the same decisions
+    on the same seed and leave bitwise the same coordinates; their running energies differ only in
+    the summation order of the dE terms."""
+    s = goldens.system("argon864")
+    dev = FFieldCUDA(s, "fp64")
+    host = FFieldCUDA(s, "fp64")
+    _, e_dev, a_dev, _ = dev.metropolis(3000, 99, trace=False)
+    _, e_host, a_host, _ = host.metropolis(3000, 99, trace=True)
+    assert a_dev == a_host
+    assert np.array_equal(dev.coords(), host.coords())
+    assert abs(e_dev - e_host) <= 1e-10 * abs(e_host)
+    # the engines stay usable: a fresh energy equals the running one
+    assert abs(dev.getE() - e_dev) <= 1e-9 * abs(e_dev)
