@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <climits>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -242,6 +243,190 @@ __global__ void __launch_bounds__(GE_THREADS, MINB) k_energy_groups(const uint4*
     block_reduce2(((double)EH + (double)EL) * Gm.inv_f1, ((double)VH + (double)VL) * Gm.inv_f1, part + 2 * blockIdx.x);
 }
 
+// The same energy with two entries per lane in packed FP32: entries k and k + 1 of a row take the
+// two halves of float2 values, so one sm_100+ packed instruction (add, multiply or FMA on a
+// register pair) does the work of both.  The switch is evaluated as S = t^2 (3 - 2 t) on
+// t = clamp((rc^2 - r^2) / (rc^2 - ron^2), 0, 1), which is 1 below ron, the reference's polynomial
+// between ron and rc, and 0 beyond rc and for masked pairs (their r^2 is set to rc^2), so no
+// comparison or clamp of r^2 is needed; S is normalised, so the partial sums need no inv_f1.  The
+// partner atoms' parameters are read from per-parameter tables in shared memory straight into the
+// halves of each float2.  Per entry pair and row atom the terms are summed in FP32, then into the
+// row atom's float-float Coulomb sum and FP32 LJ sum as in k_energy_groups.
+//
+// Placement: a row of G atoms whose offsets from its first atom stay within emax (each component)
+// places the partner atoms relative to that first atom (one fixed-point difference and conversion
+// per partner atom, not per atom pair) and adds each row atom's own offset; every partner within
+// rc is then at its minimum image.  Other rows (fewer atoms, or wider than emax in small boxes)
+// take the per-pair fixed-point displacement, exact at any box size.  The choice is made once per
+// row and is the same in every lane.
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pk_dup(float a) { return make_float2(a, a); }
+
+// fixed-point displacements of two partner coordinates from base, in Angstrom (float-float scale)
+__device__ __forceinline__ float2 pk_delta(uint32_t base, uint32_t xa, uint32_t xb, float2 Lh, float2 Ll) {
+    const float2 f = make_float2(__int2float_rn((int)(xa - base)), __int2float_rn((int)(xb - base)));
+    return pk_fma(f, Lh, pk_mul(f, Ll));
+}
+
+// The constants of the packed kernel, each duplicated into both halves of a float2
+struct PkConst {
+    float2 Lh[3], Ll[3];     // box / 2^32 per axis, float-float
+    float2 c2, m1, m2, p3, mh, p15, skl;
+    float c2s, sk;
+};
+
+__device__ __forceinline__ PkConst pk_const(const GroupGeom& G) {
+    PkConst K;
+    for (int k = 0; k < 3; k++) { K.Lh[k] = make_float2(G.Ls[k], G.Ls[k]); K.Ll[k] = make_float2(G.Ll[k], G.Ll[k]); }
+    K.c2 = make_float2(G.c2, G.c2);
+    K.m1 = make_float2(-1.0f, -1.0f);
+    K.m2 = make_float2(-2.0f, -2.0f);
+    K.p3 = make_float2(3.0f, 3.0f);
+    K.mh = make_float2(-0.5f, -0.5f);
+    K.p15 = make_float2(1.5f, 1.5f);
+    K.skl = make_float2(G.skl, G.skl);
+    K.c2s = G.c2;
+    K.sk = G.sk;
+    return K;
+}
+
+// The pair terms of one row atom with one partner atom in entries A and B (inA / inB: the pair is
+// in the rows), added to the row atom's per-entry sums.
+__device__ __forceinline__ void pk_slot(float2 dx, float2 dy, float2 dz, bool inA, bool inB, float2 si, float2 qh,
+                                        float2 ql, float2 ep, float2 sg, const PkConst& K, float2& tc, float2& tl,
+                                        float2& tv) {
+    float2 r2 = pk_fma(dx, dx, pk_fma(dy, dy, pk_mul(dz, dz)));
+    r2.x = inA ? r2.x : K.c2s;
+    r2.y = inB ? r2.y : K.c2s;
+    const float2 d = pk_fma(r2, K.m1, K.c2);                                   // rc^2 - r^2
+    const float2 dl = pk_mul(d, K.skl);
+    const float2 t = make_float2(__saturatef(fmaf(d.x, K.sk, dl.x)), __saturatef(fmaf(d.y, K.sk, dl.y)));
+    const float2 sw = pk_mul(pk_mul(t, t), pk_fma(t, K.m2, K.p3));
+    float2 ri = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    ri = pk_mul(ri, pk_fma(pk_mul(pk_mul(r2, K.mh), ri), ri, K.p15));         // one Newton step
+    const float2 gg = pk_mul(ri, sw);
+    tc = pk_fma(qh, gg, tc);
+    tl = pk_fma(ql, gg, tl);
+    const float2 y = pk_mul(pk_add(si, sg), ri);
+    const float2 x2 = pk_mul(y, y);
+    const float2 x6 = pk_mul(pk_mul(x2, x2), x2);
+    tv = pk_fma(ep, pk_mul(pk_mul(x6, pk_add(x6, K.m1)), sw), tv);
+}
+
+template <int G, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __restrict__ fx, const float4* __restrict__ cls,
+                                                               int ncls, const int* __restrict__ gstart, int ngroup,
+                                                               const int2* __restrict__ grow, const int* __restrict__ glen,
+                                                               int gcap, GroupGeom Gm, double* part) {
+    extern __shared__ float4 s_cls[];
+    float* s_qh = (float*)(s_cls + ncls);      // the class table again, one array per parameter
+    float* s_ql = s_qh + ncls;
+    float* s_ep = s_ql + ncls;
+    float* s_sg = s_ep + ncls;
+    for (int c = threadIdx.x; c < ncls; c += blockDim.x) {
+        const float4 v = cls[c];
+        s_cls[c] = v;
+        s_qh[c] = v.x; s_ql[c] = v.y; s_ep[c] = v.z; s_sg[c] = v.w;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const PkConst K = pk_const(Gm);
+    float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;
+    for (int g = warp; g < ngroup; g += nwarps) {
+        const int a0 = gstart[g], ni = gstart[g + 1] - a0;   // 1..G, the same in every lane
+        const uint4 f0 = fx[a0];
+        float2 nox[G], noy[G], noz[G], si[G];   // minus each row atom's offset from the first; its half sigma
+        float off = 0.0f;
+#pragma unroll
+        for (int a = 0; a < G; a++) {
+            const uint4 fa = fx[a0 + (a < ni ? a : 0)];
+            const float ox = fixed_delta(f0.x, fa.x, Gm.Ls[0], Gm.Ll[0]);
+            const float oy = fixed_delta(f0.y, fa.y, Gm.Ls[1], Gm.Ll[1]);
+            const float oz = fixed_delta(f0.z, fa.z, Gm.Ls[2], Gm.Ll[2]);
+            nox[a] = pk_dup(-ox);
+            noy[a] = pk_dup(-oy);
+            noz[a] = pk_dup(-oz);
+            off = fmaxf(off, fmaxf(fabsf(ox), fmaxf(fabsf(oy), fabsf(oz))));
+            si[a] = pk_dup(s_sg[fa.w]);
+        }
+        float ch[G], cl[G], vs[G];
+#pragma unroll
+        for (int a = 0; a < G; a++) { ch[a] = 0.f; cl[a] = 0.f; vs[a] = 0.f; }
+        const int m = glen[g];
+        const int2* row = grow + (size_t)g * gcap;
+        // FAST: relative placement, all G row atoms (no per-slot branch); else per-pair displacement
+        auto sweep_row = [&](auto fast_tag) {
+            constexpr bool FAST = decltype(fast_tag)::value;
+            uint4 fi[G];
+            if (!FAST) {
+#pragma unroll
+                for (int a = 0; a < G; a++) fi[a] = fx[a0 + (a < ni ? a : 0)];
+            }
+            for (int k = 2 * lane; k < m; k += 64) {
+                // entries k and k + 1 (past the row's end: the row group itself, all mask bits clear)
+                const int2 eA = row[k];
+                const int2 eB = k + 1 < m ? row[k + 1] : make_int2(a0, 0);
+                uint4 fA[G], fB[G];
+#pragma unroll
+                for (int b = 0; b < G; b++) {
+                    fA[b] = fx[eA.x + (b <= (eA.y >> 16) ? b : 0)];
+                    fB[b] = fx[eB.x + (b <= (eB.y >> 16) ? b : 0)];
+                }
+                float2 tc[G], tl[G], tv[G];
+#pragma unroll
+                for (int a = 0; a < G; a++) { tc[a] = pk_dup(0.f); tl[a] = pk_dup(0.f); tv[a] = pk_dup(0.f); }
+#pragma unroll
+                for (int b = 0; b < G; b++) {
+                    const int cA = fA[b].w, cB = fB[b].w;
+                    const float2 qh = make_float2(s_qh[cA], s_qh[cB]), ql = make_float2(s_ql[cA], s_ql[cB]);
+                    const float2 ep = make_float2(s_ep[cA], s_ep[cB]), sg = make_float2(s_sg[cA], s_sg[cB]);
+                    float2 jx, jy, jz;
+                    if (FAST) {
+                        jx = pk_delta(f0.x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
+                        jy = pk_delta(f0.y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
+                        jz = pk_delta(f0.z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < G; a++) {
+                        if (!FAST && a >= ni) break;
+                        float2 dx, dy, dz;
+                        if (FAST) {
+                            if (a == 0) { dx = jx; dy = jy; dz = jz; }
+                            else { dx = pk_add(jx, nox[a]); dy = pk_add(jy, noy[a]); dz = pk_add(jz, noz[a]); }
+                        } else {
+                            dx = pk_delta(fi[a].x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
+                            dy = pk_delta(fi[a].y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
+                            dz = pk_delta(fi[a].z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
+                        }
+                        const int bit = 1 << (a * 4 + b);
+                        pk_slot(dx, dy, dz, (eA.y & bit) != 0, (eB.y & bit) != 0, si[a], qh, ql, ep, sg, K, tc[a], tl[a],
+                                tv[a]);
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < G; a++) {
+                    if (!FAST && a >= ni) break;
+                    float sm, er;
+                    two_sum(ch[a], tc[a].x + tc[a].y, sm, er);
+                    ch[a] = sm;
+                    cl[a] += (tl[a].x + tl[a].y) + er;
+                    vs[a] += tv[a].x + tv[a].y;
+                }
+            }
+        };
+        if (ni == G && off <= Gm.emax) sweep_row(std::true_type{});   // the same in every lane
+        else sweep_row(std::false_type{});
+#pragma unroll
+        for (int a = 0; a < G; a++)
+            if (a < ni) mix_row_flush(s_cls[fx[a0 + a].w], ch[a], cl[a], vs[a], EH, EL, VH, VL);
+    }
+    block_reduce2((double)EH + (double)EL, (double)VH + (double)VL, part + 2 * blockIdx.x);
+}
+
 template <typename T>
 static int galloc(T** p, size_t count) {
     cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(1, count) * sizeof(T));
@@ -316,11 +501,18 @@ int GroupPairs::launch_energy(cudaStream_t st, int v, const uint4* fx, const flo
     blocks = 152 * B_;                                                                                            \
     k_energy_groups<GS_, ISO_, B_, PF_><<<blocks, GE_THREADS, smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, \
                                                                           gcap, G, part);
+#define MCG_GROUP_X2(GS_, NT_, B_)                                                                                \
+    blocks = 152 * B_;                                                                                            \
+    k_energy_groups_x2<GS_, NT_, B_><<<blocks, NT_, 2 * smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, gcap, \
+                                                                G, part);
 #define MCG_GROUP_G(GS_)                                                                                          \
     if (v == 0) { if (G.iso) { MCG_GROUP_ONE(GS_, true, 2, true) } else { MCG_GROUP_ONE(GS_, false, 2, true) } }   \
-    else { if (G.iso) { MCG_GROUP_ONE(GS_, true, 3, false) } else { MCG_GROUP_ONE(GS_, false, 3, false) } }
+    else if (v == 1) { if (G.iso) { MCG_GROUP_ONE(GS_, true, 3, false) } else { MCG_GROUP_ONE(GS_, false, 3, false) } } \
+    else if (v == 2) { MCG_GROUP_X2(GS_, 256, 2) }                                                                 \
+    else { MCG_GROUP_X2(GS_, 128, 5) }
     if (gmax <= 3) { MCG_GROUP_G(3) } else { MCG_GROUP_G(4) }
 #undef MCG_GROUP_G
+#undef MCG_GROUP_X2
 #undef MCG_GROUP_ONE
     return blocks;
 }

@@ -24,6 +24,12 @@ struct GroupGeom {
     float L2h, L2l;       // (box / 2^32)^2 as float-float (cubic boxes: r^2 in fixed-point units)
     float c2, n2, k3;     // rc^2, ron^2, rc^2 - 3 ron^2 (FP32)
     double inv_f1;        // 1 / (the FP32 switch polynomial at r^2 <= ron^2): makes inner pairs exactly 1
+    float sk, skl;        // 1 / (rc^2 - ron^2) as float-float: the switch's argument t = (rc^2 - r^2) sk
+                          // (sk rounded alone would scale t in every switched pair alike, a systematic
+                          // error that the switching shell's large, cancelling terms amplify)
+    float emax;           // half the smallest box edge less rc (and 1e-3 A): a row group whose atoms lie
+                          // within emax of its first atom (each component) sees every partner within rc
+                          // at its minimum image relative to that first atom
     int iso;              // cubic box: r^2 summed in fixed-point units
 };
 
@@ -42,7 +48,7 @@ public:
     // (cls, ncls > 0).
     int launch_energy(cudaStream_t st, int v, const uint4* fx, const float4* cls, int ncls, const GroupGeom& G,
                       double* part);
-    static constexpr int kVariants = 2;
+    static constexpr int kVariants = 4;
 
     bool ok = false;
     int n = 0, ngroup = 0, gcap = 0;

@@ -10,7 +10,10 @@ of one group pair's mask.  Checked:
     total), on cubic, orthorhombic and argon (one-atom groups) boxes;
   - the group rows follow new pruned rows after displacements, commits and list updates;
   - repeated energies are bitwise equal (fixed-order sums);
-  - a system without the parameter-class table has no group variants (MCG_ENOTSUP).
+  - a system without the parameter-class table has no group variants (MCG_ENOTSUP);
+  - the packed variants (8, 9: partner atoms placed relative to the row group's first atom) agree
+    on a box where half the box less rc lies between the water's smallest and largest hydrogen
+    offsets, so some rows take the relative placement and the others the per-pair displacement.
 """
 import copy
 
@@ -18,13 +21,14 @@ import numpy as np
 import pytest
 
 import goldens
-from mc_cpp_gb300 import build, native
+from mc_cpp_gb300 import build, native, systems
 from mc_cpp_gb300.engine import FFieldCUDA
 
 pytestmark = pytest.mark.gpu
 MIX_REL = 1e-6
 ORDER_REL = 2e-7
-GROUP_VARIANTS = (6, 7)
+GROUP_VARIANTS = (6, 7, 8, 9)
+PACKED_VARIANTS = (8, 9)
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -113,3 +117,23 @@ def test_no_group_variants_without_the_class_table():
     want = FFieldCUDA(s, "fp64", moves=False).getE10()
     e = ff.getE10()                                    # the tuner skips the group variants
     assert abs(e[0] - want[0]) <= MIX_REL * abs(want[0])
+
+
+def test_packed_variants_with_rows_on_both_placements():
+    # L = 25.7 A: half the box less rc is 0.85 A, and the molecules' largest hydrogen offset
+    # component from the oxygen lies between 0.6 and 0.96 A: 43% of the rows take the relative
+    # placement, the others the per-pair displacement
+    s = systems.water_box(550, seed=21, L=25.7)
+    ref = FFieldCUDA(s, "mixed", moves=False)
+    ref.set_pair_kernel(0)
+    base = ref.getE10()
+    want = FFieldCUDA(s, "fp64", moves=False).getE10()
+    for prune in (True, False):
+        ff = FFieldCUDA(s, "mixed", moves=False)
+        if not prune:
+            ff.set_prune_buffer(0.0)
+        for v in PACKED_VARIANTS:
+            ff.set_pair_kernel(v)
+            e = ff.getE10()
+            _agree(e, base, want, ("water550", prune, v))
+            assert np.array_equal(e, ff.getE10())
