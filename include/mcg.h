@@ -143,11 +143,16 @@ int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
 /* Device time (ms, CUDA events on the handle's stream) of reps launches of the switched
  * nonbonded pair kernel alone over the current list (switch mode). */
 int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);
+/* The same with the L2 cache flushed before each launch (a 256 MiB device buffer written on the
+ * handle's stream between launches, outside the timed intervals): *ms is the sum of the reps
+ * launches' own device times.  An addition without a reference counterpart. */
+int mcg_time_nonbonded_flushed(mcg_system* s, int reps, float* ms);
 /* Kernel of the mixed-precision periodic switch energy (an addition without a reference
  * counterpart: FField_MDBAS has one scalar loop).  variant -1 (the default) times every variant
  * at the first energy and keeps the fastest; 0..3 are per-atom list kernels; 4 and 5 are
- * cluster-pair kernels over the cluster form of the same Verlet list; 6 and 7 are group-pair
- * kernels over the group form of the rows the list kernels read (MCG_ENOTSUP when a form could
+ * cluster-pair kernels over the cluster form of the same Verlet list; 6 to 9 are group-pair
+ * kernels over the group form of the rows the list kernels read (8 and 9: packed FP32, two
+ * entries per lane) (MCG_ENOTSUP when a form could
  * not be built).  mcg_get_pair_kernel reports the variant in use (-1 before the first energy) and
  * the number of variants. */
 int mcg_set_pair_kernel(mcg_system* s, int variant);

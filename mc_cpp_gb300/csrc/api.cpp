@@ -223,6 +223,11 @@ int mcg_time_nonbonded(mcg_system* s, int reps, float* ms) {
     return s->eng.time_nonbonded(reps, ms);
 }
 
+int mcg_time_nonbonded_flushed(mcg_system* s, int reps, float* ms) {
+    if (!s || !ms || reps < 1) return fail(MCG_EINVAL, "bad arguments");
+    return s->eng.time_nonbonded_flushed(reps, ms);
+}
+
 int mcg_set_pair_kernel(mcg_system* s, int variant) {
     if (!s) return fail(MCG_EINVAL, "null argument");
     return s->eng.set_pair_kernel(variant);

@@ -315,57 +315,133 @@ __device__ __forceinline__ void pk_slot(float2 dx, float2 dy, float2 dz, bool in
     tv = pk_fma(ep, pk_mul(pk_mul(x6, pk_add(x6, K.m1)), sw), tv);
 }
 
+// The row state of the packed kernels: the row atoms' offsets from the first (negated, duplicated
+// into both halves), their half sigmas, raw positions (per-pair placement) and the per-atom sums.
+template <int G>
+struct PkRow {
+    uint4 f0;
+    uint4 fi[G];
+    float2 nox[G], noy[G], noz[G], si[G];
+    float ch[G], cl[G], vs[G];
+    int a0, ni;
+    bool fast;
+};
+
+template <int G>
+__device__ __forceinline__ void pk_row_begin(PkRow<G>& R, const uint4* __restrict__ fx, const float* s_sg, int a0, int ni,
+                                             const GroupGeom& Gm) {
+    R.a0 = a0;
+    R.ni = ni;
+    R.f0 = fx[a0];
+    float off = 0.0f;
+#pragma unroll
+    for (int a = 0; a < G; a++) {
+        const uint4 fa = fx[a0 + (a < ni ? a : 0)];
+        R.fi[a] = fa;
+        const float ox = fixed_delta(R.f0.x, fa.x, Gm.Ls[0], Gm.Ll[0]);
+        const float oy = fixed_delta(R.f0.y, fa.y, Gm.Ls[1], Gm.Ll[1]);
+        const float oz = fixed_delta(R.f0.z, fa.z, Gm.Ls[2], Gm.Ll[2]);
+        R.nox[a] = pk_dup(-ox);
+        R.noy[a] = pk_dup(-oy);
+        R.noz[a] = pk_dup(-oz);
+        off = fmaxf(off, fmaxf(fabsf(ox), fmaxf(fabsf(oy), fabsf(oz))));
+        R.si[a] = pk_dup(s_sg[fa.w]);
+        R.ch[a] = 0.f;
+        R.cl[a] = 0.f;
+        R.vs[a] = 0.f;
+    }
+    R.fast = ni == G && off <= Gm.emax;   // the same in every lane
+}
+
+template <int G>
+__device__ __forceinline__ void pk_row_end(const PkRow<G>& R, const uint4* __restrict__ fx, const float4* s_cls, float& EH,
+                                           float& EL, float& VH, float& VL) {
+#pragma unroll
+    for (int a = 0; a < G; a++)
+        if (a < R.ni) mix_row_flush(s_cls[fx[R.a0 + a].w], R.ch[a], R.cl[a], R.vs[a], EH, EL, VH, VL);
+}
+
+// One item: entries A and B (their G partner atoms fA, fB and masks mA, mB) against the row's atoms.
+// FAST: relative placement, all G row atoms, no per-slot branch; else per-pair displacement.
+template <int G, bool FAST>
+__device__ __forceinline__ void pk_item(PkRow<G>& R, const uint4 (&fA)[G], const uint4 (&fB)[G], int mA, int mB,
+                                        const float* s_qh, const float* s_ql, const float* s_ep, const float* s_sg,
+                                        const PkConst& K) {
+    float2 tc[G], tl[G], tv[G];
+#pragma unroll
+    for (int a = 0; a < G; a++) { tc[a] = pk_dup(0.f); tl[a] = pk_dup(0.f); tv[a] = pk_dup(0.f); }
+#pragma unroll
+    for (int b = 0; b < G; b++) {
+        const int cA = fA[b].w, cB = fB[b].w;
+        const float2 qh = make_float2(s_qh[cA], s_qh[cB]), ql = make_float2(s_ql[cA], s_ql[cB]);
+        const float2 ep = make_float2(s_ep[cA], s_ep[cB]), sg = make_float2(s_sg[cA], s_sg[cB]);
+        float2 jx, jy, jz;
+        if (FAST) {
+            jx = pk_delta(R.f0.x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
+            jy = pk_delta(R.f0.y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
+            jz = pk_delta(R.f0.z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
+        }
+#pragma unroll
+        for (int a = 0; a < G; a++) {
+            if (!FAST && a >= R.ni) break;
+            float2 dx, dy, dz;
+            if (FAST) {
+                if (a == 0) { dx = jx; dy = jy; dz = jz; }
+                else { dx = pk_add(jx, R.nox[a]); dy = pk_add(jy, R.noy[a]); dz = pk_add(jz, R.noz[a]); }
+            } else {
+                dx = pk_delta(R.fi[a].x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
+                dy = pk_delta(R.fi[a].y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
+                dz = pk_delta(R.fi[a].z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
+            }
+            const int bit = 1 << (a * 4 + b);
+            pk_slot(dx, dy, dz, (mA & bit) != 0, (mB & bit) != 0, R.si[a], qh, ql, ep, sg, K, tc[a], tl[a], tv[a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < G; a++) {
+        if (!FAST && a >= R.ni) break;
+        float sm, er;
+        two_sum(R.ch[a], tc[a].x + tc[a].y, sm, er);
+        R.ch[a] = sm;
+        R.cl[a] += (tl[a].x + tl[a].y) + er;
+        R.vs[a] += tv[a].x + tv[a].y;
+    }
+}
+
+// the class table and its per-parameter copies in shared memory (the packed kernels' layout)
+__device__ __forceinline__ void pk_load_classes(const float4* __restrict__ cls, int ncls, float4* s_cls) {
+    float* s_qh = (float*)(s_cls + ncls);
+    for (int c = threadIdx.x; c < ncls; c += blockDim.x) {
+        const float4 v = cls[c];
+        s_cls[c] = v;
+        s_qh[c] = v.x; s_qh[ncls + c] = v.y; s_qh[2 * ncls + c] = v.z; s_qh[3 * ncls + c] = v.w;
+    }
+}
+
+// Packed kernel, gathers in registers: a warp per row, entries k and k + 1 per lane.
 template <int G, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __restrict__ fx, const float4* __restrict__ cls,
                                                                int ncls, const int* __restrict__ gstart, int ngroup,
                                                                const int2* __restrict__ grow, const int* __restrict__ glen,
                                                                int gcap, GroupGeom Gm, double* part) {
     extern __shared__ float4 s_cls[];
-    float* s_qh = (float*)(s_cls + ncls);      // the class table again, one array per parameter
-    float* s_ql = s_qh + ncls;
-    float* s_ep = s_ql + ncls;
-    float* s_sg = s_ep + ncls;
-    for (int c = threadIdx.x; c < ncls; c += blockDim.x) {
-        const float4 v = cls[c];
-        s_cls[c] = v;
-        s_qh[c] = v.x; s_ql[c] = v.y; s_ep[c] = v.z; s_sg[c] = v.w;
-    }
+    pk_load_classes(cls, ncls, s_cls);
+    const float* s_qh = (const float*)(s_cls + ncls);
+    const float *s_ql = s_qh + ncls, *s_ep = s_ql + ncls, *s_sg = s_ep + ncls;
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const PkConst K = pk_const(Gm);
     float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;
+    PkRow<G> R;
     for (int g = warp; g < ngroup; g += nwarps) {
-        const int a0 = gstart[g], ni = gstart[g + 1] - a0;   // 1..G, the same in every lane
-        const uint4 f0 = fx[a0];
-        float2 nox[G], noy[G], noz[G], si[G];   // minus each row atom's offset from the first; its half sigma
-        float off = 0.0f;
-#pragma unroll
-        for (int a = 0; a < G; a++) {
-            const uint4 fa = fx[a0 + (a < ni ? a : 0)];
-            const float ox = fixed_delta(f0.x, fa.x, Gm.Ls[0], Gm.Ll[0]);
-            const float oy = fixed_delta(f0.y, fa.y, Gm.Ls[1], Gm.Ll[1]);
-            const float oz = fixed_delta(f0.z, fa.z, Gm.Ls[2], Gm.Ll[2]);
-            nox[a] = pk_dup(-ox);
-            noy[a] = pk_dup(-oy);
-            noz[a] = pk_dup(-oz);
-            off = fmaxf(off, fmaxf(fabsf(ox), fmaxf(fabsf(oy), fabsf(oz))));
-            si[a] = pk_dup(s_sg[fa.w]);
-        }
-        float ch[G], cl[G], vs[G];
-#pragma unroll
-        for (int a = 0; a < G; a++) { ch[a] = 0.f; cl[a] = 0.f; vs[a] = 0.f; }
+        const int a0 = gstart[g];
+        pk_row_begin(R, fx, s_sg, a0, gstart[g + 1] - a0, Gm);
         const int m = glen[g];
         const int2* row = grow + (size_t)g * gcap;
-        // FAST: relative placement, all G row atoms (no per-slot branch); else per-pair displacement
-        auto sweep_row = [&](auto fast_tag) {
+        auto sweep = [&](auto fast_tag) {
             constexpr bool FAST = decltype(fast_tag)::value;
-            uint4 fi[G];
-            if (!FAST) {
-#pragma unroll
-                for (int a = 0; a < G; a++) fi[a] = fx[a0 + (a < ni ? a : 0)];
-            }
             for (int k = 2 * lane; k < m; k += 64) {
                 // entries k and k + 1 (past the row's end: the row group itself, all mask bits clear)
                 const int2 eA = row[k];
@@ -376,54 +452,106 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __re
                     fA[b] = fx[eA.x + (b <= (eA.y >> 16) ? b : 0)];
                     fB[b] = fx[eB.x + (b <= (eB.y >> 16) ? b : 0)];
                 }
-                float2 tc[G], tl[G], tv[G];
-#pragma unroll
-                for (int a = 0; a < G; a++) { tc[a] = pk_dup(0.f); tl[a] = pk_dup(0.f); tv[a] = pk_dup(0.f); }
-#pragma unroll
-                for (int b = 0; b < G; b++) {
-                    const int cA = fA[b].w, cB = fB[b].w;
-                    const float2 qh = make_float2(s_qh[cA], s_qh[cB]), ql = make_float2(s_ql[cA], s_ql[cB]);
-                    const float2 ep = make_float2(s_ep[cA], s_ep[cB]), sg = make_float2(s_sg[cA], s_sg[cB]);
-                    float2 jx, jy, jz;
-                    if (FAST) {
-                        jx = pk_delta(f0.x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
-                        jy = pk_delta(f0.y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
-                        jz = pk_delta(f0.z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
-                    }
-#pragma unroll
-                    for (int a = 0; a < G; a++) {
-                        if (!FAST && a >= ni) break;
-                        float2 dx, dy, dz;
-                        if (FAST) {
-                            if (a == 0) { dx = jx; dy = jy; dz = jz; }
-                            else { dx = pk_add(jx, nox[a]); dy = pk_add(jy, noy[a]); dz = pk_add(jz, noz[a]); }
-                        } else {
-                            dx = pk_delta(fi[a].x, fA[b].x, fB[b].x, K.Lh[0], K.Ll[0]);
-                            dy = pk_delta(fi[a].y, fA[b].y, fB[b].y, K.Lh[1], K.Ll[1]);
-                            dz = pk_delta(fi[a].z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
-                        }
-                        const int bit = 1 << (a * 4 + b);
-                        pk_slot(dx, dy, dz, (eA.y & bit) != 0, (eB.y & bit) != 0, si[a], qh, ql, ep, sg, K, tc[a], tl[a],
-                                tv[a]);
-                    }
-                }
-#pragma unroll
-                for (int a = 0; a < G; a++) {
-                    if (!FAST && a >= ni) break;
-                    float sm, er;
-                    two_sum(ch[a], tc[a].x + tc[a].y, sm, er);
-                    ch[a] = sm;
-                    cl[a] += (tl[a].x + tl[a].y) + er;
-                    vs[a] += tv[a].x + tv[a].y;
-                }
+                pk_item<G, FAST>(R, fA, fB, eA.y, eB.y, s_qh, s_ql, s_ep, s_sg, K);
             }
         };
-        if (ni == G && off <= Gm.emax) sweep_row(std::true_type{});   // the same in every lane
-        else sweep_row(std::false_type{});
-#pragma unroll
-        for (int a = 0; a < G; a++)
-            if (a < ni) mix_row_flush(s_cls[fx[a0 + a].w], ch[a], cl[a], vs[a], EH, EL, VH, VL);
+        if (R.fast) sweep(std::true_type{});
+        else sweep(std::false_type{});
+        pk_row_end(R, fx, s_cls, EH, EL, VH, VL);
     }
+    block_reduce2((double)EH + (double)EL, (double)VH + (double)VL, part + 2 * blockIdx.x);
+}
+
+// Packed kernel, gathers prefetched in registers: a warp's items (row after row, entries k and
+// k + 1 of a row per lane, the same sequence in every lane) with the next item's 2G partner atoms
+// loaded into a second register set while the current item is evaluated, and each item's entries
+// loaded two items ahead (unchecked: checked against the row's length when its atoms are loaded,
+// by which time that length has arrived).  The loop body is written twice, so the two register
+// sets swap roles without copies.  A row's sums are flushed when the next item belongs to another
+// row.  It pays when the rows stream from DRAM; with the rows resident in L2 the plain packed
+// kernel is faster (fewer instructions).
+template <int G, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2r(const uint4* __restrict__ fx, const float4* __restrict__ cls,
+                                                                int ncls, const int* __restrict__ gstart, int ngroup,
+                                                                const int2* __restrict__ grow, const int* __restrict__ glen,
+                                                                int gcap, GroupGeom Gm, double* part) {
+    extern __shared__ float4 s_cls[];
+    pk_load_classes(cls, ncls, s_cls);
+    const float* s_qh = (const float*)(s_cls + ncls);
+    const float *s_ql = s_qh + ncls, *s_ep = s_ql + ncls, *s_sg = s_ep + ncls;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const PkConst K = pk_const(Gm);
+    struct Cur { int g, a0, m, k; };
+    auto advance = [&](Cur& c) {
+        if (c.k - 2 * lane + 64 < c.m) {
+            c.k += 64;
+        } else {
+            c.g += nwarps;
+            c.k = 2 * lane;
+            if (c.g < ngroup) { c.a0 = gstart[c.g]; c.m = glen[c.g]; }
+        }
+    };
+    auto raw = [&](const Cur& c, int2& A, int2& B) {
+        A = make_int2(0, 0);
+        B = make_int2(0, 0);
+        if (c.g < ngroup) {
+            const int2* r = grow + (size_t)c.g * gcap;
+            A = r[min(c.k, gcap - 1)];
+            B = r[min(c.k + 1, gcap - 1)];
+        }
+    };
+    auto gather = [&](const Cur& c, int2& A, int2& B, uint4 (&fA)[G], uint4 (&fB)[G]) {
+        if (c.g < ngroup) {
+            if (!(c.k < c.m)) A = make_int2(c.a0, 0);   // past the row's end: the row group, no mask bits
+            if (!(c.k + 1 < c.m)) B = make_int2(c.a0, 0);
+#pragma unroll
+            for (int b = 0; b < G; b++) {
+                fA[b] = fx[A.x + (b <= (A.y >> 16) ? b : 0)];
+                fB[b] = fx[B.x + (b <= (B.y >> 16) ? b : 0)];
+            }
+        }
+    };
+    float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;
+    PkRow<G> R;
+    int rg = -1;
+    Cur c0{warp, 0, 0, 2 * lane};
+    if (c0.g < ngroup) { c0.a0 = gstart[c0.g]; c0.m = glen[c0.g]; }
+    int2 A0, B0, A1, B1;
+    uint4 fA0[G], fB0[G], fA1[G], fB1[G];
+    raw(c0, A0, B0);
+    gather(c0, A0, B0, fA0, fB0);
+    Cur c1 = c0;
+    advance(c1);
+    raw(c1, A1, B1);
+    // one item: c (its atoms fA, fB already loaded); cn, An, Bn: the next item, whose atoms go to gA, gB
+    auto step = [&](Cur& c, int2& A, int2& B, uint4 (&fA)[G], uint4 (&fB)[G], Cur& cn, int2& An, int2& Bn,
+                    uint4 (&gA)[G], uint4 (&gB)[G]) {
+        Cur c2 = cn;
+        advance(c2);
+        int2 A2, B2;
+        raw(c2, A2, B2);
+        gather(cn, An, Bn, gA, gB);
+        if (c.g != rg) {
+            if (rg >= 0) pk_row_end(R, fx, s_cls, EH, EL, VH, VL);
+            pk_row_begin(R, fx, s_sg, c.a0, gstart[c.g + 1] - c.a0, Gm);
+            rg = c.g;
+        }
+        if (R.fast) pk_item<G, true>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K);
+        else pk_item<G, false>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K);
+        c = c2;          // the item after next takes this item's cursor and entries
+        A = A2;
+        B = B2;
+    };
+    while (true) {
+        if (c0.g >= ngroup) break;
+        step(c0, A0, B0, fA0, fB0, c1, A1, B1, fA1, fB1);   // c0 <- item after c1
+        if (c1.g >= ngroup) break;
+        step(c1, A1, B1, fA1, fB1, c0, A0, B0, fA0, fB0);   // c1 <- item after c0
+    }
+    if (rg >= 0) pk_row_end(R, fx, s_cls, EH, EL, VH, VL);
     block_reduce2((double)EH + (double)EL, (double)VH + (double)VL, part + 2 * blockIdx.x);
 }
 
@@ -505,13 +633,18 @@ int GroupPairs::launch_energy(cudaStream_t st, int v, const uint4* fx, const flo
     blocks = 152 * B_;                                                                                            \
     k_energy_groups_x2<GS_, NT_, B_><<<blocks, NT_, 2 * smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, gcap, \
                                                                 G, part);
+#define MCG_GROUP_X2R(GS_, NT_, B_)                                                                               \
+    blocks = 152 * B_;                                                                                            \
+    k_energy_groups_x2r<GS_, NT_, B_><<<blocks, NT_, 2 * smem, st>>>(fx, cls, ncls, d_gstart, ngroup, d_grow, d_glen, \
+                                                                     gcap, G, part);
 #define MCG_GROUP_G(GS_)                                                                                          \
     if (v == 0) { if (G.iso) { MCG_GROUP_ONE(GS_, true, 2, true) } else { MCG_GROUP_ONE(GS_, false, 2, true) } }   \
     else if (v == 1) { if (G.iso) { MCG_GROUP_ONE(GS_, true, 3, false) } else { MCG_GROUP_ONE(GS_, false, 3, false) } } \
     else if (v == 2) { MCG_GROUP_X2(GS_, 256, 2) }                                                                 \
-    else { MCG_GROUP_X2(GS_, 128, 5) }
+    else { MCG_GROUP_X2R(GS_, 128, 3) }
     if (gmax <= 3) { MCG_GROUP_G(3) } else { MCG_GROUP_G(4) }
 #undef MCG_GROUP_G
+#undef MCG_GROUP_X2R
 #undef MCG_GROUP_X2
 #undef MCG_GROUP_ONE
     return blocks;

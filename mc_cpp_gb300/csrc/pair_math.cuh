@@ -197,27 +197,30 @@ __device__ __forceinline__ float mixed_pair_delta(float dox, float doy, float do
 __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, float doz, float mx, float my, float mz,
                                                           float qk_sw, float e4_sw, float ss, float c2, float n2, float k3,
                                                           int& npair) {
-    const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
-    const float uo = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
-    const float un = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
-    npair += fminf(uo, un) <= c2 ? 1 : 0;
-    const float ro = rsqrtf(uo), rn = rsqrtf(un);
-    const float ua = fminf(fmaxf(uo, n2), c2), ub = fminf(fmaxf(un, n2), c2);
-    const float Aa = c2 - ua, Ab = c2 - ub;
-    const float Ba = fmaf(2.0f, ua, k3), Bb = fmaf(2.0f, ub, k3);
-    const float po = Aa * Aa * Ba, pn = Ab * Ab * Bb;
+    // The old and new ends of the pair are the two halves of float2 values, so the work both ends
+    // share takes one sm_100+ packed instruction; every operation rounds as the scalar form would
+    // (-x^3 is formed from -x, so x^6 - x^3 is the same single FMA).
+    const float2 dx = make_float2(dox, dox - mx), dy = make_float2(doy, doy - my), dz = make_float2(doz, doz - mz);
+    const float2 u = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    npair += fminf(u.x, u.y) <= c2 ? 1 : 0;
+    const float2 r = make_float2(rsqrtf(u.x), rsqrtf(u.y));
+    const float2 uc = make_float2(fminf(fmaxf(u.x, n2), c2), fminf(fmaxf(u.y, n2), c2));
+    const float2 A = __ffma2_rn(uc, make_float2(-1.0f, -1.0f), make_float2(c2, c2));
+    const float2 B = __ffma2_rn(make_float2(2.0f, 2.0f), uc, make_float2(k3, k3));
+    const float2 P = __fmul2_rn(__fmul2_rn(A, A), B);
     // Lennard-Jones, differenced directly (small at these distances)
-    const float xo = ss * (ro * ro), xn = ss * (rn * rn);
-    const float xo3 = xo * xo * xo, xn3 = xn * xn * xn;
-    const float d_lj = e4_sw * fmaf(fmaf(xn3, xn3, -xn3), pn, -(fmaf(xo3, xo3, -xo3) * po));
+    const float2 nx = __fmul2_rn(make_float2(-ss, -ss), __fmul2_rn(r, r));
+    const float2 nx3 = __fmul2_rn(__fmul2_rn(nx, nx), nx);
+    const float2 w = __ffma2_rn(nx3, nx3, nx3);                   // x^6 - x^3 at both ends
+    const float d_lj = e4_sw * fmaf(w.y, P.y, -(w.x * P.x));
     // Coulomb: qk (P_n / r_n - P_o / r_o) = qk ((1/r_n - 1/r_o) P_n + (P_n - P_o) / r_o)
-    const float du = -fmaf(mx, dox + dnx, fmaf(my, doy + dny, mz * (doz + dnz)));
-    const float p = ro * rn;
-    const float dinv = __fdividef(-du * p * p, ro + rn);
+    const float du = -fmaf(mx, dox + dx.y, fmaf(my, doy + dy.y, mz * (doz + dz.y)));
+    const float p = r.x * r.y;
+    const float dinv = __fdividef(-du * p * p, r.x + r.y);
     // both ends inside [ron^2, rc^2] exactly when the clamp left them unchanged
-    const float dd = (ua == uo && ub == un) ? du : (ub - ua);
-    const float dp = dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
-    return fmaf(qk_sw, fmaf(dinv, pn, ro * dp), d_lj);
+    const float dd = (uc.x == u.x && uc.y == u.y) ? du : (uc.y - uc.x);
+    const float dp = dd * fmaf(2.0f * A.x, A.x, -(A.x + A.y) * B.y);
+    return fmaf(qk_sw, fmaf(dinv, P.y, r.x * dp), d_lj);
 }
 
 // Block sums of two doubles (every thread passes its values; thread 0 of warp 0 writes out[0..1]).

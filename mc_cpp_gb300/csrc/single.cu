@@ -1495,6 +1495,39 @@ int SingleEngine::time_nonbonded(int reps, float* ms) {
     return MCG_OK;
 }
 
+int SingleEngine::time_nonbonded_flushed(int reps, float* ms) {
+    if (hs.cut != MCG_CUT_SWITCH) return fail(MCG_ENOTSUP, "the pair-kernel timing covers the switch mode");
+    {
+        int rc = prepare_pair_kernel();
+        if (rc) return rc;
+    }
+    constexpr size_t kFlush = (size_t)256 << 20;   // twice the L2
+    unsigned char* junk = nullptr;
+    CK(cudaMalloc(&junk, kFlush));
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) { cudaFree(junk); return fail(MCG_ECUDA, "cudaEventCreate"); }
+    if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); cudaFree(junk); return fail(MCG_ECUDA, "cudaEventCreate"); }
+    float total = 0.0f;
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < reps && e == cudaSuccess; r++) {
+        e = cudaMemsetAsync(junk, r & 0xff, kFlush, stream);
+        if (e == cudaSuccess) e = cudaEventRecord(a, stream);
+        if (e == cudaSuccess) launch_nonbonded(d_part);
+        if (e == cudaSuccess) e = cudaEventRecord(b, stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+        total += t;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(junk);
+    if (e != cudaSuccess) return fail(MCG_ECUDA, std::string("flushed pair-kernel timing: ") + cudaGetErrorString(e));
+    launches += reps;
+    *ms = total;
+    return MCG_OK;
+}
+
 AtomsDev SingleEngine::atoms() const {
     AtomsDev A;
     A.pq = d_pq; A.es = d_es; A.es14 = d_es14; A.fx = d_fx; A.esf = d_esf; A.esf14 = d_esf14; A.qf = d_qf;

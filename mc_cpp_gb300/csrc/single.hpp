@@ -36,6 +36,7 @@ public:
     bool pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const;
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
     int time_nonbonded(int reps, float* ms);
+    int time_nonbonded_flushed(int reps, float* ms);
     // Pair-kernel variant of the mixed periodic switch energy: -1 = chosen by timing at the first
     // use; 0..3 per-atom list kernels; 4.. cluster-pair kernels (when the cluster list exists).
     int set_pair_kernel(int v);

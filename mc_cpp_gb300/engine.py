@@ -108,9 +108,15 @@ class FFieldCUDA:
         native.check(native.lib().mcg_time_nonbonded(self.h, reps, C.byref(ms)))
         return ms.value
 
+    def time_nonbonded_flushed(self, reps: int) -> float:
+        """Device ms of reps launches of the switched pair kernel, the L2 cache flushed before each."""
+        ms = C.c_float(0)
+        native.check(native.lib().mcg_time_nonbonded_flushed(self.h, reps, C.byref(ms)))
+        return ms.value
+
     def set_pair_kernel(self, variant: int) -> None:
         """Pins the mixed periodic switch-energy kernel (-1: fastest by timing at the first use;
-        0..3 per-atom list kernels; 4.. cluster-pair kernels)."""
+        0..3 per-atom list kernels; 4, 5 cluster-pair kernels; 6..9 group-pair kernels)."""
         native.check(native.lib().mcg_set_pair_kernel(self.h, variant))
 
     def pair_kernel(self):

@@ -138,6 +138,7 @@ def lib():
         "mcg_batch_get_lists": (C.c_int, [P, C.c_int, _i, _i, C.c_int64, _i64]),
         "mcg_pair_count": (C.c_int, [P, _i64, _i64]),
         "mcg_time_nonbonded": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
+        "mcg_time_nonbonded_flushed": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
         "mcg_set_pair_kernel": (C.c_int, [P, C.c_int]),
         "mcg_get_pair_kernel": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "mcg_cluster_stats": (C.c_int, [P, _i64, _i64, _i64]),
