@@ -273,7 +273,7 @@ __device__ __forceinline__ float2 pk_delta(uint32_t base, uint32_t xa, uint32_t 
 // The constants of the packed kernel, each duplicated into both halves of a float2
 struct PkConst {
     float2 Lh[3], Ll[3];     // box / 2^32 per axis, float-float
-    float2 c2, m1, m2, p3, mh, p15, skl;
+    float2 c2, m1, m2, p3, m3, skl;
     float c2s, sk;
 };
 
@@ -284,8 +284,7 @@ __device__ __forceinline__ PkConst pk_const(const GroupGeom& G) {
     K.m1 = make_float2(-1.0f, -1.0f);
     K.m2 = make_float2(-2.0f, -2.0f);
     K.p3 = make_float2(3.0f, 3.0f);
-    K.mh = make_float2(-0.5f, -0.5f);
-    K.p15 = make_float2(1.5f, 1.5f);
+    K.m3 = make_float2(-3.0f, -3.0f);
     K.skl = make_float2(G.skl, G.skl);
     K.c2s = G.c2;
     K.sk = G.sk;
@@ -305,7 +304,9 @@ __device__ __forceinline__ void pk_slot(float2 dx, float2 dy, float2 dz, bool in
     const float2 t = make_float2(__saturatef(fmaf(d.x, K.sk, dl.x)), __saturatef(fmaf(d.y, K.sk, dl.y)));
     const float2 sw = pk_mul(pk_mul(t, t), pk_fma(t, K.m2, K.p3));
     float2 ri = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-    ri = pk_mul(ri, pk_fma(pk_mul(pk_mul(r2, K.mh), ri), ri, K.p15));         // one Newton step
+    // one Newton step, scaled by -2 (exact): ri = -2 / r.  The Coulomb sums carry the factor (the
+    // row's flush takes it out), the half sigmas carry -1/2 (the per-parameter table holds them so)
+    ri = pk_mul(ri, pk_fma(pk_mul(r2, ri), ri, K.m3));
     const float2 gg = pk_mul(ri, sw);
     tc = pk_fma(qh, gg, tc);
     tl = pk_fma(ql, gg, tl);
@@ -358,18 +359,42 @@ __device__ __forceinline__ void pk_row_end(const PkRow<G>& R, const uint4* __res
                                            float& EL, float& VH, float& VL) {
 #pragma unroll
     for (int a = 0; a < G; a++)
-        if (a < R.ni) mix_row_flush(s_cls[fx[R.a0 + a].w], R.ch[a], R.cl[a], R.vs[a], EH, EL, VH, VL);
+        if (a < R.ni) mix_row_flush(s_cls[fx[R.a0 + a].w], -0.5f * R.ch[a], -0.5f * R.cl[a], R.vs[a], EH, EL, VH, VL);
 }
 
-// One item: entries A and B (their G partner atoms fA, fB and masks mA, mB) against the row's atoms.
-// FAST: relative placement, all G row atoms, no per-slot branch; else per-pair displacement.
+// FP32 sums of a row atom's pair terms over one item (both halves), before they go into the row's
+// float-float Coulomb and FP32 LJ sums (summing two items before that moved the Coulomb total of a
+// 550-water box 2.7e-7 from the per-atom list kernel's, past their 2e-7 agreement)
+template <int G>
+struct PkAcc {
+    float2 tc[G], tl[G], tv[G];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int a = 0; a < G; a++) { tc[a] = pk_dup(0.f); tl[a] = pk_dup(0.f); tv[a] = pk_dup(0.f); }
+    }
+};
+
+// the item sums into the row sums (the atoms past the row's size hold zeros)
+template <int G>
+__device__ __forceinline__ void pk_flush(PkRow<G>& R, PkAcc<G>& T) {
+#pragma unroll
+    for (int a = 0; a < G; a++) {
+        float sm, er;
+        two_sum(R.ch[a], T.tc[a].x + T.tc[a].y, sm, er);
+        R.ch[a] = sm;
+        R.cl[a] += (T.tl[a].x + T.tl[a].y) + er;
+        R.vs[a] += T.tv[a].x + T.tv[a].y;
+    }
+    T.zero();
+}
+
+// One item: entries A and B (their G partner atoms fA, fB and masks mA, mB) against the row's atoms,
+// added to T.  FAST: relative placement, all G row atoms, no per-slot branch; else per-pair
+// displacement.
 template <int G, bool FAST>
 __device__ __forceinline__ void pk_item(PkRow<G>& R, const uint4 (&fA)[G], const uint4 (&fB)[G], int mA, int mB,
                                         const float* s_qh, const float* s_ql, const float* s_ep, const float* s_sg,
-                                        const PkConst& K) {
-    float2 tc[G], tl[G], tv[G];
-#pragma unroll
-    for (int a = 0; a < G; a++) { tc[a] = pk_dup(0.f); tl[a] = pk_dup(0.f); tv[a] = pk_dup(0.f); }
+                                        const PkConst& K, PkAcc<G>& T) {
 #pragma unroll
     for (int b = 0; b < G; b++) {
         const int cA = fA[b].w, cB = fB[b].w;
@@ -394,27 +419,19 @@ __device__ __forceinline__ void pk_item(PkRow<G>& R, const uint4 (&fA)[G], const
                 dz = pk_delta(R.fi[a].z, fA[b].z, fB[b].z, K.Lh[2], K.Ll[2]);
             }
             const int bit = 1 << (a * 4 + b);
-            pk_slot(dx, dy, dz, (mA & bit) != 0, (mB & bit) != 0, R.si[a], qh, ql, ep, sg, K, tc[a], tl[a], tv[a]);
+            pk_slot(dx, dy, dz, (mA & bit) != 0, (mB & bit) != 0, R.si[a], qh, ql, ep, sg, K, T.tc[a], T.tl[a], T.tv[a]);
         }
-    }
-#pragma unroll
-    for (int a = 0; a < G; a++) {
-        if (!FAST && a >= R.ni) break;
-        float sm, er;
-        two_sum(R.ch[a], tc[a].x + tc[a].y, sm, er);
-        R.ch[a] = sm;
-        R.cl[a] += (tl[a].x + tl[a].y) + er;
-        R.vs[a] += tv[a].x + tv[a].y;
     }
 }
 
-// the class table and its per-parameter copies in shared memory (the packed kernels' layout)
+// the class table and its per-parameter copies in shared memory (the packed kernels' layout; the
+// half sigmas times -1/2, the scale of pk_slot's inverse distance)
 __device__ __forceinline__ void pk_load_classes(const float4* __restrict__ cls, int ncls, float4* s_cls) {
     float* s_qh = (float*)(s_cls + ncls);
     for (int c = threadIdx.x; c < ncls; c += blockDim.x) {
         const float4 v = cls[c];
         s_cls[c] = v;
-        s_qh[c] = v.x; s_qh[ncls + c] = v.y; s_qh[2 * ncls + c] = v.z; s_qh[3 * ncls + c] = v.w;
+        s_qh[c] = v.x; s_qh[ncls + c] = v.y; s_qh[2 * ncls + c] = v.z; s_qh[3 * ncls + c] = -0.5f * v.w;
     }
 }
 
@@ -442,6 +459,8 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __re
         const int2* row = grow + (size_t)g * gcap;
         auto sweep = [&](auto fast_tag) {
             constexpr bool FAST = decltype(fast_tag)::value;
+            PkAcc<G> T;
+            T.zero();
             for (int k = 2 * lane; k < m; k += 64) {
                 // entries k and k + 1 (past the row's end: the row group itself, all mask bits clear)
                 const int2 eA = row[k];
@@ -452,7 +471,8 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __re
                     fA[b] = fx[eA.x + (b <= (eA.y >> 16) ? b : 0)];
                     fB[b] = fx[eB.x + (b <= (eB.y >> 16) ? b : 0)];
                 }
-                pk_item<G, FAST>(R, fA, fB, eA.y, eB.y, s_qh, s_ql, s_ep, s_sg, K);
+                pk_item<G, FAST>(R, fA, fB, eA.y, eB.y, s_qh, s_ql, s_ep, s_sg, K, T);
+                pk_flush(R, T);
             }
         };
         if (R.fast) sweep(std::true_type{});
@@ -516,6 +536,8 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2r(const uint4* __r
     };
     float EH = 0.0f, EL = 0.0f, VH = 0.0f, VL = 0.0f;
     PkRow<G> R;
+    PkAcc<G> T;
+    T.zero();
     int rg = -1;
     Cur c0{warp, 0, 0, 2 * lane};
     if (c0.g < ngroup) { c0.a0 = gstart[c0.g]; c0.m = glen[c0.g]; }
@@ -539,8 +561,9 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2r(const uint4* __r
             pk_row_begin(R, fx, s_sg, c.a0, gstart[c.g + 1] - c.a0, Gm);
             rg = c.g;
         }
-        if (R.fast) pk_item<G, true>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K);
-        else pk_item<G, false>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K);
+        if (R.fast) pk_item<G, true>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K, T);
+        else pk_item<G, false>(R, fA, fB, A.y, B.y, s_qh, s_ql, s_ep, s_sg, K, T);
+        pk_flush(R, T);
         c = c2;          // the item after next takes this item's cursor and entries
         A = A2;
         B = B2;
