@@ -435,7 +435,7 @@ __device__ __forceinline__ bool metropolis_accept(float deh, float del, const Mo
 // The displacements come straight from the fixed-point mirrors (exact minimum images); g's new
 // displacement is the old one less g's atom move, the minimum image for every pair within rc since
 // rc + the largest move <= L/2.
-template <int A>
+template <int A, bool PK>
 __device__ __forceinline__ float pair_correction(const MoveRec<A>& Qg, const MoveRec<A>& Qh, int apr, int lane,
                                                  const float4 (*tab)[MAX_APR], float Ls0, float Ls1, float Ls2,
                                                  float Ll0, float Ll1, float Ll2, float c2, float n2, float k3) {
@@ -450,7 +450,7 @@ __device__ __forceinline__ float pair_correction(const MoveRec<A>& Qg, const Mov
         const float mx = fdelta(a.x, an.x, Ls0, Ll0), my = fdelta(a.y, an.y, Ls1, Ll1), mz = fdelta(a.z, an.z, Ls2, Ll2);
         const float4 tb = tab[j][hb.w];
         int np = 0;
-        const float v = mixed_pair_delta_clamped(dx, dy, dz, mx, my, mz, tb.x, tb.y, tb.z, c2, n2, k3, np);
+        const float v = pair_delta<PK>(dx, dy, dz, mx, my, mz, tb.x, tb.y, tb.z, c2, n2, k3, np);
         s += side ? -v : v;
     }
     return s;
@@ -514,6 +514,9 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : (APR == 1
     namespace cg = cooperative_groups;
     constexpr int NW = NT / 32;
     constexpr int A = APR ? APR : MAX_APR;        // register arrays per moved atom
+    // the pair delta on packed FP32, except in the one-atom 128-thread kernel held to 64 registers
+    // (8 CTAs per SM), where the packed form's extra live registers spill
+    constexpr bool PK = !(APR == 1 && NT == 128);
     static_assert(CL == 1 || CL == 2, "clusters of one or two CTAs");
     // moves per iteration, at most (shared-memory records): a warp per move at the least
     constexpr int KM = (A <= 4 ? KMAX : 8) < NT * CL / 32 ? (A <= 4 ? KMAX : 8) : NT * CL / 32;
@@ -751,7 +754,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : (APR == 1
                             ez -= (ez > C.Lhalf[2]) ? C.Lf[2] : ((ez < -C.Lhalf[2]) ? -C.Lf[2] : 0.0f);
                         }
                         // d_old = b - a_old, d_new = b - a_new = d_old - m
-                        acc += mixed_pair_delta_clamped(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, c2f, n2f,
+                        acc += pair_delta<PK>(ex, ey, ez, m[j][0], m[j][1], m[j][2], tb.x, tb.y, tb.z, c2f, n2f,
                                                         k3f, np);
                     }
                 };
@@ -874,7 +877,7 @@ __global__ void __launch_bounds__(NT, NT >= 512 ? 1 : (NT >= 256 ? 2 : (APR == 1
                     for (unsigned nb = __ballot_sync(0xffffffffu, near); nb; nb &= nb - 1) {
                         const int l = __ffs(nb) - 1;
                         const int gg = __shfl_sync(0xffffffffu, g, l), hh = __shfl_sync(0xffffffffu, h, l);
-                        float ch = pair_correction(Q[gg], Q[hh], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f, n2f, k3f);
+                        float ch = pair_correction<A, PK>(Q[gg], Q[hh], apr, lane, s_tab, Ls0, Ls1, Ls2, Ll0, Ll1, Ll2, c2f, n2f, k3f);
                         float cl = 0.0f;
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) {

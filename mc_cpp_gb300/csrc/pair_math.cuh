@@ -223,6 +223,41 @@ __device__ __forceinline__ float mixed_pair_delta_clamped(float dox, float doy, 
     return fmaf(qk_sw, fmaf(dinv, P.y, r.x * dp), d_lj);
 }
 
+// The same arithmetic without packed instructions: fewer live registers, for a kernel held to 64.
+__device__ __forceinline__ float mixed_pair_delta_clamped_scalar(float dox, float doy, float doz, float mx, float my, float mz,
+                                                          float qk_sw, float e4_sw, float ss, float c2, float n2, float k3,
+                                                          int& npair) {
+    const float dnx = dox - mx, dny = doy - my, dnz = doz - mz;
+    const float uo = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
+    const float un = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
+    npair += fminf(uo, un) <= c2 ? 1 : 0;
+    const float ro = rsqrtf(uo), rn = rsqrtf(un);
+    const float ua = fminf(fmaxf(uo, n2), c2), ub = fminf(fmaxf(un, n2), c2);
+    const float Aa = c2 - ua, Ab = c2 - ub;
+    const float Ba = fmaf(2.0f, ua, k3), Bb = fmaf(2.0f, ub, k3);
+    const float po = Aa * Aa * Ba, pn = Ab * Ab * Bb;
+    // Lennard-Jones, differenced directly (small at these distances)
+    const float xo = ss * (ro * ro), xn = ss * (rn * rn);
+    const float xo3 = xo * xo * xo, xn3 = xn * xn * xn;
+    const float d_lj = e4_sw * fmaf(fmaf(xn3, xn3, -xn3), pn, -(fmaf(xo3, xo3, -xo3) * po));
+    // Coulomb: qk (P_n / r_n - P_o / r_o) = qk ((1/r_n - 1/r_o) P_n + (P_n - P_o) / r_o)
+    const float du = -fmaf(mx, dox + dnx, fmaf(my, doy + dny, mz * (doz + dnz)));
+    const float p = ro * rn;
+    const float dinv = __fdividef(-du * p * p, ro + rn);
+    // both ends inside [ron^2, rc^2] exactly when the clamp left them unchanged
+    const float dd = (ua == uo && ub == un) ? du : (ub - ua);
+    const float dp = dd * fmaf(2.0f * Aa, Aa, -(Aa + Ab) * Bb);
+    return fmaf(qk_sw, fmaf(dinv, pn, ro * dp), d_lj);
+}
+
+// the packed or the scalar form (the same values)
+template <bool PACKED>
+__device__ __forceinline__ float pair_delta(float dox, float doy, float doz, float mx, float my, float mz, float qk_sw,
+                                            float e4_sw, float ss, float c2, float n2, float k3, int& npair) {
+    if (PACKED) return mixed_pair_delta_clamped(dox, doy, doz, mx, my, mz, qk_sw, e4_sw, ss, c2, n2, k3, npair);
+    return mixed_pair_delta_clamped_scalar(dox, doy, doz, mx, my, mz, qk_sw, e4_sw, ss, c2, n2, k3, npair);
+}
+
 // Block sums of two doubles (every thread passes its values; thread 0 of warp 0 writes out[0..1]).
 __device__ __forceinline__ void block_reduce2(double a, double b, double* out) {
     __shared__ double sa[32], sb[32];
