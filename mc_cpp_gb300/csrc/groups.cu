@@ -245,10 +245,11 @@ __global__ void __launch_bounds__(GE_THREADS, MINB) k_energy_groups(const uint4*
 
 // The same energy with two entries per lane in packed FP32: entries k and k + 1 of a row take the
 // two halves of float2 values, so one sm_100+ packed instruction (add, multiply or FMA on a
-// register pair) does the work of both.  The switch is evaluated as S = t^2 (3 - 2 t) on
-// t = clamp((rc^2 - r^2) / (rc^2 - ron^2), 0, 1), which is 1 below ron, the reference's polynomial
-// between ron and rc, and 0 beyond rc and for masked pairs (their r^2 is set to rc^2), so no
-// comparison or clamp of r^2 is needed; S is normalised, so the partial sums need no inv_f1.  The
+// register pair) does the work of both.  The switch is evaluated as P = u^2 (3 D - 2 u) on
+// u = clamp(rc^2 - r^2, 0, D), D = rc^2 - ron^2: the reference's polynomial (c2 - r^2)^2
+// (c2 + 2 r^2 - 3 n2) rewritten in u, D^3 below ron and 0 beyond rc and for masked pairs (their
+// r^2 is set to rc^2).  rc^2 - r^2 is exact in the switching region, the clamps run on the ALU
+// pipe, and the block sums take 1 / (that polynomial at u = D) in FP64 at the end (inv_p1).  The
 // partner atoms' parameters are read from per-parameter tables in shared memory straight into the
 // halves of each float2.  Per entry pair and row atom the terms are summed in FP32, then into the
 // row atom's float-float Coulomb sum and FP32 LJ sum as in k_energy_groups.
@@ -273,8 +274,8 @@ __device__ __forceinline__ float2 pk_delta(uint32_t base, uint32_t xa, uint32_t 
 // The constants of the packed kernel, each duplicated into both halves of a float2
 struct PkConst {
     float2 Lh[3], Ll[3];     // box / 2^32 per axis, float-float
-    float2 c2, m1, m2, p3, m3, skl;
-    float c2s, sk;
+    float2 c2, m1, m2, d3, m3;
+    float c2s, D;
 };
 
 __device__ __forceinline__ PkConst pk_const(const GroupGeom& G) {
@@ -283,11 +284,10 @@ __device__ __forceinline__ PkConst pk_const(const GroupGeom& G) {
     K.c2 = make_float2(G.c2, G.c2);
     K.m1 = make_float2(-1.0f, -1.0f);
     K.m2 = make_float2(-2.0f, -2.0f);
-    K.p3 = make_float2(3.0f, 3.0f);
+    K.d3 = make_float2(3.0f * G.D, 3.0f * G.D);
     K.m3 = make_float2(-3.0f, -3.0f);
-    K.skl = make_float2(G.skl, G.skl);
     K.c2s = G.c2;
-    K.sk = G.sk;
+    K.D = G.D;
     return K;
 }
 
@@ -300,9 +300,8 @@ __device__ __forceinline__ void pk_slot(float2 dx, float2 dy, float2 dz, bool in
     r2.x = inA ? r2.x : K.c2s;
     r2.y = inB ? r2.y : K.c2s;
     const float2 d = pk_fma(r2, K.m1, K.c2);                                   // rc^2 - r^2
-    const float2 dl = pk_mul(d, K.skl);
-    const float2 t = make_float2(__saturatef(fmaf(d.x, K.sk, dl.x)), __saturatef(fmaf(d.y, K.sk, dl.y)));
-    const float2 sw = pk_mul(pk_mul(t, t), pk_fma(t, K.m2, K.p3));
+    const float2 u = make_float2(fminf(fmaxf(d.x, 0.0f), K.D), fminf(fmaxf(d.y, 0.0f), K.D));
+    const float2 sw = pk_mul(pk_mul(u, u), pk_fma(u, K.m2, K.d3));             // D^3 S
     float2 ri = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
     // one Newton step, scaled by -2 (exact): ri = -2 / r.  The Coulomb sums carry the factor (the
     // row's flush takes it out), the half sigmas carry -1/2 (the per-parameter table holds them so)
@@ -313,7 +312,7 @@ __device__ __forceinline__ void pk_slot(float2 dx, float2 dy, float2 dz, bool in
     const float2 y = pk_mul(pk_add(si, sg), ri);
     const float2 x2 = pk_mul(y, y);
     const float2 x6 = pk_mul(pk_mul(x2, x2), x2);
-    tv = pk_fma(ep, pk_mul(pk_mul(x6, pk_add(x6, K.m1)), sw), tv);
+    tv = pk_fma(ep, pk_mul(pk_fma(x6, x6, make_float2(-x6.x, -x6.y)), sw), tv);   // the negation folds into the FMA
 }
 
 // The row state of the packed kernels: the row atoms' offsets from the first (negated, duplicated
@@ -479,7 +478,7 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2(const uint4* __re
         else sweep(std::false_type{});
         pk_row_end(R, fx, s_cls, EH, EL, VH, VL);
     }
-    block_reduce2((double)EH + (double)EL, (double)VH + (double)VL, part + 2 * blockIdx.x);
+    block_reduce2(((double)EH + (double)EL) * Gm.inv_p1, ((double)VH + (double)VL) * Gm.inv_p1, part + 2 * blockIdx.x);
 }
 
 // Packed kernel, gathers prefetched in registers: a warp's items (row after row, entries k and
@@ -575,7 +574,7 @@ __global__ void __launch_bounds__(NT, MINB) k_energy_groups_x2r(const uint4* __r
         step(c1, A1, B1, fA1, fB1, c0, A0, B0, fA0, fB0);   // c1 <- item after c0
     }
     if (rg >= 0) pk_row_end(R, fx, s_cls, EH, EL, VH, VL);
-    block_reduce2((double)EH + (double)EL, (double)VH + (double)VL, part + 2 * blockIdx.x);
+    block_reduce2(((double)EH + (double)EL) * Gm.inv_p1, ((double)VH + (double)VL) * Gm.inv_p1, part + 2 * blockIdx.x);
 }
 
 template <typename T>

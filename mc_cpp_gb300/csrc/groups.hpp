@@ -24,9 +24,8 @@ struct GroupGeom {
     float L2h, L2l;       // (box / 2^32)^2 as float-float (cubic boxes: r^2 in fixed-point units)
     float c2, n2, k3;     // rc^2, ron^2, rc^2 - 3 ron^2 (FP32)
     double inv_f1;        // 1 / (the FP32 switch polynomial at r^2 <= ron^2): makes inner pairs exactly 1
-    float sk, skl;        // 1 / (rc^2 - ron^2) as float-float: the switch's argument t = (rc^2 - r^2) sk
-                          // (sk rounded alone would scale t in every switched pair alike, a systematic
-                          // error that the switching shell's large, cancelling terms amplify)
+    float D;              // rc^2 - ron^2 (FP32)
+    double inv_p1;        // 1 / (the packed kernels' polynomial u^2 (3D - 2u) at u = D, in FP32 as they form it)
     float emax;           // half the smallest box edge less rc (and 1e-3 A): a row group whose atoms lie
                           // within emax of its first atom (each component) sees every partner within rc
                           // at its minimum image relative to that first atom

@@ -1297,9 +1297,8 @@ GroupGeom SingleEngine::group_geom() const {
     G.n2 = C.n2;
     G.k3 = C.k3;
     G.inv_f1 = C.inv_f1;
-    const double skd = 1.0 / ((double)C.c2 - (double)C.n2);
-    G.sk = (float)skd;
-    G.skl = (float)(skd - (double)G.sk);
+    G.D = C.c2 - C.n2;
+    G.inv_p1 = 1.0 / (double)((G.D * G.D) * std::fmaf(G.D, -2.0f, 3.0f * G.D));
     const double lmin = std::min(pbc.L[0], std::min(pbc.L[1], pbc.L[2]));
     G.emax = (float)(0.5 * lmin - std::sqrt((double)C.c2) - 1e-3);
     return G;
