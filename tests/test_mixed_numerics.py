@@ -221,3 +221,31 @@ def test_mixed_delta_e_within_tolerance_and_analytic_coulomb_difference():
         worst_d = max(worst_d, abs(dd - want) / KCALTOIU)
     assert worst_a <= 1e-4, worst_a
     assert worst_d >= 3.0 * worst_a, (worst_d, worst_a)
+
+
+def test_packed_switch_polynomial_in_u_equals_the_reference_switch():
+    """The packed group-pair kernels (k_energy_groups_x2*, mc_cpp_gb300/csrc/groups.cu) evaluate the
+    switch as P = u^2 (3D - 2u) on u = clamp(rc^2 - r^2, 0, D), D = rc^2 - ron^2, in float32, and
+    divide the block sums by P(D) in FP64.  The reference's switch is
+    (rc^2 - r^2)^2 (rc^2 + 2 r^2 - 3 ron^2) / (rc^2 - ron^2)^3 between ron and rc, 1 below, 0
+    beyond (FField_MDBAS.cpp:348-402).  Checked on r from 0.5 to 13 A for the 10-12 and 8-9 A switches: within 4 float32
+    roundings of the FP64 value, exactly 1 below ron (P(D) is formed as the kernel forms it) and
+    exactly 0 beyond rc."""
+    for ron, rc in ((10.0, 12.0), (8.0, 9.0)):
+        c2, n2 = f32(rc * rc), f32(ron * ron)
+        D = f32(c2 - n2)
+        d3 = f32(f32(3.0) * D)
+        r = np.linspace(0.5, 13.0, 20001)
+        r2 = (r * r).astype(f32)
+        u = np.minimum(np.maximum((c2 - r2).astype(f32), f32(0.0)), D)
+        P = ((u * u).astype(f32) * _fma(u, np.full_like(u, -2.0), d3)).astype(f32)
+        pD = float(f32(D * D) * _fma(np.array([D]), np.array([f32(-2.0)]), d3)[0])
+        S = P.astype(np.float64) / pD
+        r2d = r2.astype(np.float64)
+        c2d, n2d = float(c2), float(n2)
+        ref = np.where(r2d <= n2d, 1.0, np.where(r2d >= c2d, 0.0,
+                       (c2d - r2d) ** 2 * (c2d + 2.0 * r2d - 3.0 * n2d) / (c2d - n2d) ** 3))
+        assert np.all(S[r2d <= n2d] == 1.0)
+        assert np.all(S[r2d >= c2d] == 0.0)
+        mid = (r2d > n2d) & (r2d < c2d)
+        assert np.all(np.abs(S[mid] - ref[mid]) <= 4 * 2.0 ** -24 * np.maximum(ref[mid], 2.0 ** -20))
