@@ -12,8 +12,13 @@ float32 value, within 2 ulp of the kernel's rsqrt + Newton step) over the oracle
 
 It checks the design, not the device: the total energy within 1e-6 relative of the oracle's FP64
 value (the tolerance the GPU tests apply to the kernel), each component within 1e-6 of the larger
-of the two.
+of the two.  The packed group-pair kernels' arithmetic (partners placed relative to the row
+group's first atom, the switch as a polynomial in rc^2 - r^2, the inverse distance scaled by -2)
+is restated the same way (packed_energy): 2.6e-8 to 8.8e-8 of the larger component on argon,
+water 512 and water 4,096, as the list kernel's restatement.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -249,3 +254,91 @@ def test_packed_switch_polynomial_in_u_equals_the_reference_switch():
         assert np.all(S[r2d >= c2d] == 0.0)
         mid = (r2d > n2d) & (r2d < c2d)
         assert np.all(np.abs(S[mid] - ref[mid]) <= 4 * 2.0 ** -24 * np.maximum(ref[mid], 2.0 ** -20))
+
+
+def _fixed_delta(fa, fb, lh, ll):
+    """fixed_delta (pair_math.cuh): the int32 wrap of b - a converted to float32 and scaled by the
+    float-float unit length."""
+    f = (fb - fa).astype(np.uint32).view(np.int32).astype(f32)
+    return _fma(f, np.full_like(f, lh), (f * ll).astype(f32))
+
+
+def packed_energy(s, rows):
+    """(elec, vdw) in internal units by the pair arithmetic of the packed group-pair kernels
+    (k_energy_groups_x2*, mc_cpp_gb300/csrc/groups.cu), in float32; pair terms summed in float64
+    (the kernels' float-float row sums are the other test's subject).  Groups are runs of up to 4
+    atoms of one residue; a row group of G atoms whose offsets from its first atom stay within
+    emax places its partners relative to that atom and adds each row atom's own offset, the other
+    rows take the per-pair displacement.  The switch is u^2 (3D - 2u), u = clamp(rc^2 - r^2, 0, D);
+    the inverse distance carries a factor -2 (exact) that the Coulomb sums drop at the row's end
+    and the half sigmas carry as -1/2."""
+    L = [float(b) for b in s.box]
+    n = s.natom
+    resid = np.asarray(s.resid)
+    gstart = []
+    for a in range(n):
+        if a == 0 or resid[a] != resid[a - 1] or a - gstart[-1] == 4:
+            gstart.append(a)
+    gof = np.repeat(np.arange(len(gstart)), np.diff(gstart + [n]))
+    first = np.asarray(gstart)[gof]
+    gsize = np.diff(gstart + [n])
+    G = 3 if gsize.max() <= 3 else 4
+    i = np.repeat(np.arange(n), [len(r) for r in rows])
+    j = np.concatenate(rows).astype(np.int64)
+    fx, lh, ll = [], [], []
+    for a in range(3):
+        fx.append(_to_fixed(np.asarray((s.x, s.y, s.z)[a], np.float64), L[a]))
+        ls = L[a] / 4294967296.0
+        lh.append(f32(ls))
+        ll.append(f32(ls - float(f32(ls))))
+    c2, n2 = f32(s.cutoff * s.cutoff), f32(s.cuton * s.cuton)
+    D = f32(c2 - n2)
+    emax = f32(0.5 * min(L) - math.sqrt(float(c2)) - 1e-3)
+    # each atom's offset from its group's first atom, and the row groups that take the relative form
+    off = [_fixed_delta(fx[a][first], fx[a], lh[a], ll[a]) for a in range(3)]
+    big = np.maximum.reduce([np.abs(o) for o in off])
+    gbig = np.zeros(len(gstart), f32)
+    np.maximum.at(gbig, gof, big)
+    rel = (gsize[gof[i]] == G) & (gbig[gof[i]] <= emax)
+    d = []
+    for a in range(3):
+        dj = _fixed_delta(fx[a][first[i]], fx[a][j], lh[a], ll[a])
+        d_rel = (dj + (-off[a][i])).astype(f32)
+        d_pair = _fixed_delta(fx[a][i], fx[a][j], lh[a], ll[a])
+        d.append(np.where(rel, d_rel, d_pair))
+    r2 = _fma(d[0], d[0], _fma(d[1], d[1], (d[2] * d[2]).astype(f32)))
+    u = np.minimum(np.maximum((c2 - r2).astype(f32), f32(0.0)), D)
+    P = ((u * u).astype(f32) * _fma(u, np.full_like(u, -2.0), np.full_like(u, f32(3.0) * D))).astype(f32)
+    ri = (f32(-2.0) * (1.0 / np.sqrt(r2.astype(np.float64))).astype(f32)).astype(f32)
+    gg = (ri * P).astype(f32)
+    q = np.asarray(s.q, np.float64)
+    qh = q.astype(f32)
+    ql = (q - qh.astype(np.float64)).astype(f32)
+    eps = np.sqrt(np.asarray(s.eps, np.float64) * KCALTOIU).astype(f32)
+    hs = (f32(-0.5) * np.asarray(s.sig, np.float64).astype(f32)).astype(f32)
+    y = ((hs[i] + hs[j]) * ri).astype(f32)
+    x2 = (y * y).astype(f32)
+    x6 = (x2 * x2 * x2).astype(f32)
+    lj = (eps[j] * ((_fma(x6, x6, -x6) * P).astype(f32))).astype(f32)
+    cq = (qh[j] * gg).astype(np.float64) + (ql[j] * gg).astype(np.float64)
+    pD = float(f32(D * D) * _fma(np.array([D]), np.array([f32(-2.0)]), np.array([f32(3.0) * D]))[0])
+    elec = -0.5 * float(np.sum(q[i] * cq)) / pD
+    vdw = float(np.sum(eps[i].astype(np.float64) * lj.astype(np.float64))) / pD
+    return CHGCHARMM * KCALTOIU * elec, 4.0 * vdw, float(np.mean(rel))
+
+
+@pytest.mark.parametrize("name", ["argon864", "water512", "water4096"])
+def test_packed_group_arithmetic_within_tolerance_of_fp64(name):
+    """The packed kernels' pair arithmetic (relative placement, switch in u, the -2 scaled inverse
+    distance) in float32 against the oracle's FP64 energy: within 1e-6 of the larger component, as
+    the GPU tests hold the kernels.  water4096 takes the relative placement on every row, water512
+    (half the box less rc below the hydrogens' offsets) and argon (one-atom groups) the per-pair
+    displacement."""
+    s = goldens.system(name, "switch")
+    o = orc.Oracle(s, moves=False)
+    want = o.energy()
+    elec, vdw, frac_rel = packed_energy(s, o.verlet_rows())
+    assert frac_rel == {"argon864": 0.0, "water512": 0.0, "water4096": 1.0}[name], frac_rel
+    scale = max(1.0, abs(want[3]), abs(want[4]))
+    assert abs(elec - want[3]) <= TOL * scale, (elec, want[3])
+    assert abs(vdw - want[4]) <= TOL * scale, (vdw, want[4])
