@@ -338,11 +338,12 @@ static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int accepta
     int64_t acc = 0, ties = 0;
     // Without per-step output, translation moves of atom sets that carry no bonded term in a
     // periodic switched FP64 system run on the device, a launch per list-update period, on the same
-    // random words (SingleEngine::metropolis_device); every other run takes the host loop below.
+    // random words (SingleEngine::metropolis_device), when its limits hold (at most 8 move types, 64
+    // atoms a move, checked before the first step); every other run takes the host loop below.
     bool all_trn = true;
     for (const MoveKind& mk : s->moves) all_trn = all_trn && mk.type == MCG_MOVE_TRN;
     if (!trace && !follow && save_each == 0 && all_trn && h.cut == MCG_CUT_SWITCH && h.pbc != MCG_PBC_NONE &&
-        h.prec == MCG_PREC_FP64 && !E.has_bonded_terms() && nmvtyp <= 8) {
+        h.prec == MCG_PREC_FP64 && !E.has_bonded_terms() && SingleEngine::replay_fits(s->moves)) {
         rc = E.metropolis_device(gen, s->moves, beta, nsteps, &etot, &acc);
         if (rc) return rc;
         if (final_etot) *final_etot = etot;

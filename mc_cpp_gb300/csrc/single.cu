@@ -1780,8 +1780,19 @@ int SingleEngine::delta_e(int m, const int* atoms_in, const double* nx, const do
 // (two words, w0 + w1 2^32 rounded once, times 2^-64; a result of 1 becomes the largest double
 // below 1) and into uniform_real_distribution values as (b - a) u + a, every operation rounded on
 // its own as the reference's uncontracted host code rounds it.
-constexpr int RP_MAXT = 8;       // move types
-constexpr int RP_MAXM = 64;      // atoms of one move
+constexpr int RP_MAXT = SingleEngine::kReplayMaxTypes;   // move types
+constexpr int RP_MAXM = SingleEngine::kReplayMaxAtoms;   // atoms of one move
+
+bool SingleEngine::replay_fits(const std::vector<MoveKind>& moves) {
+    if (moves.empty() || (int)moves.size() > RP_MAXT) return false;
+    for (const MoveKind& mk : moves)
+        for (int k = 0; k < mk.ninst(); k++) {
+            int m = 0;
+            for (int r = mk.rstart[k]; r < mk.rstart[k + 1]; r++) m += mk.ranges[2 * r + 1] - mk.ranges[2 * r] + 1;
+            if (m > RP_MAXM) return false;
+        }
+    return true;
+}
 struct ReplayTables {
     int nmvtyp;
     int ninst[RP_MAXT];           // instances of each move type

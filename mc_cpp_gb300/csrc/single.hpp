@@ -32,6 +32,10 @@ public:
     int metropolis_device(std::mt19937& gen, const std::vector<MoveKind>& moves, double beta, int nsteps, double* etot,
                           int64_t* n_accepted);
     bool has_bonded_terms() const { return !term_data.empty(); }
+    // limits of metropolis_device: move types, and atoms in one move instance
+    static constexpr int kReplayMaxTypes = 8, kReplayMaxAtoms = 64;
+    // every instance of every move within kReplayMaxAtoms atoms (and at most kReplayMaxTypes types)
+    static bool replay_fits(const std::vector<MoveKind>& moves);
     // true when the pending proposal moves exactly atoms[0..m) (ascending) to x/y/z[atoms[k]]
     bool pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const;
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);
