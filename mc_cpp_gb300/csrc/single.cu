@@ -30,6 +30,7 @@
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "engine.hpp"
@@ -1826,81 +1827,119 @@ __device__ __forceinline__ double rp_wrap(double v, double L, double rL) {
     return __dsub_rn(v, __dmul_rn(L, r));
 }
 
-// One CTA runs the steps: GB300's FP64 pipe issues a warp's FP64 instruction over many cycles, so
-// a step is bound by the dependent FP64 operations of a pair evaluation, not by the number of SMs
-// (an 8-CTA cluster sharing the partners took 21.5 against 20.1 us per step on the 864-atom argon
-// box).
-__global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uint4* fx, PbcDev pbc, CutDev cut,
-                                                const int* __restrict__ nbr, const int* __restrict__ nup,
-                                                const int* __restrict__ nlo, int cap, const int* __restrict__ c14s,
-                                                const int* __restrict__ c14d, ReplayTables T,
-                                                const uint32_t* __restrict__ words, long long nwords, ReplayState* st,
-                                                int s0, int s1, double beta) {
+// One thread-block cluster of RP_CL CTAs of RP_NT threads runs the steps.  On GB300 a warp's FP64
+// instruction holds its scheduler's narrow FP64 pipe for tens of cycles whatever its active lanes,
+// so a step costs about (warps per scheduler) x (the dependent FP64 operations of one thread):
+//  - the proposal's uniforms (move type, instance and RP_TRIES unit-ball tries at once) are formed
+//    by the lanes of warp 0 in one pass, and the first accepted try is picked by ballot;
+//  - the dE terms are spread one per thread over the cluster's schedulers (CTAs first, then warps,
+//    then lanes), the old and the new energy of a pair on different threads;
+//  - each CTA's partial sums go to every CTA's shared memory, so every CTA sums them in rank order
+//    and takes the same decision; CTA 0 commits, and a cluster barrier orders the commit before
+//    the next step's reads.
+// Measured on the 864-atom argon box: 20 us per step with one 256-thread CTA (its ~200 dE terms at
+// two warps per scheduler), 7-8 us here.
+constexpr int RP_CL = 8;
+constexpr int RP_NT = 128;
+constexpr int RP_TRIES = 8;
+
+__device__ __forceinline__ double rp_canonical_at(const uint32_t* __restrict__ w, long long at) {
+    long long cur = at;
+    return rp_canonical(w, cur);
+}
+
+__global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
+    k_replay(AtomsDev A, double4_32a* pq, uint4* fx, PbcDev pbc, CutDev cut, const int* __restrict__ nbr,
+             const int* __restrict__ nup, const int* __restrict__ nlo, int cap, const int* __restrict__ c14s,
+             const int* __restrict__ c14d, ReplayTables T, const uint32_t* __restrict__ words, long long nwords,
+             ReplayState* st, int s0, int s1, double beta) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
     __shared__ ReplayState S;
     __shared__ int s_idx[RP_MAXM];
     __shared__ double s_xyz[3 * RP_MAXM];
+    __shared__ double s_r[3];
     __shared__ int s_m, s_type, s_stop, s_acc;
     __shared__ long long s_cur;
-    __shared__ double s_part[2][8];
+    __shared__ double s_part[2][RP_NT / 32];
+    __shared__ double2 s_cl[RP_CL];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = RP_NT / 32, G = RP_CL * RP_NT;
+    const int rank = (int)cluster.block_rank();
+    const int gslot = rank + RP_CL * (warp + NW * lane);   // this thread's place in the spread order
     if (tid == 0) S = *st;
-    __syncthreads();
+    cluster.sync();   // every CTA of the cluster is running before any writes into its shared memory
     for (int step = s0 + 1; step <= s1; step++) {
-        if (tid == 0) {
-            // the proposal: move type, instance, displacement in the unit ball times dmax (MC.cpp:142-156)
-            long long cur = S.cursor;
-            s_stop = 0;
-            if (cur + 256 > nwords) {            // 2 words per uniform: 4 for type and instance, 6 per ball draw, 2 to accept
-                s_stop = 1;
-                S.status = 1;
-            } else {
-                const int t = (int)__dmul_rn((double)T.nmvtyp, rp_canonical(words, cur));
-                const int g = T.ibase[t] + (int)__dmul_rn((double)T.ninst[t], rp_canonical(words, cur));
-                int m = 0;
-                for (int r = T.inst_first[g]; r < T.inst_first[g + 1]; r++)
-                    for (int a = T.ranges[2 * r]; a <= T.ranges[2 * r + 1]; a++) {
-                        if (m < RP_MAXM) s_idx[m] = a;
-                        m++;
+        if (warp == 0) {
+            // the proposal (MC.cpp:142-156): type and instance from the words at cur and cur + 2,
+            // unit-ball tries of 3 uniforms each from cur + 4 on (6 words a try), RP_TRIES at a time
+            const long long cur = S.cursor;
+            bool out = cur + 256 > nwords;
+            int t = 0, m = 0, first = -1;
+            if (!out) {
+                double u = 0.0;
+                if (lane < 2) u = rp_canonical_at(words, cur + 2 * lane);
+                const double u0 = __shfl_sync(0xffffffffu, u, 0), u1 = __shfl_sync(0xffffffffu, u, 1);
+                t = (int)__dmul_rn((double)T.nmvtyp, u0);
+                const int g = T.ibase[t] + (int)__dmul_rn((double)T.ninst[t], u1);
+                if (lane == 0) {
+                    for (int r = T.inst_first[g]; r < T.inst_first[g + 1]; r++)
+                        for (int a = T.ranges[2 * r]; a <= T.ranges[2 * r + 1]; a++) {
+                            if (m < RP_MAXM) s_idx[m] = a;
+                            m++;
+                        }
+                }
+                m = __shfl_sync(0xffffffffu, m, 0);
+                for (int pass = 0; first < 0; pass++) {
+                    const long long cb = cur + 4 + 6LL * RP_TRIES * pass;
+                    if (cb + 6LL * RP_TRIES + 2 > nwords) { out = true; break; }   // the pass and the acceptance draw
+                    double v = 0.0;
+                    if (lane < 3 * RP_TRIES) v = __dadd_rn(__dmul_rn(rp_canonical_at(words, cb + 2 * lane), 2.0), -1.0);
+                    const double x = __shfl_sync(0xffffffffu, v, (3 * lane) & 31);
+                    const double y = __shfl_sync(0xffffffffu, v, (3 * lane + 1) & 31);
+                    const double z = __shfl_sync(0xffffffffu, v, (3 * lane + 2) & 31);
+                    const double q = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+                    const unsigned ok = __ballot_sync(0xffffffffu, lane < RP_TRIES && q <= 1.0);
+                    if (ok) {
+                        const int k = __ffs(ok) - 1;
+                        first = pass * RP_TRIES + k;
+                        if (lane == k) {
+                            const double dm = S.dmax[t];
+                            s_r[0] = __dmul_rn(x, dm); s_r[1] = __dmul_rn(y, dm); s_r[2] = __dmul_rn(z, dm);
+                        }
                     }
-                double rx, ry, rz, q;
-                bool out = false;
-                do {
-                    if (cur + 8 > nwords) { out = true; break; }
-                    rx = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
-                    ry = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
-                    rz = __dadd_rn(__dmul_rn(rp_canonical(words, cur), 2.0), -1.0);
-                    q = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
-                } while (q > 1.0);
-                if (out) {
-                    s_stop = 1;
-                    S.status = 1;
-                } else if (m > RP_MAXM) {
-                    s_stop = 1;
-                    S.status = 2;
-                } else {
-                    const double dm = S.dmax[t];
-                    rx = __dmul_rn(rx, dm); ry = __dmul_rn(ry, dm); rz = __dmul_rn(rz, dm);
+                }
+            }
+            if (lane == 0) {
+                s_stop = 0;
+                if (out) { s_stop = 1; S.status = 1; }
+                else if (m > RP_MAXM) { s_stop = 1; S.status = 2; }
+                else {
                     for (int i = 1; i < m; i++) {        // ascending atom order (the partner lookup bisects)
                         const int v = s_idx[i];
                         int k = i - 1;
                         while (k >= 0 && s_idx[k] > v) { s_idx[k + 1] = s_idx[k]; k--; }
                         s_idx[k + 1] = v;
                     }
-                    for (int k = 0; k < m; k++) {
-                        const double4_32a p = pq[s_idx[k]];
-                        s_xyz[3 * k] = rp_wrap(__dadd_rn(p.x, rx), pbc.L[0], pbc.rL[0]);
-                        s_xyz[3 * k + 1] = rp_wrap(__dadd_rn(p.y, ry), pbc.L[1], pbc.rL[1]);
-                        s_xyz[3 * k + 2] = rp_wrap(__dadd_rn(p.z, rz), pbc.L[2], pbc.rL[2]);
-                    }
                     s_m = m;
                     s_type = t;
-                    s_cur = cur;
+                    s_cur = cur + 4 + 6LL * (first + 1);
                 }
             }
+            __syncwarp();
+            if (!out && m <= RP_MAXM)
+                for (int i = lane; i < 3 * m; i += 32) {   // the moved atoms' new positions, wrapped
+                    const int k = i / 3, c = i - 3 * k;
+                    const double4_32a p = pq[s_idx[k]];
+                    const double pc = c == 0 ? p.x : (c == 1 ? p.y : p.z);
+                    s_xyz[i] = rp_wrap(__dadd_rn(pc, s_r[c]), pbc.L[c], pbc.rL[c]);
+                }
         }
         __syncthreads();
-        if (s_stop) break;
-        // dE of the moved set over its Verlet partners and 1-4 pairs, FP64 (as k_delta_e)
+        if (s_stop) break;   // the same in every CTA: each formed the same proposal from the same words
+        // dE of the moved set over its Verlet partners and 1-4 pairs, FP64 (as k_delta_e): term
+        // (k, t, side) of the moved atoms' partner lists, numbered in list order, goes to the thread
+        // whose gslot it equals modulo G; side 0 is the old pair energy (subtracted), 1 the new
         const int m = s_m;
         auto slot = [&](int j) -> int {
             int lo = 0, hi = m - 1;
@@ -1913,26 +1952,31 @@ __global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uin
         };
         double del = 0.0, dvd = 0.0;
         const uint4 f0 = make_uint4(0, 0, 0, 0);
+        int base = 0;
         for (int k = 0; k < m; k++) {
             const int a = s_idx[k];
-            const double4_32a ao = pq[a];
-            const double4_32a an = make_double4_32a(s_xyz[3 * k], s_xyz[3 * k + 1], s_xyz[3 * k + 2], ao.w);
-            auto visit = [&](int j, bool fourteen) {
-                const int sj = slot(j);
-                if (sj >= 0 && j < a) return;   // a pair of moved atoms, counted at its lower atom
-                const double4_32a jo = pq[j];
-                double4_32a jn = jo;
-                if (sj >= 0) { jn.x = s_xyz[3 * sj]; jn.y = s_xyz[3 * sj + 1]; jn.z = s_xyz[3 * sj + 2]; }
-                double e0, v0, e1, v1;
-                pair_energy<PREC_F64>(A, pbc, cut, fourteen, ao, f0, a, jo, f0, j, true, e0, v0);
-                pair_energy<PREC_F64>(A, pbc, cut, fourteen, an, f0, a, jn, f0, j, true, e1, v1);
-                del += e1 - e0;
-                dvd += v1 - v0;
-            };
             const int* row = nbr + (size_t)a * cap;
-            const int u = nup[a], l = nlo[a];
-            for (int t = tid; t < u + l; t += blockDim.x) visit(t < u ? row[t] : row[cap - 1 - (t - u)], false);
-            for (int t = c14s[a] + tid; t < c14s[a + 1]; t += blockDim.x) visit(c14d[t], true);
+            const int u = nup[a], l = nlo[a], n14 = c14s[a + 1] - c14s[a];
+            const int cnt = u + l + n14;
+            int q = (gslot - 2 * base) % G;
+            if (q < 0) q += G;
+            for (; q < 2 * cnt; q += G) {
+                const int t = q >> 1, side = q & 1;
+                const bool fourteen = t >= u + l;
+                const int j = fourteen ? c14d[c14s[a] + t - u - l] : (t < u ? row[t] : row[cap - 1 - (t - u)]);
+                const int sj = slot(j);
+                if (sj >= 0 && j < a) continue;   // a pair of moved atoms, counted at its lower atom
+                double4_32a ai = pq[a], jj = pq[j];
+                if (side) {
+                    ai.x = s_xyz[3 * k]; ai.y = s_xyz[3 * k + 1]; ai.z = s_xyz[3 * k + 2];
+                    if (sj >= 0) { jj.x = s_xyz[3 * sj]; jj.y = s_xyz[3 * sj + 1]; jj.z = s_xyz[3 * sj + 2]; }
+                }
+                double e, v;
+                pair_energy<PREC_F64>(A, pbc, cut, fourteen, ai, f0, a, jj, f0, j, true, e, v);
+                del += side ? e : -e;
+                dvd += side ? v : -v;
+            }
+            base += cnt;
         }
         del = warp_sum(del);
         dvd = warp_sum(dvd);
@@ -1940,13 +1984,19 @@ __global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uin
         __syncthreads();
         if (tid == 0) {
             double se = 0.0, sv = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) { se += s_part[0][w]; sv += s_part[1][w]; }
+            for (int w = 0; w < NW; w++) { se += s_part[0][w]; sv += s_part[1][w]; }
+            for (int r = 0; r < RP_CL; r++) *cluster.map_shared_rank(&s_cl[rank], r) = make_double2(se, sv);
+        }
+        cluster.sync();
+        if (tid == 0) {
+            double se = 0.0, sv = 0.0;
+            for (int r = 0; r < RP_CL; r++) { se += s_cl[r].x; sv += s_cl[r].y; }
             const double de = CHGCHARMM * KCALTOIU * se + 4.0 * sv;
-            // MC_metropolis::apply_criterion (MC_metropolis.cpp:175-204)
+            // MC_metropolis::apply_criterion (MC_metropolis.cpp:175-204); exp is CUDA's (at most 1 ulp
+            // from the exact value) where the host loop calls glibc's: the two runs can part only on a
+            // uniform within an ulp of the threshold
             long long cur = s_cur;
             bool accepted;
-            // exp is CUDA's (at most 1 ulp from the exact value) where the host loop calls glibc's: the
-            // two runs can part only on a uniform within an ulp of the threshold
             if (de <= 2.220446049250313e-16) accepted = true;
             else accepted = rp_canonical(words, cur) < exp(-beta * de);
             S.cursor = cur;
@@ -1967,8 +2017,8 @@ __global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uin
             s_acc = accepted ? 1 : 0;
         }
         __syncthreads();
-        if (s_acc) {
-            for (int k = tid; k < m; k += blockDim.x) {
+        if (s_acc && rank == 0) {
+            for (int k = tid; k < m; k += RP_NT) {
                 const int a = s_idx[k];
                 double4_32a p = pq[a];
                 p.x = s_xyz[3 * k]; p.y = s_xyz[3 * k + 1]; p.z = s_xyz[3 * k + 2];
@@ -1977,10 +2027,11 @@ __global__ void __launch_bounds__(256) k_replay(AtomsDev A, double4_32a* pq, uin
                 f.x = to_fixed(p.x, pbc.rL[0]); f.y = to_fixed(p.y, pbc.rL[1]); f.z = to_fixed(p.z, pbc.rL[2]);
                 fx[a] = f;
             }
+            __threadfence();
         }
-        __syncthreads();
+        cluster.sync();   // the commit before the next step's reads; every CTA is past this step's sums
     }
-    if (tid == 0) *st = S;
+    if (tid == 0 && rank == 0) *st = S;
 }
 
 int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKind>& moves, double beta, int nsteps,
@@ -2041,8 +2092,8 @@ int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKin
         if (cudaMemcpyAsync(d_words, w.data(), sizeof(uint32_t) * (size_t)W, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
             cudaMemcpyAsync(d_st, &S, sizeof S, cudaMemcpyHostToDevice, stream) != cudaSuccess)
             return done(fail(MCG_ECUDA, "device run: upload"));
-        k_replay<<<1, 256, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
-                                        d_words, W, d_st, step, s1, beta);
+        k_replay<<<RP_CL, RP_NT, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
+                                              d_words, W, d_st, step, s1, beta);
         launches++;
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpyAsync(&S, d_st, sizeof S, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
