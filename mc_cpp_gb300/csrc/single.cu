@@ -2097,14 +2097,16 @@ int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKin
     T.ninst_all = (int)first.size();
     T.nranges = (int)ranges.size() / 2;
     std::vector<uint32_t> w((size_t)W);
+    std::vector<uint32_t> stash;     // the generator's next words, drawn while the previous launch ran
+    size_t stash_at = 0;
     long long filled = 0;
     int step = 0;
     while (step < nsteps) {
-        // the words not consumed yet, then fresh ones from the generator
+        // the words not consumed yet, then the generator's next ones (from the stash first)
         const long long keep = filled - S.cursor;
         if (keep > 0 && S.cursor > 0) std::memmove(w.data(), w.data() + S.cursor, sizeof(uint32_t) * (size_t)keep);
         filled = std::max(0LL, keep);
-        while (filled < W) w[(size_t)filled++] = gen();
+        while (filled < W) w[(size_t)filled++] = stash_at < stash.size() ? stash[stash_at++] : gen();
         S.cursor = 0;
         S.status = 0;
         const int s1 = std::min(nsteps, (step / 50 + 1) * 50);     // up to the next list update
@@ -2114,6 +2116,10 @@ int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKin
         k_replay<<<RP_CL, RP_NT, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
                                               d_words, W, d_st, step, s1, beta);
         launches++;
+        // while the launch runs: the next W words of the generator, in order, for the next buffer
+        stash.erase(stash.begin(), stash.begin() + (long)stash_at);
+        stash_at = 0;
+        while ((long long)stash.size() < W) stash.push_back(gen());
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpyAsync(&S, d_st, sizeof S, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
             cudaStreamSynchronize(stream) != cudaSuccess)
