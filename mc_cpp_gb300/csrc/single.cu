@@ -1840,12 +1840,19 @@ __device__ __forceinline__ double rp_wrap(double v, double L, double rL) {
 //    the next step's reads.
 // The launch's random words, and the move-instance tables when they fit, are copied into each
 // CTA's shared memory first: the proposal's loads are then shared-memory loads, not L2 round trips.
+// While the four warps of a CTA take the dE terms, a fifth forms the next step's uniforms: the next
+// step's words start at this step's post-proposal cursor, or 2 words later when this step draws an
+// acceptance uniform, so 27 uniforms from that cursor cover both cases; the warp forms both cases'
+// move type, instance and RP_TRIES unit-ball tries.  The next proposal picks the case its cursor
+// matches and only scales, orders and wraps; when none of those tries lies in the ball it goes on
+// with the following ones as before.  The same operations on the same words: the same proposals.
 // Measured on the 864-atom argon box (moves per second, host work included): 49.8k with one
 // 256-thread CTA (its ~200 dE terms at two warps per scheduler), 89.9k with the cluster and the
 // words read from global memory, 94.8k with them in shared memory.
 constexpr int RP_CL = 8;
 constexpr int RP_NT = 128;
 constexpr int RP_TRIES = 8;
+constexpr int RP_SPEC = 32;            // a fifth warp: the next step's uniforms, formed during this step's dE
 constexpr int RP_WORDS = 8192;        // random words of one launch, staged in each CTA's shared memory
 constexpr int RP_TAB = 3072;          // ints of the instance tables staged with them when they fit
 
@@ -1854,7 +1861,7 @@ __device__ __forceinline__ double rp_canonical_at(const uint32_t* __restrict__ w
     return rp_canonical(w, cur);
 }
 
-__global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
+__global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT + RP_SPEC)
     k_replay(AtomsDev A, double4_32a* pq, uint4* fx, PbcDev pbc, CutDev cut, const int* __restrict__ nbr,
              const int* __restrict__ nup, const int* __restrict__ nlo, int cap, const int* __restrict__ c14s,
              const int* __restrict__ c14d, ReplayTables T, const uint32_t* __restrict__ words, long long nwords,
@@ -1871,15 +1878,20 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
     __shared__ double2 s_cl[RP_CL];
     __shared__ __align__(16) uint32_t s_words[RP_WORDS];
     __shared__ int s_tab[RP_TAB];
+    // the next step's uniforms, both cases (0: no acceptance draw in this step, 1: one)
+    __shared__ double s_sx[2 * RP_TRIES], s_sy[2 * RP_TRIES], s_sz[2 * RP_TRIES], s_sq[2 * RP_TRIES];
+    __shared__ int s_st[2], s_sg[2], s_sok;
+    __shared__ long long s_sbase;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = RP_NT / 32, G = RP_CL * RP_NT;
-    for (int i = tid; i < (int)(nwords >> 2); i += RP_NT)
+    for (int i = tid; i < (int)(nwords >> 2); i += blockDim.x)
         reinterpret_cast<uint4*>(s_words)[i] = reinterpret_cast<const uint4*>(words)[i];
     const bool tab_sh = T.ninst_all + 2 * T.nranges <= RP_TAB;
     if (tab_sh) {
-        for (int i = tid; i < T.ninst_all; i += RP_NT) s_tab[i] = T.inst_first[i];
-        for (int i = tid; i < 2 * T.nranges; i += RP_NT) s_tab[T.ninst_all + i] = T.ranges[i];
+        for (int i = tid; i < T.ninst_all; i += blockDim.x) s_tab[i] = T.inst_first[i];
+        for (int i = tid; i < 2 * T.nranges; i += blockDim.x) s_tab[T.ninst_all + i] = T.ranges[i];
     }
+    if (tid == 0) s_sok = 0;
     const int* inst_first = tab_sh ? s_tab : T.inst_first;
     const int* ranges = tab_sh ? s_tab + T.ninst_all : T.ranges;
     const int rank = (int)cluster.block_rank();
@@ -1893,12 +1905,20 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
             const long long cur = S.cursor;
             bool out = cur + 256 > nwords;
             int t = 0, m = 0, first = -1;
+            int sv = -1;   // the case of the uniforms formed during the previous step that matches cur
+            if (!out && s_sok) sv = cur == s_sbase ? 0 : (cur == s_sbase + 2 ? 1 : -1);
             if (!out) {
-                double u = 0.0;
-                if (lane < 2) u = rp_canonical_at(s_words, cur + 2 * lane);
-                const double u0 = __shfl_sync(0xffffffffu, u, 0), u1 = __shfl_sync(0xffffffffu, u, 1);
-                t = (int)__dmul_rn((double)T.nmvtyp, u0);
-                const int g = T.ibase[t] + (int)__dmul_rn((double)T.ninst[t], u1);
+                int g;
+                if (sv >= 0) {
+                    t = s_st[sv];
+                    g = s_sg[sv];
+                } else {
+                    double u = 0.0;
+                    if (lane < 2) u = rp_canonical_at(s_words, cur + 2 * lane);
+                    const double u0 = __shfl_sync(0xffffffffu, u, 0), u1 = __shfl_sync(0xffffffffu, u, 1);
+                    t = (int)__dmul_rn((double)T.nmvtyp, u0);
+                    g = T.ibase[t] + (int)__dmul_rn((double)T.ninst[t], u1);
+                }
                 if (lane == 0) {
                     for (int r = inst_first[g]; r < inst_first[g + 1]; r++)
                         for (int a = ranges[2 * r]; a <= ranges[2 * r + 1]; a++) {
@@ -1907,7 +1927,21 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
                         }
                 }
                 m = __shfl_sync(0xffffffffu, m, 0);
-                for (int pass = 0; first < 0; pass++) {
+                int pass0 = 0;
+                if (sv >= 0) {   // the first RP_TRIES tries, formed in advance
+                    const unsigned ok = __ballot_sync(0xffffffffu, lane < RP_TRIES && s_sq[sv * RP_TRIES + lane] <= 1.0);
+                    if (ok) {
+                        const int k = __ffs(ok) - 1;
+                        first = k;
+                        if (lane == k) {
+                            const double dm = S.dmax[t];
+                            const int e = sv * RP_TRIES + k;
+                            s_r[0] = __dmul_rn(s_sx[e], dm); s_r[1] = __dmul_rn(s_sy[e], dm); s_r[2] = __dmul_rn(s_sz[e], dm);
+                        }
+                    }
+                    pass0 = 1;
+                }
+                for (int pass = pass0; first < 0; pass++) {
                     const long long cb = cur + 4 + 6LL * RP_TRIES * pass;
                     if (cb + 6LL * RP_TRIES + 2 > nwords) { out = true; break; }   // the pass and the acceptance draw
                     double v = 0.0;
@@ -1954,6 +1988,30 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
         }
         __syncthreads();
         if (s_stop) break;   // the same in every CTA: each formed the same proposal from the same words
+        if (warp == NW) {
+            // the next step's uniforms (words from b = this step's post-proposal cursor): type and
+            // instance of case v from uniforms v and v + 1, try k from v + 2 + 3k .. v + 4 + 3k
+            const long long b = s_cur;
+            const bool ok = b + 54 <= nwords;
+            double c = 0.0;
+            if (ok && lane < 27) c = rp_canonical_at(s_words, b + 2 * lane);
+            const double cn = __shfl_sync(0xffffffffu, c, (lane + 1) & 31);
+            if (lane < 2) {
+                const int tv = (int)__dmul_rn((double)T.nmvtyp, c);
+                s_st[lane] = tv;
+                s_sg[lane] = T.ibase[tv] + (int)__dmul_rn((double)T.ninst[tv], cn);
+            }
+            const int i0 = (lane >> 3) + 2 + 3 * (lane & 7);
+            const double cx = __shfl_sync(0xffffffffu, c, i0 & 31), cy = __shfl_sync(0xffffffffu, c, (i0 + 1) & 31),
+                         cz = __shfl_sync(0xffffffffu, c, (i0 + 2) & 31);
+            if (lane < 2 * RP_TRIES) {
+                const double x = __dadd_rn(__dmul_rn(cx, 2.0), -1.0), y = __dadd_rn(__dmul_rn(cy, 2.0), -1.0),
+                             z = __dadd_rn(__dmul_rn(cz, 2.0), -1.0);
+                s_sx[lane] = x; s_sy[lane] = y; s_sz[lane] = z;
+                s_sq[lane] = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+            }
+            if (lane == 0) { s_sbase = b; s_sok = ok ? 1 : 0; }
+        }
         // dE of the moved set over its Verlet partners and 1-4 pairs, FP64 (as k_delta_e): term
         // (k, t, side) of the moved atoms' partner lists, numbered in list order, goes to the thread
         // whose gslot it equals modulo G; side 0 is the old pair energy (subtracted), 1 the new
@@ -1970,7 +2028,7 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
         double del = 0.0, dvd = 0.0;
         const uint4 f0 = make_uint4(0, 0, 0, 0);
         int base = 0;
-        for (int k = 0; k < m; k++) {
+        for (int k = 0; k < m && warp < NW; k++) {
             const int a = s_idx[k];
             const int* row = nbr + (size_t)a * cap;
             const int u = nup[a], l = nlo[a], n14 = c14s[a + 1] - c14s[a];
@@ -1997,7 +2055,7 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
         }
         del = warp_sum(del);
         dvd = warp_sum(dvd);
-        if (lane == 0) { s_part[0][warp] = del; s_part[1][warp] = dvd; }
+        if (lane == 0 && warp < NW) { s_part[0][warp] = del; s_part[1][warp] = dvd; }
         __syncthreads();
         if (tid == 0) {
             double se = 0.0, sv = 0.0;
@@ -2035,7 +2093,7 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT)
         }
         __syncthreads();
         if (s_acc && rank == 0) {
-            for (int k = tid; k < m; k += RP_NT) {
+            for (int k = tid; k < m; k += blockDim.x) {
                 const int a = s_idx[k];
                 double4_32a p = pq[a];
                 p.x = s_xyz[3 * k]; p.y = s_xyz[3 * k + 1]; p.z = s_xyz[3 * k + 2];
@@ -2113,7 +2171,7 @@ int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKin
         if (cudaMemcpyAsync(d_words, w.data(), sizeof(uint32_t) * (size_t)W, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
             cudaMemcpyAsync(d_st, &S, sizeof S, cudaMemcpyHostToDevice, stream) != cudaSuccess)
             return done(fail(MCG_ECUDA, "device run: upload"));
-        k_replay<<<RP_CL, RP_NT, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
+        k_replay<<<RP_CL, RP_NT + RP_SPEC, 0, stream>>>(atoms(), d_pq, d_fx, pbc, cut, d_nbr, d_nup, d_nlo, cap, d_c14s, d_c14d, T,
                                               d_words, W, d_st, step, s1, beta);
         launches++;
         // while the launch runs: the next W words of the generator, in order, for the next buffer
