@@ -2110,16 +2110,35 @@ int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out) {
     return MCG_OK;
 }
 
+// The device address of a pinned (page-locked) host buffer, or null for any other pointer: the
+// import and export kernels then read and write the host buffer themselves over the coherent
+// host link, without a staging copy through device memory.
+static const double* pinned_alias(const double* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();   // an unregistered pointer: not an error of this call
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? (const double*)at.devicePointer : nullptr;
+}
+
 int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* xyz_out, int64_t* accepted, double* etot) {
     if (!b || nsweeps < 0) return fail(MCG_EINVAL, "bad arguments");
     const size_t bytes = sizeof(double) * 3 * (size_t)b->natoms;
     int r;
-    if ((xyz_in || xyz_out) && !b->d_xyz) { if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r; }
+    const double* in_dev = xyz_in ? pinned_alias(xyz_in) : nullptr;
+    double* out_dev = xyz_out ? const_cast<double*>(pinned_alias(xyz_out)) : nullptr;
+    if (((xyz_in && !in_dev) || (xyz_out && !out_dev)) && !b->d_xyz) {
+        if ((r = balloc(&b->d_xyz, 3 * (size_t)b->natoms))) return r;
+    }
     if (xyz_in && !b->d_changed && (r = balloc(&b->d_changed, (size_t)b->nchains + 1))) return r;
     if (xyz_in) {
-        BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
+        if (!in_dev) {
+            BK(cudaMemcpyAsync(b->d_xyz, xyz_in, bytes, cudaMemcpyHostToDevice, b->stream));
+            in_dev = b->d_xyz;
+        }
         BK(cudaMemsetAsync(b->d_changed, 0, sizeof(int) * ((size_t)b->nchains + 1), b->stream));
-        k_batch_import<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, b->d_xyz, b->natoms, b->d_M,
+        k_batch_import<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, in_dev, b->natoms, b->d_M,
                                                                                   b->d_F, b->d_FB, b->d_state,
                                                                                   b->d_changed, b->nchains);
         BK(cudaGetLastError());
@@ -2130,11 +2149,11 @@ int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* 
     }
     if ((r = mcg_batch_sweep(b, nsweeps))) return r;
     if (xyz_out) {
-        k_batch_export<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, b->d_M, b->natoms, b->d_xyz,
-                                                                                  b->nchains);
+        k_batch_export<<<dim3(b->nchains, b->atom_slices()), 256, 0, b->stream>>>(b->d_chains, b->d_M, b->natoms,
+                                                                                  out_dev ? out_dev : b->d_xyz, b->nchains);
         BK(cudaGetLastError());
         b->launches++;
-        BK(cudaMemcpyAsync(xyz_out, b->d_xyz, bytes, cudaMemcpyDeviceToHost, b->stream));
+        if (!out_dev) BK(cudaMemcpyAsync(xyz_out, b->d_xyz, bytes, cudaMemcpyDeviceToHost, b->stream));
     }
     return mcg_batch_stats(b, nullptr, accepted, etot);
 }

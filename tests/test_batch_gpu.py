@@ -435,3 +435,26 @@ def test_checkpoint_rejects_other_batches_and_damaged_files(tmp_path):
     t0 = A.stats()[0]
     A.sweep(1)
     assert (A.stats()[0] > t0).all()
+
+
+def test_host_buffer_run_from_pinned_memory_equals_pageable():
+    """With page-locked host buffers the import and export kernels read and write them directly
+    (no staging copy); the result is bitwise the staged run from ordinary (pageable) buffers:
+    exported coordinates, running energies and accepted counts, step after step."""
+    torch = pytest.importorskip("torch")
+    ch = _waters((600, 900, 700), seed=41)
+    P = BatchChains(ch, seed=18)
+    Q = BatchChains(ch, seed=18)
+    n = P.natoms
+    pin_in = torch.empty((3, n), dtype=torch.float64, pin_memory=True).numpy()
+    pin_out = torch.empty((3, n), dtype=torch.float64, pin_memory=True).numpy()
+    out = np.zeros((3, n))
+    P.run_host(None, 0, pin_out)
+    Q.run_host(None, 0, out)
+    assert np.array_equal(pin_out, out)
+    for _ in range(3):
+        pin_in[...] = pin_out
+        ap, ep = P.run_host(pin_in, 1, pin_out)
+        aq, eq = Q.run_host(out.copy(), 1, out)
+        assert np.array_equal(pin_out, out)
+        assert np.array_equal(ap, aq) and np.array_equal(ep, eq)
