@@ -308,7 +308,9 @@ int mcg_batch_get_tuning(mcg_batch* b, mcg_batch_tuning* out);
  * energy recomputed, while a chain given back exactly the coordinates of the last export is left
  * as it is (the FP64 view of a 64-bit fixed-point coordinate converts back to a different one, so
  * this keeps the chain's state exact); run nsweeps sweeps; when xyz_out != NULL copy the
- * coordinates back; fill accepted and etot (nchains entries each, may be NULL).  Host-synchronous. */
+ * coordinates back; fill accepted and etot (nchains entries each, may be NULL).  Page-locked
+ * buffers (cudaHostAlloc, cudaHostRegister) are read and written by the device directly; other
+ * host buffers go through a device staging copy.  Host-synchronous. */
 int mcg_batch_run_host(mcg_batch* b, const double* xyz_in, int nsweeps, double* xyz_out, int64_t* accepted,
                        double* etot);
 /* Mixed-precision recompute of every chain's energy over its neighbour lists (iu). */
