@@ -140,6 +140,8 @@ int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int6
  * at the current coordinates (FP64 minimum-image distances).  Full: both are the number of pairs
  * the full energy sums (every pair i < j outside the exclusion rows). */
 int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff);
+/* Kernel launches issued by the handle so far (an addition without a reference counterpart). */
+int mcg_kernel_launches(mcg_system* s, int64_t* launches);
 /* Device time (ms, CUDA events on the handle's stream) of reps launches of the switched
  * nonbonded pair kernel alone over the current list (switch mode). */
 int mcg_time_nonbonded(mcg_system* s, int reps, float* ms);

@@ -179,6 +179,12 @@ int mcg_get_pairlist(mcg_system* s, int* counts, int* entries, int64_t cap, int6
     return s->eng.get_pairlist(counts, entries, cap, total);
 }
 
+int mcg_kernel_launches(mcg_system* s, int64_t* launches) {
+    if (!s || !launches) return fail(MCG_EINVAL, "null argument");
+    *launches = s->eng.launches;
+    return MCG_OK;
+}
+
 int mcg_pair_count(mcg_system* s, int64_t* list_pairs, int64_t* in_cutoff) {
     if (!s || !list_pairs || !in_cutoff) return fail(MCG_EINVAL, "null argument");
     const HostSystem& h = s->eng.hs;
@@ -339,11 +345,13 @@ static int metropolis_impl(mcg_system* s, int nsteps, uint64_t seed, int accepta
     // Without per-step output, translation moves of atom sets that carry no bonded term in a
     // periodic switched FP64 system run on the device, a launch per list-update period, on the same
     // random words (SingleEngine::metropolis_device), when its limits hold (at most 8 move types, 64
-    // atoms a move, checked before the first step); every other run takes the host loop below.
+    // atoms a move, and a cluster of its 8 CTAs resident on the device, checked before the first
+    // step); every other run takes the host loop below.
     bool all_trn = true;
     for (const MoveKind& mk : s->moves) all_trn = all_trn && mk.type == MCG_MOVE_TRN;
     if (!trace && !follow && save_each == 0 && all_trn && h.cut == MCG_CUT_SWITCH && h.pbc != MCG_PBC_NONE &&
-        h.prec == MCG_PREC_FP64 && !E.has_bonded_terms() && SingleEngine::replay_fits(s->moves)) {
+        h.prec == MCG_PREC_FP64 && !E.has_bonded_terms() && SingleEngine::replay_fits(s->moves) &&
+        SingleEngine::replay_cluster_ok()) {
         rc = E.metropolis_device(gen, s->moves, beta, nsteps, &etot, &acc);
         if (rc) return rc;
         if (final_etot) *final_etot = etot;

@@ -2109,6 +2109,19 @@ __global__ void __cluster_dims__(RP_CL, 1, 1) __launch_bounds__(RP_NT + RP_SPEC)
     if (tid == 0 && rank == 0) *st = S;
 }
 
+bool SingleEngine::replay_cluster_ok() {
+    static int ok = -1;
+    if (ok < 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(RP_CL);
+        cfg.blockDim = dim3(RP_NT + RP_SPEC);
+        int nclusters = 0;
+        ok = cudaOccupancyMaxActiveClusters(&nclusters, k_replay, &cfg) == cudaSuccess && nclusters >= 1 ? 1 : 0;
+        if (!ok) cudaGetLastError();
+    }
+    return ok == 1;
+}
+
 int SingleEngine::metropolis_device(std::mt19937& gen, const std::vector<MoveKind>& moves, double beta, int nsteps,
                                     double* etot, int64_t* n_accepted) {
     const int nt = (int)moves.size();

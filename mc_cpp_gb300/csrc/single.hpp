@@ -36,6 +36,8 @@ public:
     static constexpr int kReplayMaxTypes = 8, kReplayMaxAtoms = 64;
     // every instance of every move within kReplayMaxAtoms atoms (and at most kReplayMaxTypes types)
     static bool replay_fits(const std::vector<MoveKind>& moves);
+    // the device run's cluster can be resident on this device (checked once per process)
+    static bool replay_cluster_ok();
     // true when the pending proposal moves exactly atoms[0..m) (ascending) to x/y/z[atoms[k]]
     bool pending_matches(int m, const int* atoms, const double* x, const double* y, const double* z) const;
     int get_pairlist(int* counts, int* entries, int64_t cap, int64_t* total);

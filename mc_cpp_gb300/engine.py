@@ -108,6 +108,12 @@ class FFieldCUDA:
         native.check(native.lib().mcg_time_nonbonded(self.h, reps, C.byref(ms)))
         return ms.value
 
+    def kernel_launches(self) -> int:
+        """Kernel launches issued by this handle so far."""
+        v = C.c_int64(0)
+        native.check(native.lib().mcg_kernel_launches(self.h, C.byref(v)))
+        return v.value
+
     def time_nonbonded_flushed(self, reps: int) -> float:
         """Device ms of reps launches of the switched pair kernel, the L2 cache flushed before each."""
         ms = C.c_float(0)

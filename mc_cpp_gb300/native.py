@@ -139,6 +139,7 @@ def lib():
         "mcg_pair_count": (C.c_int, [P, _i64, _i64]),
         "mcg_time_nonbonded": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
         "mcg_time_nonbonded_flushed": (C.c_int, [P, C.c_int, C.POINTER(C.c_float)]),
+        "mcg_kernel_launches": (C.c_int, [P, _i64]),
         "mcg_set_pair_kernel": (C.c_int, [P, C.c_int]),
         "mcg_get_pair_kernel": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "mcg_cluster_stats": (C.c_int, [P, _i64, _i64, _i64]),

@@ -50,6 +50,7 @@ def test_null_handles_rejected_on_host():
     assert L.mcg_prune_stats(None, C.byref(i64), C.byref(i64), C.byref(f32)) == native.MCG_EINVAL
     assert L.mcg_set_pair_kernel(None, 0) == native.MCG_EINVAL
     assert L.mcg_time_nonbonded_flushed(None, 1, C.byref(f32)) == native.MCG_EINVAL
+    assert L.mcg_kernel_launches(None, C.byref(i64)) == native.MCG_EINVAL
     assert L.mcg_cluster_stats(None, C.byref(i64), C.byref(i64), C.byref(i64)) == native.MCG_EINVAL
     assert L.mcg_group_stats(None, C.byref(i64), C.byref(i64), C.byref(i64)) == native.MCG_EINVAL
     d = C.c_double(0)

@@ -286,8 +286,13 @@ def test_device_metropolis_run_equals_the_host_loop():
     s = goldens.system("argon864")
     dev = FFieldCUDA(s, "fp64")
     host = FFieldCUDA(s, "fp64")
+    l_dev, l_host = dev.kernel_launches(), host.kernel_launches()
     _, e_dev, a_dev, _ = dev.metropolis(3000, 99, trace=False)
     _, e_host, a_host, _ = host.metropolis(3000, 99, trace=True)
+    # the device run takes a launch per 50 steps (and the list builds between), the host loop at
+    # least one per step: the run without a trace did run on the device
+    l_dev, l_host = dev.kernel_launches() - l_dev, host.kernel_launches() - l_host
+    assert l_dev < 3000 // 4 and l_host >= 3000, (l_dev, l_host)
     assert a_dev == a_host
     assert np.array_equal(dev.coords(), host.coords())
     assert abs(e_dev - e_host) <= 1e-10 * abs(e_host)
